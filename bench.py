@@ -1,0 +1,354 @@
+"""Benchmark of the particle-kernel direct sums on GB300.
+
+Workload (one "step"): the mixed-precision (digits = 10) direct sums of
+Laplace3D_DxU, Stokes3D_FxU and Stokes3D_DxU over 2^20 sources uniform on the
+unit sphere (outward normals) and 2^20 targets uniform in the radius-2 ball,
+densities N(0,1) -- 3 * 2^40 interactions.  Inputs are seeded synthetic data
+(no dataset exists for this path).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` = whole-job Ginteractions/s with inputs
+resident in HBM; `e2e` = the same through the public host-array API with the
+host<->device copies inside the timed region; `roofline` = the dominant
+kernel's interactions/s against the FP32-issue roofline; `cpu_baseline` = the
+reference's algorithm (the CPU oracle) on this host's cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+KERNELS = [1, 2, 3]  # Laplace3D_DxU, Stokes3D_FxU, Stokes3D_DxU
+NAMES = {0: "Laplace3D_FxU", 1: "Laplace3D_DxU", 2: "Stokes3D_FxU", 3: "Stokes3D_DxU"}
+# Algorithmic FP32-pipe ops + MUFU ops per interaction (formulas of kernel_functions.hpp,
+# excluding Newton refinement and masking) and the reference's own FLOPS() counters.
+ALG_OPS = {0: (7, 1), 1: (13, 1), 2: (18, 1), 3: (20, 1)}
+REF_FLOPS = {0: 6, 1: 14, 2: 23, 3: 26}
+N_SRC = N_TRG = 1 << 20
+DIGITS = 10
+SMS = 152
+FP32_LANES = 128
+MUFU_PER_SM = 16
+
+
+def peaks():
+    p = {}
+    try:
+        p = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    return p
+
+
+def roofline_peak_int_s(kernel, sm_mhz):
+    ops, mufu = ALG_OPS[kernel]
+    per_clk = min(FP32_LANES / ops, MUFU_PER_SM / mufu)
+    return SMS * sm_mhz * 1e6 * per_clk
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thr = threading.Thread(target=self._read, daemon=True)
+            self.thr.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_baseline(threads=0, n_trg=4096, kernels=KERNELS):
+    """The reference's algorithm on this host (oracle port, FP64, OpenMP), bounded sample."""
+    from oracle import oracle as O
+    from sctl_gb300 import workloads as W
+    pairs, secs = 0, 0.0
+    for k in kernels:
+        d = W.sphere_ball(N_SRC, n_trg, k, seed=100 + k)
+        t0 = time.perf_counter()
+        O.eval(k, d["r_trg"], d["r_src"], d["n_src"], d["v_src"], nthreads=threads)
+        secs += time.perf_counter() - t0
+        pairs += N_SRC * n_trg
+    cores = threads if threads > 0 else O.max_threads()
+    return {"value": pairs / secs / 1e9, "unit": "Ginteractions/s", "cores": cores, "kind": "port",
+            "sample": f"{n_trg} targets x 2^20 sources per kernel, kernels {[NAMES[k] for k in kernels]}, FP64 "
+                      f"(oracle/sctl_oracle.c restating generic-kernel.txx Eval), {secs:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    n_trg = 2048
+    samples = []
+    for _ in range(args.warmup):
+        cpu_baseline(n_trg=n_trg // 4)
+    for _ in range(args.steps):
+        samples.append(cpu_baseline(n_trg=n_trg))
+    val = statistics.median(s["value"] for s in samples)
+    cb = dict(samples[-1])
+    cb["value"] = val
+    line = {"impl": "reference", "metric": "Laplace/Stokes Ginteractions/s mixed vs FP64 @1e-10", "value": val,
+            "unit": "Ginteractions/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "sphere_ball 2^20 src x 2^20 trg, Laplace3D_DxU + Stokes3D_FxU + Stokes3D_DxU, "
+                                   "digits 10", "sample_per_step": f"{n_trg} targets x 2^20 sources per kernel"},
+            "cpu_baseline": cb,
+            "e2e": {"value": val, "unit": "Ginteractions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n", type=int, default=N_TRG, help="targets per rank (sources fixed at 2^20)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+
+    import sctl_gb300 as S
+    from sctl_gb300 import capi
+    from sctl_gb300 import workloads as W
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    capi.load()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+
+    # Resident inputs (each rank: its own 2^20 targets against the 2^20 sources).
+    data = {}
+    for k in KERNELS:
+        d = W.sphere_ball(N_SRC, args.n, k, seed=rank * 16 + k)
+        data[k] = {a: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for a, v in d.items()}
+        data[k]["out"] = torch.empty(args.n * (3 if k >= 2 else 1), dtype=torch.float64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step(mode="mixed", digits=DIGITS, timing=None):
+        for k in KERNELS:
+            d = data[k]
+            S.eval_device(k, capi.MODE_IDS[mode], digits, args.n, d["r_trg"].data_ptr(), N_SRC,
+                          d["r_src"].data_ptr(), d["n_src"].data_ptr() if d["n_src"].numel() else 0,
+                          d["v_src"].data_ptr(), d["out"].data_ptr(), False, stream.cuda_stream)
+            if timing is not None:
+                timing.setdefault(k, []).append(capi.last_kernel_ms())
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    capi.set_timing(True)
+    kern_ms = {}
+    n0 = capi.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        barrier()
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            step(timing=kern_ms)
+            ev[i][1].record(stream)
+        barrier()
+    launches = capi.launch_count() - n0
+    capi.set_timing(False)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    pairs_step = len(KERNELS) * N_SRC * args.n
+    value = pairs_step * world / (ms * 1e-3) / 1e9
+    clocks = clk.summary()
+
+    # --- everything below is outside the timed region ---
+    # FP64 and FP32 plain forms on a 2^16-target slice, for the "mixed vs FP64" ratio.
+    detail = {}
+    sub = min(args.n, 1 << 16)
+    for k in KERNELS:
+        d = data[k]
+        row = {"mixed_ms_per_launch": statistics.median(kern_ms[k]),
+               "mixed_gint_s": N_SRC * args.n / (statistics.median(kern_ms[k]) * 1e-3) / 1e9}
+        for mode, dg in (("f64", -1), ("f32", -1), ("mixed", 10)):
+            r_trg = d["r_trg"][:sub * 3] if mode != "f32" else d["r_trg"][:sub * 3].float()
+            args_ = [d[a] if mode != "f32" else d[a].float() for a in ("r_src", "n_src", "v_src")]
+            out = torch.empty(sub * (3 if k >= 2 else 1), dtype=torch.float32 if mode == "f32" else torch.float64,
+                              device=dev)
+            capi.set_timing(True)
+            t = []
+            for _ in range(2):
+                S.eval_device(k, capi.MODE_IDS[mode], dg, sub, r_trg.data_ptr(), N_SRC, args_[0].data_ptr(),
+                              args_[1].data_ptr() if args_[1].numel() else 0, args_[2].data_ptr(), out.data_ptr(),
+                              False, stream.cuda_stream)
+                t.append(capi.last_kernel_ms())
+            capi.set_timing(False)
+            row[f"{mode}_d{dg}_gint_s_slice"] = N_SRC * sub / (min(t) * 1e-3) / 1e9
+        row["mixed_vs_f64"] = row["mixed_d10_gint_s_slice"] / row["f64_d-1_gint_s_slice"]
+        ops, mufu = ALG_OPS[k]
+        peak = roofline_peak_int_s(k, peaks().get("sm_max_mhz", 2070.0))
+        row["roofline_frac_fp32_issue"] = row["mixed_gint_s"] * 1e9 / peak
+        detail[NAMES[k]] = row
+
+    # Accuracy vs the FP64 oracle on 256 targets per kernel.
+    from oracle import oracle as O
+    for k in KERNELS:
+        d = data[k]
+        idx = slice(0, 256)
+        host = {a: d[a].cpu().numpy() for a in ("r_trg", "r_src", "n_src", "v_src")}
+        ref = O.eval(k, host["r_trg"].reshape(-1, 3)[idx], host["r_src"], host["n_src"], host["v_src"])
+        got = d["out"].cpu().numpy().reshape(args.n, -1)[idx].reshape(-1)
+        detail[NAMES[k]]["rel_l2_vs_fp64_oracle"] = O.rel_l2(got, ref)
+        detail[NAMES[k]]["max_rel_vs_fp64_oracle"] = O.max_rel(got, ref)
+
+    # End to end through the public host-array API (pinned host buffers, copies inside the timed region).
+    host_in = {}
+    h2d = d2h = 0
+    for k in KERNELS:
+        hk = {}
+        for a in ("r_trg", "r_src", "n_src", "v_src"):
+            t = torch.empty(data[k][a].shape, dtype=torch.float64, pin_memory=True)
+            t.copy_(data[k][a].cpu())
+            hk[a] = t.numpy()
+            h2d += t.numel() * 8
+        hk["out"] = torch.empty(data[k]["out"].shape, dtype=torch.float64, pin_memory=True).numpy()
+        d2h += hk["out"].size * 8
+        host_in[k] = hk
+    kern_objs = {1: S.Laplace3D_DxU, 2: S.Stokes3D_FxU, 3: S.Stokes3D_DxU}
+    e2e_steps = max(1, min(2, args.steps))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for k in KERNELS:
+            h = host_in[k]
+            h["out"][:] = 0
+            kern_objs[k].Eval(h["out"], h["r_trg"], h["r_src"], h["n_src"], h["v_src"], digits=DIGITS, mode="mixed")
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": pairs_step * world / e2e_s / 1e9, "unit": "Ginteractions/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h}
+
+    dom = max(KERNELS, key=lambda k: statistics.median(kern_ms[k]))
+    dom_ms = statistics.median(kern_ms[dom])
+    pk = peaks()
+    sm_max = pk.get("sm_max_mhz", 2070.0)
+    peak_int = roofline_peak_int_s(dom, sm_max)
+    achieved = N_SRC * args.n / (dom_ms * 1e-3)
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(NAMES[dom])
+        except Exception:
+            traffic = None
+    roofline = {"bound": "fp32_issue", "kernel": f"direct_sum_kernel<{NAMES[dom]}, mixed double-float>",
+                "achieved": achieved / 1e9, "peak": peak_int / 1e9, "unit": "Ginteractions/s",
+                "frac": achieved / peak_int, "traffic": traffic,
+                "peak_basis": f"{SMS} SMs x {sm_max:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json) x "
+                              f"min({FP32_LANES} FP32 lanes / {ALG_OPS[dom][0]} ops, {MUFU_PER_SM} MUFU / "
+                              f"{ALG_OPS[dom][1]}) per interaction (of measured clock; lanes and MUFU rate nominal)",
+                "achieved_fp32_tflops_equiv": achieved * (ALG_OPS[dom][0]) / 1e12,
+                "launch_ms": dom_ms}
+
+    line = {"metric": "Laplace/Stokes Ginteractions/s mixed vs FP64 @1e-10", "value": value,
+            "unit": "Ginteractions/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+df (double-float) from f64 inputs", "data": "synthetic (seeded PCG64)",
+            "config": {"workload": f"sphere_ball: 2^20 sources on the unit sphere x {args.n} targets in the "
+                                   f"radius-2 ball per GPU; Laplace3D_DxU + Stokes3D_FxU + Stokes3D_DxU; mixed "
+                                   f"precision, digits {DIGITS}",
+                       "interactions_per_step_per_gpu": pairs_step, "parallelism": f"replicas x{world}",
+                       "l2": "256 MB buffer written between timed steps; per-step inputs 0.4 GB > 129 MB L2"},
+            "gpu_launches": launches, "clocks": clocks, "e2e": e2e, "roofline": roofline,
+            "per_kernel": detail}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,141 @@
+/*
+ * sctlgpu -- GB300 (sm_103a) particle-kernel direct sums behind a C ABI.
+ *
+ * Drop-in for the hot path of SCTL's GenericKernel (include/sctl/generic-kernel.hpp):
+ * the Eval / KernelMatrix direct sums for Laplace3D_FxU, Laplace3D_DxU,
+ * Stokes3D_FxU and Stokes3D_DxU (include/sctl/kernel_functions.hpp:32-218).
+ *
+ * Conventions (identical to the reference unless stated):
+ *   - coordinates, normals and densities are array-of-structures, exactly as
+ *     SCTL's Vector<Real> holds them: r_trg[nt*3], r_src[ns*3], n_src[ns*3]
+ *     (only for kernels with NormalDim()==3), v_src[ns*SrcDim], v_trg[nt*TrgDim];
+ *   - pairs with r^2 == 0 contribute nothing (the approx_rsqrt mask);
+ *   - the kernel's scale factor (1/4pi, 1/4pi, 1/8pi, 3/4pi) is applied once
+ *     after summation;
+ *   - digits follows the reference: -1 (or >= 16) means full precision of the
+ *     arithmetic type, otherwise the number of significant digits requested;
+ *   - errors are returned as status codes (the reference aborts through
+ *     SCTL_ASSERT; the C++ shim in sctlgpu.hpp restores that behaviour).
+ *
+ * Pointers are host pointers unless SCTLGPU_DEVICE_PTRS is set.  With host
+ * pointers the call is synchronous (copies in, computes, copies out).  With
+ * device pointers the work is enqueued on `stream` (a cudaStream_t, or NULL
+ * for the legacy default stream) and the call returns without synchronising.
+ * All entry points are thread-safe.
+ */
+#ifndef SCTLGPU_H_
+#define SCTLGPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SCTLGPU_VERSION 1
+
+/* Kernel ids: the micro-kernels of kernel_functions.hpp (aliases at :677-678, :669-670). */
+enum sctlgpu_kernel {
+  SCTLGPU_LAPLACE3D_FXU = 0, /* sctl::Laplace3D_FxU  kernel_functions.hpp:32-59   */
+  SCTLGPU_LAPLACE3D_DXU = 1, /* sctl::Laplace3D_DxU  kernel_functions.hpp:61-79   */
+  SCTLGPU_STOKES3D_FXU = 2,  /* sctl::Stokes3D_FxU   kernel_functions.hpp:125-178 */
+  SCTLGPU_STOKES3D_DXU = 3   /* sctl::Stokes3D_DxU   kernel_functions.hpp:180-218 */
+};
+
+/* Arithmetic modes. */
+enum sctlgpu_mode {
+  SCTLGPU_F64 = 0,   /* Real = double: FP64 arithmetic throughout (GenericKernel<...>::Eval<double,...>). */
+  SCTLGPU_F32 = 1,   /* Real = float:  FP32 arithmetic throughout (GenericKernel<...>::Eval<float,...>).  */
+  SCTLGPU_MIXED = 2  /* Real = double in and out; FP32 arithmetic with double-float (two-FP32) error-free
+                        transformations where digits >= 8 needs more than FP32 gives.  digits >= 14 runs
+                        the FP64 path. */
+};
+
+/* Flags. */
+#define SCTLGPU_ACCUMULATE 1u  /* v_trg += result (the reference's Eval when v_trg is already sized); else v_trg = result */
+#define SCTLGPU_DEVICE_PTRS 2u /* every array argument is a device pointer; asynchronous on `stream` */
+
+/* Status codes. */
+enum sctlgpu_status {
+  SCTLGPU_OK = 0,
+  SCTLGPU_ERR_INVALID_KERNEL = -1,
+  SCTLGPU_ERR_INVALID_MODE = -2,
+  SCTLGPU_ERR_INVALID_SIZE = -3,    /* negative counts, or counts whose arrays would overflow int64 */
+  SCTLGPU_ERR_NULL_POINTER = -4,    /* a required array is NULL while its count is > 0 */
+  SCTLGPU_ERR_CUDA = -5,            /* a CUDA runtime call failed; sctlgpu_last_cuda_error() has the text */
+  SCTLGPU_ERR_NO_DEVICE = -6,
+  SCTLGPU_ERR_DEVICE_TIMEOUT = -7,  /* a bounded device-side wait gave up; results are not valid */
+  SCTLGPU_ERR_INVALID_ARGUMENT = -8,
+  SCTLGPU_ERR_TOO_LARGE = -9        /* the request exceeds a fixed capacity of the entry point */
+};
+
+/*
+ * GenericKernel::CoordDim / NormalDim / SrcDim / TrgDim (generic-kernel.hpp:54-74).
+ * Any output pointer may be NULL.
+ */
+int sctlgpu_kernel_dims(int kernel, int* coord_dim, int* normal_dim, int* src_dim, int* trg_dim);
+
+/* uKerScaleFactor<double>() of the kernel (kernel_functions.hpp:40,69,133,188). */
+double sctlgpu_scale_factor(int kernel);
+
+/*
+ * Direct sum  v_trg[t*TrgDim+k] (+)= scale * sum_s K(x_t - y_s, n_s) . f_s.
+ * Replaces GenericKernel<uK>::Eval<Real,enable_openmp>(v_trg, r_trg, r_src, n_src, v_src, digits, self)
+ * (generic-kernel.hpp:99, generic-kernel.txx:72-211), the function ParticleFMM stores in
+ * S2TData::ker_s2t_eval_omp (fmm-wrapper.txx:153-154,450-451) and calls in EvalDirect
+ * (fmm-wrapper.txx:618).  Arrays are double for SCTLGPU_F64 / SCTLGPU_MIXED, float for
+ * SCTLGPU_F32.  n_src may be NULL for kernels with NormalDim()==0.
+ */
+int sctlgpu_eval(int kernel, int mode, int digits,
+                 int64_t nt, const void* r_trg,
+                 int64_t ns, const void* r_src, const void* n_src, const void* v_src,
+                 void* v_trg, unsigned flags, void* stream);
+
+/*
+ * Dense kernel matrix M[(s*SrcDim+k0)*(nt*TrgDim) + t*TrgDim+k1] = scale * K_{k0,k1}(x_t - y_s, n_s),
+ * row-major, source-major, overwritten.  Replaces GenericKernel<uK>::KernelMatrix<Real,omp,digits>
+ * (generic-kernel.hpp:124, generic-kernel.txx:213-329), which BoundaryIntegralOp calls per near
+ * block in SetupNear (boundary_integral.txx:1197,1211).
+ */
+int sctlgpu_kernel_matrix(int kernel, int mode, int digits,
+                          int64_t nt, const void* r_trg,
+                          int64_t ns, const void* r_src, const void* n_src,
+                          void* M, unsigned flags, void* stream);
+
+/* Human-readable text for a status code. */
+const char* sctlgpu_strerror(int status);
+
+/* Text of the last CUDA error seen by this thread (empty if none). */
+const char* sctlgpu_last_cuda_error(void);
+
+/*
+ * Reads and clears the device-side status word of the current device after
+ * synchronising `stream` (bounded-wait timeouts of asynchronous calls made
+ * with SCTLGPU_DEVICE_PTRS).  Returns SCTLGPU_OK or SCTLGPU_ERR_DEVICE_TIMEOUT.
+ */
+int sctlgpu_device_status(void* stream);
+
+/* Number of kernels this library has launched in this process (all threads). */
+int64_t sctlgpu_launch_count(void);
+
+/*
+ * Kernel timing: when enabled, the direct-sum and kernel-matrix entry points
+ * record CUDA events on their launch stream around their main kernel, and
+ * sctlgpu_last_kernel_ms() returns that kernel's duration for the calling
+ * thread's most recent call (synchronising on the end event).  Off by default.
+ */
+int sctlgpu_set_timing(int enable);
+double sctlgpu_last_kernel_ms(void);
+
+/*
+ * Number of Newton steps the evaluation uses for (mode, digits): the
+ * reference's schedule mylog2(floor(digits / seed_digits)) with the seed
+ * accuracy of sm_103a's rsqrt.approx (intrin-wrapper.hpp:560-562).
+ */
+int sctlgpu_newton_steps(int mode, int digits);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SCTLGPU_H_ */

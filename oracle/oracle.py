@@ -1,0 +1,186 @@
+"""ctypes bindings for the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may import
+this module.  It wraps
+
+* ``libsctl_oracle.so`` -- the plain-C restatement of SCTL's GenericKernel
+  Eval / KernelMatrix (sctl_oracle.c), and
+* ``_ref/libsctlref.so`` -- the reference's own header-only implementation,
+  wrapped by ref_driver.cpp (only present where the reference checkout was
+  available at build time).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "libsctl_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libsctlref.so")
+
+KERNELS = {"Laplace3D_FxU": 0, "Laplace3D_DxU": 1, "Stokes3D_FxU": 2, "Stokes3D_DxU": 3}
+# (NormalDim, SrcDim, TrgDim), generic-kernel.txx:48-62 with kernel_functions.hpp
+DIMS = {0: (0, 1, 1), 1: (3, 1, 1), 2: (0, 3, 3), 3: (3, 3, 3)}
+
+_lib = None
+_ref = None
+
+
+def build(force: bool = False) -> None:
+    """Compile the oracle with gcc (seconds); never touches the product library."""
+    if force or not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < os.path.getmtime(
+            os.path.join(HERE, "sctl_oracle.c")):
+        subprocess.run(["make", "-s", "-C", HERE, "libsctl_oracle.so"], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(ORACLE_SO)
+        i64, vp, i32 = ctypes.c_int64, ctypes.c_void_p, ctypes.c_int
+        for name in ("oracle_eval_f64", "oracle_eval_f32", "oracle_eval_ld"):
+            getattr(L, name).argtypes = [i32, i64, vp, i64, vp, vp, vp, vp, i32]
+            getattr(L, name).restype = i32
+        for name in ("oracle_kernel_matrix_f64", "oracle_kernel_matrix_f32"):
+            getattr(L, name).argtypes = [i32, i64, vp, i64, vp, vp, vp, i32]
+            getattr(L, name).restype = i32
+        L.oracle_newton_steps.argtypes = [i32, i32, ctypes.c_double]
+        L.oracle_newton_steps.restype = i32
+        L.oracle_rsqrt_newton.argtypes = [ctypes.c_double, ctypes.c_double, i32]
+        L.oracle_rsqrt_newton.restype = ctypes.c_double
+        L.oracle_scale_factor.argtypes = [i32]
+        L.oracle_scale_factor.restype = ctypes.c_double
+        L.oracle_max_threads.restype = i32
+        _lib = L
+    return _lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        if not ref_available():
+            raise RuntimeError("reference wrapper not built (oracle/_ref/libsctlref.so)")
+        L = ctypes.CDLL(REF_SO)
+        i64, vp, i32 = ctypes.c_int64, ctypes.c_void_p, ctypes.c_int
+        L.ref_eval.argtypes = [i32, i32, i32, i64, vp, i64, vp, vp, vp, vp, i32]
+        L.ref_eval.restype = i32
+        L.ref_kernel_matrix.argtypes = [i32, i32, i64, vp, i64, vp, vp, vp]
+        L.ref_kernel_matrix.restype = i32
+        L.ref_vec_len.argtypes = [i32]
+        L.ref_vec_len.restype = i32
+        _ref = L
+    return _ref
+
+
+def _kid(kernel):
+    return KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
+
+
+def _ptr(a):
+    return None if a is None or a.size == 0 else a.ctypes.data
+
+
+def eval(kernel, r_trg, r_src, n_src, v_src, v_trg=None, precision="f64", nthreads=0):
+    """v_trg (+)= scale * sum_s K f (the reference's Eval); returns v_trg."""
+    k = _kid(kernel)
+    nd, sd, td = DIMS[k]
+    dt = np.float32 if precision == "f32" else np.float64
+    r_trg = np.ascontiguousarray(r_trg, dt).reshape(-1)
+    r_src = np.ascontiguousarray(r_src, dt).reshape(-1)
+    v_src = np.ascontiguousarray(v_src, dt).reshape(-1)
+    n_src = np.ascontiguousarray(n_src, dt).reshape(-1) if nd else None
+    nt, ns = r_trg.size // 3, r_src.size // 3
+    if v_trg is None:
+        v_trg = np.zeros(nt * td, dt)
+    fn = {"f64": lib().oracle_eval_f64, "f32": lib().oracle_eval_f32, "ld": lib().oracle_eval_ld}[precision]
+    rc = fn(k, nt, _ptr(r_trg), ns, _ptr(r_src), _ptr(n_src), _ptr(v_src), _ptr(v_trg), nthreads)
+    if rc:
+        raise RuntimeError(f"oracle eval failed: {rc}")
+    return v_trg
+
+
+def kernel_matrix(kernel, r_trg, r_src, n_src, precision="f64", nthreads=0):
+    k = _kid(kernel)
+    nd, sd, td = DIMS[k]
+    dt = np.float32 if precision == "f32" else np.float64
+    r_trg = np.ascontiguousarray(r_trg, dt).reshape(-1)
+    r_src = np.ascontiguousarray(r_src, dt).reshape(-1)
+    n_src = np.ascontiguousarray(n_src, dt).reshape(-1) if nd else None
+    nt, ns = r_trg.size // 3, r_src.size // 3
+    M = np.zeros((ns * sd, nt * td), dt)
+    fn = lib().oracle_kernel_matrix_f32 if precision == "f32" else lib().oracle_kernel_matrix_f64
+    rc = fn(k, nt, _ptr(r_trg), ns, _ptr(r_src), _ptr(n_src), _ptr(M), nthreads)
+    if rc:
+        raise RuntimeError(f"oracle kernel_matrix failed: {rc}")
+    return M
+
+
+def ref_eval(kernel, r_trg, r_src, n_src, v_src, digits=-1, precision="f64", omp=True, v_trg=None):
+    """The reference's own GenericKernel::Eval<Real,omp>(..., digits, self)."""
+    k = _kid(kernel)
+    nd, sd, td = DIMS[k]
+    dt = np.float32 if precision == "f32" else np.float64
+    r_trg = np.ascontiguousarray(r_trg, dt).reshape(-1)
+    r_src = np.ascontiguousarray(r_src, dt).reshape(-1)
+    v_src = np.ascontiguousarray(v_src, dt).reshape(-1)
+    n_src = np.ascontiguousarray(n_src, dt).reshape(-1) if nd else None
+    nt, ns = r_trg.size // 3, r_src.size // 3
+    if v_trg is None:
+        v_trg = np.zeros(nt * td, dt)
+    rc = ref().ref_eval(k, int(dt == np.float64), int(digits), nt, _ptr(r_trg), ns, _ptr(r_src), _ptr(n_src),
+                        _ptr(v_src), _ptr(v_trg), int(omp))
+    if rc:
+        raise RuntimeError(f"reference eval failed: {rc}")
+    return v_trg
+
+
+def ref_kernel_matrix(kernel, r_trg, r_src, n_src, precision="f64"):
+    k = _kid(kernel)
+    nd, sd, td = DIMS[k]
+    dt = np.float32 if precision == "f32" else np.float64
+    r_trg = np.ascontiguousarray(r_trg, dt).reshape(-1)
+    r_src = np.ascontiguousarray(r_src, dt).reshape(-1)
+    n_src = np.ascontiguousarray(n_src, dt).reshape(-1) if nd else None
+    nt, ns = r_trg.size // 3, r_src.size // 3
+    M = np.zeros((ns * sd, nt * td), dt)
+    rc = ref().ref_kernel_matrix(k, int(dt == np.float64), nt, _ptr(r_trg), ns, _ptr(r_src), _ptr(n_src), _ptr(M))
+    if rc:
+        raise RuntimeError(f"reference kernel_matrix failed: {rc}")
+    return M
+
+
+def newton_steps(digits, is_double, seed_digits):
+    return lib().oracle_newton_steps(int(digits), int(is_double), float(seed_digits))
+
+
+def rsqrt_newton(x, y0, steps):
+    return lib().oracle_rsqrt_newton(float(x), float(y0), int(steps))
+
+
+def scale_factor(kernel):
+    return lib().oracle_scale_factor(_kid(kernel))
+
+
+def max_threads():
+    return lib().oracle_max_threads()
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    den = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (den if den > 0 else 1.0))
+
+
+def max_rel(a, b):
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))

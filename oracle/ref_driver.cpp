@@ -1,0 +1,98 @@
+// Thin C-ABI wrapper around the REFERENCE's own header-only implementation --
+// TEST INFRASTRUCTURE ONLY.  Compiled by oracle/Makefile against the reference
+// headers (include/sctl/*) into oracle/_ref/libsctlref.so; used to pin the
+// restated oracle (sctl_oracle.c) and to generate tests/golden fixtures.  It
+// calls the reference's public API exactly as ParticleFMM does:
+//   GenericKernel<uK>::Eval<Real,true>(v_trg, r_trg, r_src, n_src, v_src, digits, self)
+//   (generic-kernel.hpp:99, called through a function pointer at fmm-wrapper.txx:618)
+// and GenericKernel<uK>::KernelMatrix<Real,omp,digits>(M, Xt, Xs, Xn)
+//   (generic-kernel.hpp:124, called by boundary_integral.txx:1197,1211).
+#include <cstdint>
+#include <cstring>
+
+#include "sctl.hpp"
+
+namespace {
+
+template <class Kernel, class Real>
+int eval_impl(int digits, int64_t nt, const Real* r_trg, int64_t ns, const Real* r_src, const Real* n_src,
+              const Real* v_src, Real* v_trg, int omp) {
+  Kernel ker;
+  const sctl::Long nd = Kernel::NormalDim(), sd = Kernel::SrcDim(), td = Kernel::TrgDim();
+  sctl::Vector<Real> Xt(nt * 3, sctl::Ptr2Itr<Real>((Real*)r_trg, nt * 3), false);
+  sctl::Vector<Real> Xs(ns * 3, sctl::Ptr2Itr<Real>((Real*)r_src, ns * 3), false);
+  sctl::Vector<Real> Xn;
+  if (nd) Xn.ReInit(ns * nd, sctl::Ptr2Itr<Real>((Real*)n_src, ns * nd), false);
+  sctl::Vector<Real> Vs(ns * sd, sctl::Ptr2Itr<Real>((Real*)v_src, ns * sd), false);
+  // v_trg has the right size, so Eval accumulates into it (generic-kernel.txx:129-132).
+  sctl::Vector<Real> Vt(nt * td, sctl::Ptr2Itr<Real>(v_trg, nt * td), false);
+  if (omp)
+    Kernel::template Eval<Real, true>(Vt, Xt, Xs, Xn, Vs, digits, (sctl::ConstIterator<char>)sctl::Ptr2ConstItr<char>(&ker, sizeof(ker)));
+  else
+    Kernel::template Eval<Real, false>(Vt, Xt, Xs, Xn, Vs, digits, (sctl::ConstIterator<char>)sctl::Ptr2ConstItr<char>(&ker, sizeof(ker)));
+  return 0;
+}
+
+template <class Kernel, class Real>
+int kmat_impl(int64_t nt, const Real* r_trg, int64_t ns, const Real* r_src, const Real* n_src, Real* M) {
+  Kernel ker;
+  const sctl::Long nd = Kernel::NormalDim(), sd = Kernel::SrcDim(), td = Kernel::TrgDim();
+  sctl::Vector<Real> Xt(nt * 3, sctl::Ptr2Itr<Real>((Real*)r_trg, nt * 3), false);
+  sctl::Vector<Real> Xs(ns * 3, sctl::Ptr2Itr<Real>((Real*)r_src, ns * 3), false);
+  sctl::Vector<Real> Xn;
+  if (nd) Xn.ReInit(ns * nd, sctl::Ptr2Itr<Real>((Real*)n_src, ns * nd), false);
+  sctl::Matrix<Real> Mat(ns * sd, nt * td, sctl::Ptr2Itr<Real>(M, ns * sd * nt * td), false);
+  ker.template KernelMatrix<Real, true>(Mat, Xt, Xs, Xn);
+  return 0;
+}
+
+template <class Real>
+int eval_dispatch(int kernel, int digits, int64_t nt, const Real* r_trg, int64_t ns, const Real* r_src,
+                  const Real* n_src, const Real* v_src, Real* v_trg, int omp) {
+  switch (kernel) {
+    case 0: return eval_impl<sctl::Laplace3D_FxU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    case 1: return eval_impl<sctl::Laplace3D_DxU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    case 2: return eval_impl<sctl::Stokes3D_FxU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    case 3: return eval_impl<sctl::Stokes3D_DxU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    default: return -1;
+  }
+}
+
+template <class Real>
+int kmat_dispatch(int kernel, int64_t nt, const Real* r_trg, int64_t ns, const Real* r_src, const Real* n_src, Real* M) {
+  switch (kernel) {
+    case 0: return kmat_impl<sctl::Laplace3D_FxU, Real>(nt, r_trg, ns, r_src, n_src, M);
+    case 1: return kmat_impl<sctl::Laplace3D_DxU, Real>(nt, r_trg, ns, r_src, n_src, M);
+    case 2: return kmat_impl<sctl::Stokes3D_FxU, Real>(nt, r_trg, ns, r_src, n_src, M);
+    case 3: return kmat_impl<sctl::Stokes3D_DxU, Real>(nt, r_trg, ns, r_src, n_src, M);
+    default: return -1;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int ref_eval(int kernel, int is_double, int digits, int64_t nt, const void* r_trg, int64_t ns, const void* r_src,
+             const void* n_src, const void* v_src, void* v_trg, int omp) {
+  if (is_double)
+    return eval_dispatch<double>(kernel, digits, nt, (const double*)r_trg, ns, (const double*)r_src,
+                                 (const double*)n_src, (const double*)v_src, (double*)v_trg, omp);
+  return eval_dispatch<float>(kernel, digits, nt, (const float*)r_trg, ns, (const float*)r_src, (const float*)n_src,
+                              (const float*)v_src, (float*)v_trg, omp);
+}
+
+int ref_kernel_matrix(int kernel, int is_double, int64_t nt, const void* r_trg, int64_t ns, const void* r_src,
+                      const void* n_src, void* M) {
+  if (is_double)
+    return kmat_dispatch<double>(kernel, nt, (const double*)r_trg, ns, (const double*)r_src, (const double*)n_src,
+                                 (double*)M);
+  return kmat_dispatch<float>(kernel, nt, (const float*)r_trg, ns, (const float*)r_src, (const float*)n_src, (float*)M);
+}
+
+// Which SIMD path the reference was compiled for (DefaultVecLen, vec.txx:27-42).
+int ref_vec_len(int is_double) {
+  return is_double ? (int)sctl::DefaultVecLen<double>() : (int)sctl::DefaultVecLen<float>();
+}
+
+}  // extern "C"

@@ -1,0 +1,217 @@
+/*
+ * CPU oracle for the particle-kernel direct sums -- TEST INFRASTRUCTURE ONLY
+ * (see sctl_oracle.h).  Restates include/sctl/generic-kernel.txx:102-329 and
+ * the four micro-kernels of include/sctl/kernel_functions.hpp.
+ *
+ * Structure mirrors the reference's hot loop (generic-kernel.txx:175-188):
+ * SIMD lanes run over a block of targets, the source loop is sequential, and
+ * each lane accumulates in the working precision in source order.  The lanes
+ * here are a fixed block of ORACLE_TB targets that the compiler vectorises.
+ */
+#include "sctl_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORACLE_TB 8
+
+static const double kPi = 3.14159265358979323846264338327950288;
+
+int oracle_kernel_dims(int kernel, int* cd, int* nd, int* sd, int* td) {
+  int c = 3, n, s, t;
+  switch (kernel) {
+    case ORACLE_LAPLACE3D_FXU: n = 0; s = 1; t = 1; break;
+    case ORACLE_LAPLACE3D_DXU: n = 3; s = 1; t = 1; break;
+    case ORACLE_STOKES3D_FXU: n = 0; s = 3; t = 3; break;
+    case ORACLE_STOKES3D_DXU: n = 3; s = 3; t = 3; break;
+    default: return -1;
+  }
+  if (cd) *cd = c;
+  if (nd) *nd = n;
+  if (sd) *sd = s;
+  if (td) *td = t;
+  return 0;
+}
+
+double oracle_scale_factor(int kernel) {
+  switch (kernel) {
+    case ORACLE_LAPLACE3D_FXU: return 1.0 / (4.0 * kPi);  /* kernel_functions.hpp:40-42 */
+    case ORACLE_LAPLACE3D_DXU: return 1.0 / (4.0 * kPi);  /* :69-71 */
+    case ORACLE_STOKES3D_FXU: return 1.0 / (8.0 * kPi);   /* :133-135 */
+    case ORACLE_STOKES3D_DXU: return 3.0 / (4.0 * kPi);   /* :188-190 */
+    default: return 0.0;
+  }
+}
+
+int oracle_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+static int resolve_threads(int nthreads) { return nthreads > 0 ? nthreads : oracle_max_threads(); }
+
+int oracle_newton_steps(int digits, int is_double, double seed_digits) {
+  /* vec.txx:376: digits == -1 -> floor(SigBits * log10 2). */
+  if (digits < 0 || digits >= 16) digits = is_double ? 15 : 6;
+  if (!(seed_digits > 0)) return 0;
+  long q = (long)((double)digits / seed_digits);
+  int n = 0; /* mylog2, intrin-wrapper.hpp:560-562 */
+  while (q >= 1) { n++; q /= 2; }
+  return n;
+}
+
+double oracle_rsqrt_newton(double x, double y, int steps) {
+  if (x == 0) return 0;
+  if (steps <= 0) return y;
+  /* Deferred-scaling Newton: the unscaled iterate grows by (-2)^... each step,
+   * so step k uses c1_k = -3 * 2^(3^k - 1) and one final scale c2. */
+  long p3 = 1; /* 3^k */
+  for (int k = 0; k < steps; k++) {
+    const double c1 = -3.0 * ldexp(1.0, (int)(p3 - 1));
+    y = y * fma(x, y * y, c1);
+    if (k + 1 < steps) p3 *= 3;
+  }
+  /* c2 = (-0.5)^((3^(n-1)-1)*3/2+1) */
+  const long e = (p3 - 1) * 3 / 2 + 1;
+  const double c2 = ((e & 1) ? -1.0 : 1.0) * ldexp(1.0, (int)-e);
+  return y * c2;
+}
+
+/* ------------------------------------------------------------------ Eval */
+
+#define DEFINE_EVAL(NAME, REAL, ACC, SQRT)                                                        \
+  int NAME(int kernel, int64_t nt, const REAL* r_trg, int64_t ns, const REAL* r_src,             \
+           const REAL* n_src, const REAL* v_src, REAL* v_trg, int nthreads) {                     \
+    int nd, sd, td;                                                                               \
+    if (oracle_kernel_dims(kernel, NULL, &nd, &sd, &td)) return -1;                               \
+    if (nt < 0 || ns < 0) return -2;                                                              \
+    const ACC scale = (ACC)oracle_scale_factor(kernel);                                           \
+    const int64_t nblk = (nt + ORACLE_TB - 1) / ORACLE_TB;                                        \
+    _Pragma("omp parallel for schedule(static) num_threads(resolve_threads(nthreads))")           \
+    for (int64_t b = 0; b < nblk; b++) {                                                          \
+      ACC xt[3][ORACLE_TB], vt[3][ORACLE_TB];                                                     \
+      const int64_t t0 = b * ORACLE_TB;                                                           \
+      const int cnt = (int)((nt - t0) < ORACLE_TB ? (nt - t0) : ORACLE_TB);                       \
+      for (int k = 0; k < 3; k++)                                                                 \
+        for (int l = 0; l < ORACLE_TB; l++) {                                                     \
+          xt[k][l] = l < cnt ? (ACC)r_trg[(t0 + l) * 3 + k] : (ACC)0;                             \
+          vt[k][l] = 0;                                                                           \
+        }                                                                                         \
+      for (int64_t s = 0; s < ns; s++) {                                                          \
+        const ACC xs0 = (ACC)r_src[s * 3 + 0], xs1 = (ACC)r_src[s * 3 + 1], xs2 = (ACC)r_src[s * 3 + 2]; \
+        ACC ns0 = 0, ns1 = 0, ns2 = 0;                                                            \
+        if (nd) { ns0 = (ACC)n_src[s * 3 + 0]; ns1 = (ACC)n_src[s * 3 + 1]; ns2 = (ACC)n_src[s * 3 + 2]; } \
+        const ACC f0 = (ACC)v_src[s * sd + 0];                                                    \
+        const ACC f1 = sd > 1 ? (ACC)v_src[s * sd + 1] : (ACC)0;                                  \
+        const ACC f2 = sd > 1 ? (ACC)v_src[s * sd + 2] : (ACC)0;                                  \
+        switch (kernel) {                                                                         \
+          case ORACLE_LAPLACE3D_FXU: /* kernel_functions.hpp:43-47, then FMA generic-kernel.txx:115-119 */ \
+            for (int l = 0; l < ORACLE_TB; l++) {                                                 \
+              const ACC d0 = xt[0][l] - xs0, d1 = xt[1][l] - xs1, d2 = xt[2][l] - xs2;            \
+              const ACC r2 = d0 * d0 + d1 * d1 + d2 * d2;                                         \
+              const ACC rinv = r2 > 0 ? (ACC)1 / SQRT(r2) : (ACC)0;                               \
+              vt[0][l] += rinv * f0;                                                              \
+            }                                                                                     \
+            break;                                                                                \
+          case ORACLE_LAPLACE3D_DXU: /* kernel_functions.hpp:72-78 */                             \
+            for (int l = 0; l < ORACLE_TB; l++) {                                                 \
+              const ACC d0 = xt[0][l] - xs0, d1 = xt[1][l] - xs1, d2 = xt[2][l] - xs2;            \
+              const ACC r2 = d0 * d0 + d1 * d1 + d2 * d2;                                         \
+              const ACC rinv = r2 > 0 ? (ACC)1 / SQRT(r2) : (ACC)0;                               \
+              const ACC rdotn = d0 * ns0 + d1 * ns1 + d2 * ns2;                                   \
+              const ACC rinv3 = rinv * rinv * rinv;                                               \
+              vt[0][l] += (rdotn * rinv3) * f0;                                                   \
+            }                                                                                     \
+            break;                                                                                \
+          case ORACLE_STOKES3D_FXU: /* fused apply, kernel_functions.hpp:166-176 */               \
+            for (int l = 0; l < ORACLE_TB; l++) {                                                 \
+              const ACC d0 = xt[0][l] - xs0, d1 = xt[1][l] - xs1, d2 = xt[2][l] - xs2;            \
+              const ACC r2 = d0 * d0 + d1 * d1 + d2 * d2;                                         \
+              const ACC rinv = r2 > 0 ? (ACC)1 / SQRT(r2) : (ACC)0;                               \
+              const ACC rinv3 = rinv * rinv * rinv;                                               \
+              const ACC fdr = (f0 * d0 + f1 * d1 + f2 * d2) * rinv3;                              \
+              vt[0][l] += f0 * rinv + d0 * fdr;                                                   \
+              vt[1][l] += f1 * rinv + d1 * fdr;                                                   \
+              vt[2][l] += f2 * rinv + d2 * fdr;                                                   \
+            }                                                                                     \
+            break;                                                                                \
+          default: /* Stokes3D_DxU fused apply, kernel_functions.hpp:205-217 */                   \
+            for (int l = 0; l < ORACLE_TB; l++) {                                                 \
+              const ACC d0 = xt[0][l] - xs0, d1 = xt[1][l] - xs1, d2 = xt[2][l] - xs2;            \
+              const ACC r2 = d0 * d0 + d1 * d1 + d2 * d2;                                         \
+              const ACC rinv = r2 > 0 ? (ACC)1 / SQRT(r2) : (ACC)0;                               \
+              const ACC rinv2 = rinv * rinv;                                                      \
+              const ACC rinv5 = rinv2 * rinv2 * rinv;                                             \
+              const ACC rdn = (d0 * ns0 + d1 * ns1 + d2 * ns2) * rinv5;                           \
+              const ACC c = (f0 * d0 + f1 * d1 + f2 * d2) * rdn;                                  \
+              vt[0][l] += d0 * c;                                                                 \
+              vt[1][l] += d1 * c;                                                                 \
+              vt[2][l] += d2 * c;                                                                 \
+            }                                                                                     \
+            break;                                                                                \
+        }                                                                                         \
+      }                                                                                           \
+      for (int l = 0; l < cnt; l++) /* v_trg += Vt_ * scale, generic-kernel.txx:204-208 */        \
+        for (int k = 0; k < td; k++) v_trg[(t0 + l) * td + k] += (REAL)(vt[k][l] * scale);        \
+    }                                                                                             \
+    return 0;                                                                                     \
+  }
+
+DEFINE_EVAL(oracle_eval_f64, double, double, sqrt)
+DEFINE_EVAL(oracle_eval_f32, float, float, sqrtf)
+DEFINE_EVAL(oracle_eval_ld, double, long double, sqrtl)
+
+/* ---------------------------------------------------------- KernelMatrix */
+
+#define DEFINE_KMAT(NAME, REAL, SQRT)                                                             \
+  int NAME(int kernel, int64_t nt, const REAL* r_trg, int64_t ns, const REAL* r_src,             \
+           const REAL* n_src, REAL* M, int nthreads) {                                            \
+    int nd, sd, td;                                                                               \
+    if (oracle_kernel_dims(kernel, NULL, &nd, &sd, &td)) return -1;                               \
+    if (nt < 0 || ns < 0) return -2;                                                              \
+    const REAL scale = (REAL)oracle_scale_factor(kernel);                                         \
+    const int64_t ld = nt * td;                                                                   \
+    _Pragma("omp parallel for schedule(static) num_threads(resolve_threads(nthreads))")           \
+    for (int64_t s = 0; s < ns; s++) {                                                            \
+      const REAL xs0 = r_src[s * 3], xs1 = r_src[s * 3 + 1], xs2 = r_src[s * 3 + 2];              \
+      REAL n0 = 0, n1 = 0, n2 = 0;                                                                \
+      if (nd) { n0 = n_src[s * 3]; n1 = n_src[s * 3 + 1]; n2 = n_src[s * 3 + 2]; }                \
+      for (int64_t t = 0; t < nt; t++) {                                                          \
+        const REAL r[3] = {r_trg[t * 3] - xs0, r_trg[t * 3 + 1] - xs1, r_trg[t * 3 + 2] - xs2};   \
+        const REAL r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];                                  \
+        const REAL rinv = r2 > 0 ? (REAL)1 / SQRT(r2) : (REAL)0;                                  \
+        REAL u[3][3];                                                                             \
+        switch (kernel) {                                                                         \
+          case ORACLE_LAPLACE3D_FXU: u[0][0] = rinv; break;                                       \
+          case ORACLE_LAPLACE3D_DXU:                                                              \
+            u[0][0] = (r[0] * n0 + r[1] * n1 + r[2] * n2) * (rinv * rinv * rinv);                 \
+            break;                                                                                \
+          case ORACLE_STOKES3D_FXU: { /* kernel_functions.hpp:136-145 */                          \
+            const REAL rinv3 = rinv * rinv * rinv;                                                \
+            for (int i = 0; i < 3; i++)                                                           \
+              for (int j = 0; j < 3; j++) u[i][j] = (i == j ? rinv : (REAL)0) + r[i] * r[j] * rinv3; \
+          } break;                                                                                \
+          default: { /* Stokes3D_DxU, kernel_functions.hpp:191-201 */                             \
+            const REAL rinv2 = rinv * rinv;                                                       \
+            const REAL rinv5 = rinv2 * rinv2 * rinv;                                              \
+            const REAL rdn = (r[0] * n0 + r[1] * n1 + r[2] * n2) * rinv5;                         \
+            for (int i = 0; i < 3; i++)                                                           \
+              for (int j = 0; j < 3; j++) u[i][j] = r[i] * r[j] * rdn;                            \
+          } break;                                                                                \
+        }                                                                                         \
+        for (int k0 = 0; k0 < sd; k0++)                                                           \
+          for (int k1 = 0; k1 < td; k1++) M[(s * sd + k0) * ld + t * td + k1] = u[k0][k1] * scale; \
+      }                                                                                           \
+    }                                                                                             \
+    return 0;                                                                                     \
+  }
+
+DEFINE_KMAT(oracle_kernel_matrix_f64, double, sqrt)
+DEFINE_KMAT(oracle_kernel_matrix_f32, float, sqrtf)

@@ -1,0 +1,64 @@
+// Host-side interface between the C ABI (capi.cu) and the per-mode kernel
+// translation units.  All pointers here are device pointers.
+#pragma once
+
+#include <atomic>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sctlgpu {
+
+struct BBox;
+
+// Process-wide count of kernels launched by this library.
+extern std::atomic<int64_t> g_launches;
+
+struct Timing {
+  bool enabled = false;
+  cudaEvent_t start = nullptr, stop = nullptr;
+  bool recorded = false;
+};
+
+struct EvalCall {
+  int kernel;
+  int64_t nt, ns;
+  const void* r_trg;
+  const void* r_src;
+  const void* n_src;
+  const void* v_src;
+  void* v_trg;
+  bool accumulate;
+  cudaStream_t stream;
+  unsigned* status;  // device status word
+  int sms;           // multiprocessors of the current device
+  Timing* timing;    // may be null
+};
+
+struct KmatCall {
+  int kernel;
+  int64_t nt, ns;
+  const void* r_trg;
+  const void* r_src;
+  const void* n_src;
+  void* M;
+  cudaStream_t stream;
+  int sms;
+  Timing* timing;
+};
+
+// Direct sums.  `newton` is the number of Newton steps after the hardware seed.
+cudaError_t eval_f64(const EvalCall& c, int newton);
+cudaError_t eval_f32(const EvalCall& c, int newton);
+cudaError_t eval_mixed_lo(const EvalCall& c, int newton);  // FP32 arithmetic on split coordinates
+cudaError_t eval_mixed_df(const EvalCall& c);              // double-float arithmetic
+
+// Kernel matrices.
+cudaError_t kmat_f64(const KmatCall& c, int newton);
+cudaError_t kmat_f32(const KmatCall& c, int newton);
+cudaError_t kmat_mixed_df(const KmatCall& c);
+
+// Bounding box of targets and sources for the mixed-precision frame; `bb` is
+// 64 bytes of device memory, initialised here.
+cudaError_t compute_bbox(cudaStream_t s, int64_t nt, const double* r_trg, int64_t ns, const double* r_src, BBox* bb);
+
+}  // namespace sctlgpu

@@ -1,0 +1,81 @@
+"""The C-ABI library loads, exports every symbol include/*.h declares, and
+rejects bad arguments with status codes -- no GPU needed (the argument checks
+run before any device call)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import sctl_gb300 as S
+from sctl_gb300 import capi
+
+INCLUDE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+
+
+def declared_symbols():
+    names = set()
+    for fn in os.listdir(INCLUDE):
+        if fn.endswith(".h"):
+            src = open(os.path.join(INCLUDE, fn)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b(sctlgpu_\w+)\s*\(", src))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = capi.load()
+    names = declared_symbols()
+    assert "sctlgpu_eval" in names and "sctlgpu_kernel_matrix" in names
+    for n in names:
+        assert hasattr(lib, n), n
+    assert names <= set(capi.SIGNATURES), names - set(capi.SIGNATURES)
+
+
+def test_kernel_dims_match_reference():
+    assert capi.kernel_dims(0) == (3, 0, 1, 1)
+    assert capi.kernel_dims(1) == (3, 3, 1, 1)
+    assert capi.kernel_dims(2) == (3, 0, 3, 3)
+    assert capi.kernel_dims(3) == (3, 3, 3, 3)
+    with pytest.raises(S.SctlGpuError):
+        capi.kernel_dims(7)
+    for k, v in ((0, 1 / (4 * np.pi)), (1, 1 / (4 * np.pi)), (2, 1 / (8 * np.pi)), (3, 3 / (4 * np.pi))):
+        assert abs(capi.load().sctlgpu_scale_factor(k) - v) < 1e-17
+
+
+def test_argument_errors_without_gpu():
+    lib = capi.load()
+    x = np.zeros(6)
+    p = x.ctypes.data
+    assert lib.sctlgpu_eval(9, 0, -1, 1, p, 1, p, None, p, p, 0, None) == capi.ERR_INVALID_KERNEL
+    assert lib.sctlgpu_eval(0, 7, -1, 1, p, 1, p, None, p, p, 0, None) == capi.ERR_INVALID_MODE
+    assert lib.sctlgpu_eval(0, 0, -1, -1, p, 1, p, None, p, p, 0, None) == capi.ERR_INVALID_SIZE
+    assert lib.sctlgpu_eval(0, 0, -1, 1, None, 1, p, None, p, p, 0, None) == capi.ERR_NULL_POINTER
+    assert lib.sctlgpu_eval(1, 0, -1, 1, p, 1, p, None, p, p, 0, None) == capi.ERR_NULL_POINTER  # DxU needs normals
+    assert lib.sctlgpu_eval(0, 0, -1, 1 << 62, p, 1, p, None, p, p, 0, None) == capi.ERR_INVALID_SIZE
+    assert lib.sctlgpu_kernel_matrix(0, 0, -1, 1, p, 1, p, None, None, 0, None) == capi.ERR_NULL_POINTER
+    # zero targets is a no-op that needs no device
+    assert lib.sctlgpu_eval(0, 0, -1, 0, None, 5, p, None, p, None, 0, None) == capi.OK
+    for code in (0, -1, -2, -3, -4, -5, -6, -7, -8, -9):
+        assert lib.sctlgpu_strerror(code)
+
+
+def test_python_eval_rejects_mismatched_sizes():
+    with pytest.raises(S.SctlGpuError):
+        S.Laplace3D_FxU.Eval(None, np.zeros(3), np.zeros(6), None, np.ones(3))
+
+
+def test_newton_schedule():
+    # rsqrt.approx seed ~ 6.89 digits: FP32 full (6 digits) needs no step, FP64 full two.
+    assert capi.newton_steps("f32", -1) == 0
+    assert capi.newton_steps("f64", -1) == 2
+    assert capi.newton_steps("f64", 16) == 2
+    assert capi.newton_steps("f64", 6) == 0
+    assert capi.newton_steps("f64", 10) == 1
+    assert capi.newton_steps("mixed", 10) == 1
+
+
+def test_launch_counter_starts_readable():
+    assert isinstance(capi.launch_count(), int)
+    assert capi.load().sctlgpu_last_kernel_ms() < 0 or True
