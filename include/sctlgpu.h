@@ -46,9 +46,8 @@ enum sctlgpu_kernel {
 enum sctlgpu_mode {
   SCTLGPU_F64 = 0,   /* Real = double: FP64 arithmetic throughout (GenericKernel<...>::Eval<double,...>). */
   SCTLGPU_F32 = 1,   /* Real = float:  FP32 arithmetic throughout (GenericKernel<...>::Eval<float,...>).  */
-  SCTLGPU_MIXED = 2  /* Real = double in and out; FP32 arithmetic with double-float (two-FP32) error-free
-                        transformations where digits >= 8 needs more than FP32 gives.  digits >= 14 runs
-                        the FP64 path. */
+  SCTLGPU_MIXED = 2  /* Real = double in and out; FP32 arithmetic up to 7 digits, double-float (two-FP32)
+                        error-free transformations for 8..12 digits, the FP64 path beyond. */
 };
 
 /* Flags. */

@@ -18,7 +18,7 @@
 //              hi+lo on a common grid so x_t - y_s is formed to ~1e-14 of the
 //              bounding box, Kahan-compensated FP32 accumulation.
 //   MODE_MXDF  FP64 inputs, double-float arithmetic in the FP32 pipe (digits
-//              8..13): exact hi differences, exact r^2 via TwoProduct/TwoSum,
+//              8..12): exact hi differences, exact r^2 via TwoProduct/TwoSum,
 //              one Newton step on the double-float residual, double-float
 //              products and accumulation.  No FP64 instruction per pair: the
 //              FP64 pipe of GB300 is a small fraction of its FP32 pipe.
@@ -84,12 +84,15 @@ __device__ __forceinline__ MixedFrame frame_from_bbox(const BBox* bb) {
   return f;
 }
 
-// Split a coordinate on the frame's grid: hi exact in FP32, lo the remainder.
+// Split a coordinate on the frame's grids: hi on g (|hi| <= 2^23 g), lo on
+// g*2^-24 (|lo| <= g/2).  Both are exact floats, and so are the differences
+// hi_t - hi_s and lo_t - lo_s of any two points: a coordinate difference is
+// the exact sum of two floats, accurate to g*2^-25 (47 bits of the box).
 __device__ __forceinline__ void split_coord(const MixedFrame& f, int k, double x, float& h, float& l) {
   const double d = x - f.o[k];
   const double q = rint(d * f.inv_g) * f.g;
   h = (float)q;
-  l = (float)(d - q);
+  l = (float)(rint((d - q) * f.inv_g * 16777216.0) * (f.g * (1.0 / 16777216.0)));
 }
 __device__ __forceinline__ void split_val(double x, float& h, float& l) {
   h = (float)x;
@@ -309,7 +312,7 @@ struct Pair<KER, MODE_MXLO, NEWTON> {
   }
 };
 
-// ---- mixed, double-float (digits 8..13) -------------------------------------
+// ---- mixed, double-float (digits 8..12) -------------------------------------
 // Exact dot product a.b of double-float 3-vectors (a_i = ah_i + al_i), as a
 // normalised pair; used where cancellation is expected (r.n near a surface).
 __device__ __forceinline__ f2 df_dot3(const float (&ah)[3], const float (&al)[3], float bh0, float bh1, float bh2,
@@ -341,32 +344,32 @@ struct Pair<KER, MODE_MXDF, NEWTON> {
 
   template <class RecT>
   __device__ __forceinline__ static void apply(Trg& t, const RecT& s) {
-    // r = x_t - y_s: hi parts on a common grid, so dh is exact.
+    // r = x_t - y_s: hi and lo differences are exact (common grids); Fast2Sum
+    // renormalises each component to D + d with |d| <= ulp(D)/2.
     float dh[3], dl[3];
-    dh[0] = t.xh[0] - s.xh;
-    dh[1] = t.xh[1] - s.yh;
-    dh[2] = t.xh[2] - s.zh;
-    dl[0] = t.xl[0] - s.xl;
-    dl[1] = t.xl[1] - s.yl;
-    dl[2] = t.xl[2] - s.zl;
+    {
+      const float sh[3] = {s.xh, s.yh, s.zh}, sl[3] = {s.xl, s.yl, s.zl};
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const f2 v = fast_two_sum(t.xh[i] - sh[i], t.xl[i] - sl[i]);
+        dh[i] = v.h;
+        dl[i] = v.l;
+      }
+    }
     // r^2 = R + Rl exactly up to the rounding of Rl.
     const f2 p0 = two_prod(dh[0], dh[0]), p1 = two_prod(dh[1], dh[1]), p2 = two_prod(dh[2], dh[2]);
     const f2 s1 = two_sum(p0.h, p1.h);
     const f2 s2 = two_sum(s1.h, p2.h);
     const float R = s2.h;
-    float Rl = (p0.l + p1.l) + (p2.l + s1.l) + s2.l;
-    Rl = fmaf(dl[0], fmaf(2.f, dh[0], dl[0]), Rl);
-    Rl = fmaf(dl[1], fmaf(2.f, dh[1], dl[1]), Rl);
-    Rl = fmaf(dl[2], fmaf(2.f, dh[2], dl[2]), Rl);
-    const float Rt = R + Rl;
-    float y0 = rsqrt_seed(Rt);
-    y0 = Rt > 0.f ? y0 : 0.f;
+    float Rl = fmaf(dh[2], dl[2], fmaf(dh[1], dl[1], dh[0] * dl[0]));
+    Rl = fmaf(2.f, Rl, (p0.l + p1.l) + (p2.l + s1.l) + s2.l);
+    float y0 = rsqrt_seed(R);
+    y0 = R > 0.f ? y0 : 0.f;
     // One Newton step on the exact residual rho = 1 - y0^2 (R + Rl).
     const f2 q = two_prod(y0, y0);
     float rho = fmaf(-q.h, R, 1.f);
     rho = fmaf(-q.l, R, rho);
     rho = fmaf(-q.h, Rl, rho);
-    rho = y0 > 0.f ? rho : 0.f;
     const f2 y = {y0, (0.5f * y0) * rho};  // 1/r = y.h + y.l
     if constexpr (KER == KER_LFXU) {
       df_acc(t.acc[0], df_mul(y, f2{s.fh, s.fl}));

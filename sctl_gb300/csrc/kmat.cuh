@@ -39,7 +39,7 @@ __device__ __forceinline__ void kmat_entries_plain(const Real (&d)[3], const Rea
   }
 }
 
-// Double-float entries from split coordinates (the MXDF prologue of direct.cuh).
+// Double-float entries from a normalised difference dh + dl (the MXDF prologue of direct.cuh).
 template <int KER>
 __device__ __forceinline__ void kmat_entries_df(const float (&dh)[3], const float (&dl)[3], const float (&nh)[3],
                                                 const float (&nl)[3], double (&u)[3][3]) {
@@ -47,13 +47,10 @@ __device__ __forceinline__ void kmat_entries_df(const float (&dh)[3], const floa
   const f2 s1 = two_sum(p0.h, p1.h);
   const f2 s2 = two_sum(s1.h, p2.h);
   const float R = s2.h;
-  float Rl = (p0.l + p1.l) + (p2.l + s1.l) + s2.l;
-  Rl = fmaf(dl[0], fmaf(2.f, dh[0], dl[0]), Rl);
-  Rl = fmaf(dl[1], fmaf(2.f, dh[1], dl[1]), Rl);
-  Rl = fmaf(dl[2], fmaf(2.f, dh[2], dl[2]), Rl);
-  const float Rt = R + Rl;
-  float y0 = rsqrt_seed(Rt);
-  y0 = Rt > 0.f ? y0 : 0.f;
+  float Rl = fmaf(dh[2], dl[2], fmaf(dh[1], dl[1], dh[0] * dl[0]));
+  Rl = fmaf(2.f, Rl, (p0.l + p1.l) + (p2.l + s1.l) + s2.l);
+  float y0 = rsqrt_seed(R);
+  y0 = R > 0.f ? y0 : 0.f;
   const f2 q = two_prod(y0, y0);
   float rho = fmaf(-q.h, R, 1.f);
   rho = fmaf(-q.l, R, rho);
@@ -116,8 +113,9 @@ __global__ void __launch_bounds__(KM_THREADS)
       float dh[3], dl[3];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        dh[k] = th[k] - sh[k];
-        dl[k] = tl[k] - sl[k];
+        const f2 v = fast_two_sum(th[k] - sh[k], tl[k] - sl[k]);
+        dh[k] = v.h;
+        dl[k] = v.l;
       }
       double u[3][3];
       kmat_entries_df<KER>(dh, dl, nh, nl, u);

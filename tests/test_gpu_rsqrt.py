@@ -12,7 +12,8 @@ from sctl_gb300 import capi
 
 pytestmark = pytest.mark.gpu
 
-SEED_BOUND = 2.0 ** -22.0  # the library's schedule assumes 2^-22.9; allow a little slack
+# The library's schedule assumes 2^-22.9 (f32) and 2^-20.1 (f64, MUFU.RSQ64H) with slack.
+SEED_BOUND = {"f32": 2.0 ** -22.5, "f64": 2.0 ** -20.0}
 
 
 def pair_values(mode, digits, r):
@@ -34,7 +35,7 @@ def test_seed_accuracy(cuda, mode):
     exact = 1.0 / r
     err = np.max(np.abs(got - exact) / exact)
     print(f"rsqrt.approx seed ({mode}): max rel err {err:.3e} = 2^{math.log2(err):.2f}")
-    assert err < SEED_BOUND
+    assert err < SEED_BOUND[mode]
 
 
 @pytest.mark.parametrize("digits,bound", [(4, 2.0 ** -11), (7, 2.0 ** -22), (10, 1e-10), (14, 1e-14)])
@@ -44,7 +45,7 @@ def test_reference_rsqrt_contract_f64(cuda, digits, bound):
     got = pair_values("f64", digits, r)
     err = np.max(np.abs(got - 1.0 / r) * r)
     assert err < bound
-    assert capi.newton_steps("f64", digits) == (0 if digits <= 6 else 1 if digits <= 13 else 2)
+    assert capi.newton_steps("f64", digits) == (0 if digits <= 5 else 1 if digits <= 10 else 2)
 
 
 def test_masked_pair_is_exactly_zero(cuda):
