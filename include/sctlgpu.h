@@ -47,7 +47,7 @@ enum sctlgpu_mode {
   SCTLGPU_F64 = 0,   /* Real = double: FP64 arithmetic throughout (GenericKernel<...>::Eval<double,...>). */
   SCTLGPU_F32 = 1,   /* Real = float:  FP32 arithmetic throughout (GenericKernel<...>::Eval<float,...>).  */
   SCTLGPU_MIXED = 2  /* Real = double in and out; FP32 arithmetic up to 7 digits, double-float (two-FP32)
-                        error-free transformations for 8..12 digits, the FP64 path beyond. */
+                        error-free transformations for 8..11 digits, the FP64 path beyond. */
 };
 
 /* Flags. */

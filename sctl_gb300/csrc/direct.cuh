@@ -18,7 +18,7 @@
 //              hi+lo on a common grid so x_t - y_s is formed to ~1e-14 of the
 //              bounding box, Kahan-compensated FP32 accumulation.
 //   MODE_MXDF  FP64 inputs, double-float arithmetic in the FP32 pipe (digits
-//              8..12): exact hi differences, exact r^2 via TwoProduct/TwoSum,
+//              8..11): exact hi differences, exact r^2 via TwoProduct/TwoSum,
 //              one Newton step on the double-float residual, double-float
 //              products and accumulation.  No FP64 instruction per pair: the
 //              FP64 pipe of GB300 is a small fraction of its FP32 pipe.
@@ -228,6 +228,7 @@ struct PlainPair {
 #pragma unroll
     for (int k = 0; k < K1; ++k) t.acc[k] = 0;
   }
+  __device__ __forceinline__ static void flush(Trg&) {}
   __device__ static double result(const Trg& t, int k) { return (double)t.acc[k]; }
 
   template <class RecT>
@@ -277,6 +278,7 @@ struct Pair<KER, MODE_MXLO, NEWTON> {
 #pragma unroll
     for (int k = 0; k < K1; ++k) t.acc[k] = {0.f, 0.f};
   }
+  __device__ __forceinline__ static void flush(Trg&) {}
   __device__ static double result(const Trg& t, int k) { return (double)t.acc[k].s - (double)t.acc[k].c; }
 
   template <class RecT>
@@ -312,7 +314,7 @@ struct Pair<KER, MODE_MXLO, NEWTON> {
   }
 };
 
-// ---- mixed, double-float (digits 8..12) -------------------------------------
+// ---- mixed, double-float (digits 8..11) -------------------------------------
 // Exact dot product a.b of double-float 3-vectors (a_i = ah_i + al_i), as a
 // normalised pair; used where cancellation is expected (r.n near a surface).
 __device__ __forceinline__ f2 df_dot3(const float (&ah)[3], const float (&al)[3], float bh0, float bh1, float bh2,
@@ -332,15 +334,30 @@ struct Pair<KER, MODE_MXDF, NEWTON> {
   static constexpr int K1 = KDims<KER>::K1;
   struct Trg {
     float xh[3], xl[3];
-    f2 acc[K1];
+    f2 acc[K1];      // double-float sum over the current source tile
+    double tot[K1];  // FP64 sum of the tile sums
   };
   __device__ static void load_trg(Trg& t, const double* r, int64_t i, const MixedFrame& fr) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) split_coord(fr, k, r[i * 3 + k], t.xh[k], t.xl[k]);
 #pragma unroll
-    for (int k = 0; k < K1; ++k) t.acc[k] = {0.f, 0.f};
+    for (int k = 0; k < K1; ++k) {
+      t.acc[k] = {0.f, 0.f};
+      t.tot[k] = 0.0;
+    }
   }
-  __device__ static double result(const Trg& t, int k) { return (double)t.acc[k].h + (double)t.acc[k].l; }
+  // Once per tile: move the tile's double-float sum into FP64 so the pair
+  // accumulator stays small and its rounding stays below 2^-48 of the result.
+  __device__ __forceinline__ static void flush(Trg& t) {
+#pragma unroll
+    for (int k = 0; k < K1; ++k) {
+      t.tot[k] += (double)t.acc[k].h + (double)t.acc[k].l;
+      t.acc[k] = {0.f, 0.f};
+    }
+  }
+  __device__ static double result(const Trg& t, int k) {
+    return t.tot[k] + ((double)t.acc[k].h + (double)t.acc[k].l);
+  }
 
   template <class RecT>
   __device__ __forceinline__ static void apply(Trg& t, const RecT& s) {
@@ -483,6 +500,8 @@ __global__ void __launch_bounds__(TileCfg<KER, MODE>::THREADS)
 #pragma unroll
       for (int j = 0; j < T; ++j) P::apply(tg[j], rec);
     }
+#pragma unroll
+    for (int j = 0; j < T; ++j) P::flush(tg[j]);
     __syncthreads();  // every thread is done with this buffer
     if (threadIdx.x == 0 && k + 2 < ntiles) {
       fence_proxy_async_smem();
