@@ -101,6 +101,38 @@ int sctlgpu_kernel_matrix(int kernel, int mode, int digits,
                           int64_t ns, const void* r_src, const void* n_src,
                           void* M, unsigned flags, void* stream);
 
+/*
+ * sctlgpu_eval with SCTLGPU_MIXED and device pointers, for callers that cannot
+ * allocate device memory.  This entry point has no counterpart in the
+ * reference.  sctlgpu_eval takes its scratch (packed sources, partial sums)
+ * from the stream-ordered allocator; some callers must not allocate at all:
+ * a host whose device memory is owned by another allocator or pool it may not
+ * bypass, code running after its caller has frozen allocations, or a real-time
+ * loop that cannot risk an allocation stall or an out-of-memory error.  This
+ * variant allocates nothing: it works in one fixed scratch array of
+ * SCTLGPU_NOALLOC_SCRATCH_BYTES (64 MiB) that every GPU loading the library
+ * holds until the process exits.
+ *   - Arrays are device pointers (double); flags may hold SCTLGPU_ACCUMULATE
+ *     (SCTLGPU_DEVICE_PTRS is implied).  Digits are routed as for SCTLGPU_MIXED.
+ *   - Returns SCTLGPU_ERR_TOO_LARGE, before launching anything, when the packed
+ *     sources plus partial sums do not fit: 512 B + ns * (32, 48, 48, 80 bytes
+ *     for Laplace FxU, Laplace DxU, Stokes FxU, Stokes DxU) + nt * TrgDim * 8 B
+ *     must stay within the array (e.g. 2^20 Laplace FxU sources and 2^20
+ *     targets fit; 2^20 Stokes DxU sources do not).
+ *   - The first call on a device looks up the array's device address; make it
+ *     before any stream capture.
+ *   - All calls share the array and it keeps the last call's contents: calls
+ *     whose work overlaps on the GPU race and give wrong results, so order
+ *     them (one stream, or synchronise between them).
+ *   - The call waits for `stream` to finish before it returns, and reports a
+ *     device-side wait timeout as SCTLGPU_ERR_DEVICE_TIMEOUT.
+ */
+#define SCTLGPU_NOALLOC_SCRATCH_BYTES (64u << 20)
+int sctlgpu_eval_mixed_noalloc(int kernel, int digits,
+                               int64_t nt, const double* r_trg,
+                               int64_t ns, const double* r_src, const double* n_src, const double* v_src,
+                               double* v_trg, unsigned flags, void* stream);
+
 /* Human-readable text for a status code. */
 const char* sctlgpu_strerror(int status);
 

@@ -39,7 +39,9 @@ SIGNATURES = {
     "sctlgpu_set_timing": (_i, [_i]),
     "sctlgpu_last_kernel_ms": (_d, []),
     "sctlgpu_newton_steps": (_i, [_i, _i]),
+    "sctlgpu_eval_mixed_noalloc": (_i, [_i, _i, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _u, _vp]),
 }
+NOALLOC_SCRATCH_BYTES = 64 << 20
 
 _lib = None
 
