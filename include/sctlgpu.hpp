@@ -1,0 +1,137 @@
+// C++ drop-in for sctl::GenericKernel<uKernel> on the GB300 direct-sum path.
+//
+// sctlgpu::GpuKernel<KID> offers the members of GenericKernel that
+// BoundaryIntegralOp and ParticleFMM use (include/sctl/generic-kernel.hpp):
+//
+//   static constexpr CoordDim/NormalDim/SrcDim/TrgDim()            (:54-74)
+//   template <class Real, bool omp> static void Eval(v_trg, r_trg, r_src, n_src, v_src, digits, self)   (:99)
+//   template <class Real, bool omp=false, Integer digits=-1> void Eval(v_trg, r_trg, r_src, n_src, v_src) const (:112)
+//   template <class Real, bool omp=false, Integer digits=-1> void KernelMatrix(M, Xt, Xs, Xn) const     (:124)
+//
+// with the same argument meaning: AoS coordinates, v_trg re-initialised and
+// zeroed when its size is wrong and otherwise accumulated into
+// (generic-kernel.txx:129-132), M re-initialised when mis-sized
+// (generic-kernel.txx:220-223).  The vector/matrix types are template
+// parameters, so sctl::Vector<Real> / sctl::Matrix<Real> (or any type with
+// Dim(), operator[], ReInit and SetZero) work unchanged, and
+//
+//   &sctlgpu::Laplace3D_DxU::Eval<double, true, sctl::Vector<double>, sctl::ConstIterator<char>>
+//
+// has exactly the type of ParticleFMM's S2TData::ker_s2t_eval_omp
+// (fmm-wrapper.txx:153-154).  Failures abort like SCTL_ASSERT
+// (common.hpp:98-105) unless SCTLGPU_ON_ERROR is defined to something else.
+#ifndef SCTLGPU_HPP_
+#define SCTLGPU_HPP_
+
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <type_traits>
+
+#include "sctlgpu.h"
+
+#ifndef SCTLGPU_ON_ERROR
+#define SCTLGPU_ON_ERROR(rc, what)                                                              \
+  do {                                                                                          \
+    std::fprintf(stderr, "sctlgpu: %s failed: %s %s\n", what, sctlgpu_strerror(rc),              \
+                 rc == SCTLGPU_ERR_CUDA ? sctlgpu_last_cuda_error() : "");                       \
+    std::abort();                                                                               \
+  } while (0)
+#endif
+
+namespace sctlgpu {
+
+// Arithmetic used for Real = double (Real = float always runs SCTLGPU_F32).
+// SCTLGPU_F64 reproduces the reference's FP64 Eval; SCTLGPU_MIXED trades the
+// FP64 pipe for double-float FP32 arithmetic at the same digits.
+inline int& double_mode() {
+  static int mode = SCTLGPU_F64;
+  return mode;
+}
+inline void set_double_mode(int mode) { double_mode() = mode; }
+
+template <int KID>
+class GpuKernel {
+  static constexpr long kDims[4][3] = {{0, 1, 1}, {3, 1, 1}, {0, 3, 3}, {3, 3, 3}};  // NormalDim, SrcDim, TrgDim
+
+  template <class V>
+  static auto ptr(V& v) -> decltype(&v[0]) {
+    return v.Dim() ? &v[0] : nullptr;
+  }
+  template <class Real>
+  static int mode_for() {
+    return std::is_same<Real, float>::value ? SCTLGPU_F32 : double_mode();
+  }
+
+ public:
+  static_assert(KID >= 0 && KID < 4, "unknown sctlgpu kernel id");
+
+  static constexpr long CoordDim() { return 3; }
+  static constexpr long NormalDim() { return kDims[KID][0]; }
+  static constexpr long SrcDim() { return kDims[KID][1]; }
+  static constexpr long TrgDim() { return kDims[KID][2]; }
+  static const std::string& Name() {  // kernel_functions.hpp:33-36,62-65,126-129,181-184
+    static const std::string names[4] = {"Laplace3D-FxU", "Laplace3D-DxU", "Stokes3D-FxU", "Stokes3D-DxU"};
+    return names[KID];
+  }
+
+  GpuKernel() : ctx_ptr(nullptr) {}
+  void SetCtxPtr(void* ctx) { ctx_ptr = ctx; }
+  const void* GetCtxPtr() const { return ctx_ptr; }
+
+  // GenericKernel<uK>::Eval<Real,enable_openmp>(..., digits, self), generic-kernel.hpp:99.
+  template <class Real, bool enable_openmp, class VecT, class SelfT>
+  static void Eval(VecT& v_trg, const VecT& r_trg, const VecT& r_src, const VecT& n_src, const VecT& v_src,
+                   long digits, SelfT /*self*/) {
+    static_assert(std::is_same<Real, float>::value || std::is_same<Real, double>::value, "Real must be float or double");
+    const long nt = (long)r_trg.Dim() / 3, ns = (long)r_src.Dim() / 3;
+    if ((long)r_trg.Dim() != nt * 3 || (long)r_src.Dim() != ns * 3 || (long)v_src.Dim() != ns * SrcDim() ||
+        (NormalDim() && (long)n_src.Dim() != ns * NormalDim()))
+      SCTLGPU_ON_ERROR(SCTLGPU_ERR_INVALID_SIZE, "GpuKernel::Eval");
+    unsigned flags = SCTLGPU_ACCUMULATE;
+    if ((long)v_trg.Dim() != nt * TrgDim()) {
+      v_trg.ReInit(nt * TrgDim());
+      v_trg.SetZero();
+      flags = 0;
+    }
+    const int rc = sctlgpu_eval(KID, mode_for<Real>(), (int)digits, nt, ptr(r_trg), ns, ptr(r_src),
+                                NormalDim() ? ptr(n_src) : nullptr, ptr(v_src), ptr(v_trg), flags, nullptr);
+    if (rc != SCTLGPU_OK) SCTLGPU_ON_ERROR(rc, "GpuKernel::Eval");
+  }
+
+  // Member form with compile-time digits, generic-kernel.hpp:112.
+  template <class Real, bool enable_openmp = false, long digits = -1, class VecT>
+  void Eval(VecT& v_trg, const VecT& r_trg, const VecT& r_src, const VecT& n_src, const VecT& v_src) const {
+    Eval<Real, enable_openmp, VecT, const void*>(v_trg, r_trg, r_src, n_src, v_src, digits, this);
+  }
+
+  // KernelMatrix<Real,omp,digits>(M, Xt, Xs, Xn), generic-kernel.hpp:124: M[(s*K0+k0)][(t*K1+k1)].
+  template <class Real, bool enable_openmp = false, long digits = -1, class MatT, class VecT>
+  void KernelMatrix(MatT& M, const VecT& Xt, const VecT& Xs, const VecT& Xn) const {
+    const long ns = (long)Xs.Dim() / 3, nt = (long)Xt.Dim() / 3;
+    if ((long)M.Dim(0) != ns * SrcDim() || (long)M.Dim(1) != nt * TrgDim()) {
+      M.ReInit(ns * SrcDim(), nt * TrgDim());
+      M.SetZero();
+    }
+    if (!ns || !nt) return;
+    const int rc = sctlgpu_kernel_matrix(KID, mode_for<Real>(), (int)digits, nt, ptr(Xt), ns, ptr(Xs),
+                                         NormalDim() ? ptr(Xn) : nullptr, &M[0][0], 0, nullptr);
+    if (rc != SCTLGPU_OK) SCTLGPU_ON_ERROR(rc, "GpuKernel::KernelMatrix");
+  }
+
+ private:
+  void* ctx_ptr;
+};
+
+template <int KID>
+constexpr long GpuKernel<KID>::kDims[4][3];
+
+// The aliases of kernel_functions.hpp:669-678.
+using Laplace3D_FxU = GpuKernel<SCTLGPU_LAPLACE3D_FXU>;
+using Laplace3D_DxU = GpuKernel<SCTLGPU_LAPLACE3D_DXU>;
+using Stokes3D_FxU = GpuKernel<SCTLGPU_STOKES3D_FXU>;
+using Stokes3D_DxU = GpuKernel<SCTLGPU_STOKES3D_DXU>;
+
+}  // namespace sctlgpu
+
+#endif  // SCTLGPU_HPP_

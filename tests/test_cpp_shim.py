@@ -1,0 +1,43 @@
+"""The C++ drop-in (include/sctlgpu.hpp): type-compatible with the reference's
+GenericKernel call sites, and the reference's own unit tests pass through it."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INC = os.path.join(ROOT, "include")
+LIBDIR = os.path.join(ROOT, "sctl_gb300")
+REF = os.environ.get("SCTL_REF", "/root/reference")
+CXX = shutil.which("g++") or "g++"
+
+
+def build_shim_test(tmp_path):
+    exe = os.path.join(str(tmp_path), "test_gpu_shim")
+    cmd = [CXX, "-std=c++17", "-O2", "-I", INC, os.path.join(ROOT, "tests", "cpp", "test_gpu_shim.cpp"), "-L", LIBDIR,
+           "-lsctlgpu", "-Wl,-rpath," + LIBDIR, "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_shim_compiles_and_links(tmp_path):
+    from sctl_gb300 import capi
+    capi.load()  # the library must exist for the link
+    assert os.path.exists(build_shim_test(tmp_path))
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "include", "sctl")), reason="reference headers not present")
+def test_shim_types_match_reference_call_sites():
+    src = os.path.join(ROOT, "tests", "cpp", "check_reference_types.cpp")
+    r = subprocess.run([CXX, "-std=c++17", "-fsyntax-only", "-I", os.path.join(REF, "include"), "-I", INC, src],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.gpu
+def test_reference_unit_tests_through_shim(cuda, tmp_path):
+    exe = build_shim_test(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "PASS (0 check(s) failed)" in r.stdout, r.stdout + r.stderr
