@@ -102,6 +102,59 @@ int sctlgpu_kernel_matrix(int kernel, int mode, int digits,
                           void* M, unsigned flags, void* stream);
 
 /*
+ * Batched near-field direct sums: many independent blocks of uneven sizes in one
+ * persistent launch, captured in a CUDA graph.  Replaces BoundaryIntegralOp's
+ * per-block near-field loops -- KNearSubtract's KernelMatrix per near block
+ * (boundary_integral.txx:1165-1240) and ComputeNearInterac's per-block apply
+ * plus ScatterForward / per-target sum (:1311-1381) -- done matrix-free: block b
+ * adds  scale * sum_{s in b} K(x_t - y_s, n_s) * w_s * f_s  to each of its targets.
+ *
+ * Sources and targets of all blocks are concatenated arrays (AoS, as for
+ * sctlgpu_eval); a block names its ranges in them.  With trg_map (nt entries,
+ * output index of every target) results are added into v_out[trg_map[t]]
+ * (n_out outputs; several blocks may feed one output, as in the reference's
+ * scatter), otherwise v_out has one entry per target.  w_src (optional, one
+ * weight per source) multiplies the densities: quadrature weights of upsampled
+ * nodes, or negative smooth-quadrature weights for the subtraction.
+ *
+ * A plan fixes the block structure (the reference's Setup / ComputePotential
+ * split): creation validates the blocks, cuts them into work items sized by
+ * the autotuned table, sorts them by cost and uploads them; execution
+ * replays a captured CUDA graph (re-captured when the array pointers change).
+ * Execution takes device pointers and is asynchronous on `stream`.
+ */
+typedef struct sctlgpu_block {
+  int64_t src_begin, src_count; /* sources [src_begin, src_begin+src_count) */
+  int64_t trg_begin, trg_count; /* targets [trg_begin, trg_begin+trg_count) */
+} sctlgpu_block;
+typedef struct sctlgpu_near_plan_s* sctlgpu_near_plan;
+
+int sctlgpu_near_plan_create(sctlgpu_near_plan* plan, int kernel, int mode, int digits,
+                             int64_t nblk, const sctlgpu_block* blocks, /* host array */
+                             int64_t ns, int64_t nt,
+                             const int64_t* trg_map, int64_t n_out); /* host array or NULL */
+int sctlgpu_near_plan_execute(sctlgpu_near_plan plan, const void* r_trg, const void* r_src, const void* n_src,
+                              const void* v_src, const void* w_src, void* v_out, unsigned flags, void* stream);
+/* Work items, interactions per execution, and CUDA-graph kernel nodes of a plan. */
+int sctlgpu_near_plan_info(sctlgpu_near_plan plan, int64_t* n_items, int64_t* interactions, int* graph_kernels);
+/* Synchronises `stream` and returns SCTLGPU_ERR_DEVICE_TIMEOUT if a bounded device wait of the plan gave up. */
+int sctlgpu_near_plan_status(sctlgpu_near_plan plan, void* stream);
+/* Waits for the device (the plan's graph may still be running), then frees the plan. */
+int sctlgpu_near_plan_destroy(sctlgpu_near_plan plan);
+
+/*
+ * Runs (or returns the cached result of) the tile autotuner for the batched
+ * path on the current device: for each block-size class it times the source
+ * split factors 1, 2, 4, 8 on synthetic blocks and keeps the fastest.  Fills
+ * splits[i] for the SCTLGPU_NEAR_CLASSES classes (target-count buckets
+ * <=24, <=48, <=96, <=192, larger; each for source counts <=512 and larger).
+ * Environment SCTLGPU_NEAR_AUTOTUNE=0 replaces the measurement by the
+ * lane-filling rule.
+ */
+#define SCTLGPU_NEAR_CLASSES 10
+int sctlgpu_near_autotune(int kernel, int mode, int digits, int* splits);
+
+/*
  * sctlgpu_eval with SCTLGPU_MIXED and device pointers, for callers that cannot
  * allocate device memory.  This entry point has no counterpart in the
  * reference.  sctlgpu_eval takes its scratch (packed sources, partial sums)

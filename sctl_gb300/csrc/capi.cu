@@ -181,6 +181,14 @@ cudaError_t run_kmat(KmatCall& c, int mode, int d) {
 }
 
 }  // namespace
+
+// Shared with the other entry-point files (near_plan.cu).
+int runtime_device(int* dev, unsigned** status, int* sms) { return device_state(dev, status, sms); }
+int runtime_record(cudaError_t e) { return record(e); }
+int runtime_effective_digits(int mode, int digits) { return effective_digits(mode, digits); }
+int runtime_steps(int mode, int digits) { return steps_for(mode, digits); }
+int runtime_mixed_df_max_digits() { return kMixedDfMaxDigits; }
+
 }  // namespace sctlgpu
 
 using namespace sctlgpu;

@@ -149,9 +149,12 @@ __global__ void bbox_kernel(int64_t n, const Real* __restrict__ x, BBox* bb) {
   }
 }
 
+// Packs AoS sources into records; `w` (optional) scales every density, the
+// quadrature weight of a source node in a near-field correction.
 template <int KER, int MODE, class Real>
 __global__ void pack_sources_kernel(int64_t ns, const Real* __restrict__ xs, const Real* __restrict__ nrm,
-                                    const Real* __restrict__ f, Rec<KER, MODE>* __restrict__ out, const BBox* bb) {
+                                    const Real* __restrict__ f, Rec<KER, MODE>* __restrict__ out, const BBox* bb,
+                                    const Real* __restrict__ w = nullptr) {
   using R = Rec<KER, MODE>;
   MixedFrame fr;
   if (MODE == MODE_MXDF || MODE == MODE_MXLO) fr = frame_from_bbox(bb);
@@ -159,42 +162,45 @@ __global__ void pack_sources_kernel(int64_t ns, const Real* __restrict__ xs, con
     R r;
     memset(&r, 0, sizeof(R));
     if constexpr (MODE == MODE_F64 || MODE == MODE_F32) {
+      const Real ws = w ? w[s] : Real(1);
       r.x = xs[s * 3 + 0];
       r.y = xs[s * 3 + 1];
       r.z = xs[s * 3 + 2];
       if constexpr (KER == KER_LFXU) {
-        r.f = f[s];
+        r.f = f[s] * ws;
       } else if constexpr (KER == KER_LDXU) {  // fold the density into the normal: m = f n
-        r.m0 = f[s] * nrm[s * 3 + 0];
-        r.m1 = f[s] * nrm[s * 3 + 1];
-        r.m2 = f[s] * nrm[s * 3 + 2];
+        const Real fs = f[s] * ws;
+        r.m0 = fs * nrm[s * 3 + 0];
+        r.m1 = fs * nrm[s * 3 + 1];
+        r.m2 = fs * nrm[s * 3 + 2];
       } else if constexpr (KER == KER_SFXU) {
-        r.f0 = f[s * 3 + 0];
-        r.f1 = f[s * 3 + 1];
-        r.f2 = f[s * 3 + 2];
+        r.f0 = f[s * 3 + 0] * ws;
+        r.f1 = f[s * 3 + 1] * ws;
+        r.f2 = f[s * 3 + 2] * ws;
       } else {
         r.n0 = nrm[s * 3 + 0];
         r.n1 = nrm[s * 3 + 1];
         r.n2 = nrm[s * 3 + 2];
-        r.f0 = f[s * 3 + 0];
-        r.f1 = f[s * 3 + 1];
-        r.f2 = f[s * 3 + 2];
+        r.f0 = f[s * 3 + 0] * ws;
+        r.f1 = f[s * 3 + 1] * ws;
+        r.f2 = f[s * 3 + 2] * ws;
       }
     } else {
+      const double ws = w ? (double)w[s] : 1.0;
       split_coord(fr, 0, (double)xs[s * 3 + 0], r.xh, r.xl);
       split_coord(fr, 1, (double)xs[s * 3 + 1], r.yh, r.yl);
       split_coord(fr, 2, (double)xs[s * 3 + 2], r.zh, r.zl);
       if constexpr (KER == KER_LFXU) {
-        split_val((double)f[s], r.fh, r.fl);
+        split_val((double)f[s] * ws, r.fh, r.fl);
       } else if constexpr (KER == KER_LDXU) {
-        const double fs = (double)f[s];
+        const double fs = (double)f[s] * ws;
         split_val(fs * (double)nrm[s * 3 + 0], r.mh0, r.ml0);
         split_val(fs * (double)nrm[s * 3 + 1], r.mh1, r.ml1);
         split_val(fs * (double)nrm[s * 3 + 2], r.mh2, r.ml2);
       } else {
-        split_val((double)f[s * 3 + 0], r.fh0, r.fl0);
-        split_val((double)f[s * 3 + 1], r.fh1, r.fl1);
-        split_val((double)f[s * 3 + 2], r.fh2, r.fl2);
+        split_val((double)f[s * 3 + 0] * ws, r.fh0, r.fl0);
+        split_val((double)f[s * 3 + 1] * ws, r.fh1, r.fl1);
+        split_val((double)f[s * 3 + 2] * ws, r.fh2, r.fl2);
         if constexpr (KER == KER_SDXU) {
           split_val((double)nrm[s * 3 + 0], r.nh0, r.nl0);
           split_val((double)nrm[s * 3 + 1], r.nh1, r.nl1);
@@ -230,6 +236,7 @@ struct PlainPair {
   }
   __device__ __forceinline__ static void flush(Trg&) {}
   __device__ static double result(const Trg& t, int k) { return (double)t.acc[k]; }
+  __device__ static void add_partial(Trg& t, int k, double v) { t.acc[k] += (Real)v; }
 
   template <class RecT>
   __device__ __forceinline__ static void apply(Trg& t, const RecT& s) {
@@ -270,16 +277,29 @@ struct Pair<KER, MODE_MXLO, NEWTON> {
   static constexpr int K1 = KDims<KER>::K1;
   struct Trg {
     float xh[3], xl[3];
-    kahan acc[K1];
+    kahan acc[K1];   // compensated FP32 sum over the current source tile
+    double tot[K1];  // FP64 sum of the tile sums
   };
   __device__ static void load_trg(Trg& t, const double* r, int64_t i, const MixedFrame& fr) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) split_coord(fr, k, r[i * 3 + k], t.xh[k], t.xl[k]);
 #pragma unroll
-    for (int k = 0; k < K1; ++k) t.acc[k] = {0.f, 0.f};
+    for (int k = 0; k < K1; ++k) {
+      t.acc[k] = {0.f, 0.f};
+      t.tot[k] = 0.0;
+    }
   }
-  __device__ __forceinline__ static void flush(Trg&) {}
-  __device__ static double result(const Trg& t, int k) { return (double)t.acc[k].s - (double)t.acc[k].c; }
+  __device__ __forceinline__ static void flush(Trg& t) {
+#pragma unroll
+    for (int k = 0; k < K1; ++k) {
+      t.tot[k] += (double)t.acc[k].s - (double)t.acc[k].c;
+      t.acc[k] = {0.f, 0.f};
+    }
+  }
+  __device__ static double result(const Trg& t, int k) {
+    return t.tot[k] + ((double)t.acc[k].s - (double)t.acc[k].c);
+  }
+  __device__ static void add_partial(Trg& t, int k, double v) { t.tot[k] += v; }
 
   template <class RecT>
   __device__ __forceinline__ static void apply(Trg& t, const RecT& s) {
@@ -358,6 +378,7 @@ struct Pair<KER, MODE_MXDF, NEWTON> {
   __device__ static double result(const Trg& t, int k) {
     return t.tot[k] + ((double)t.acc[k].h + (double)t.acc[k].l);
   }
+  __device__ static void add_partial(Trg& t, int k, double v) { t.tot[k] += v; }
 
   template <class RecT>
   __device__ __forceinline__ static void apply(Trg& t, const RecT& s) {

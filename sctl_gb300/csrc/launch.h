@@ -62,3 +62,33 @@ cudaError_t kmat_mixed_df(const KmatCall& c);
 cudaError_t compute_bbox(cudaStream_t s, int64_t nt, const double* r_trg, int64_t ns, const double* r_src, BBox* bb);
 
 }  // namespace sctlgpu
+
+namespace sctlgpu {
+
+struct NearParams;
+
+// Per (kernel, arithmetic, Newton) entry points of the batched near-field path.
+struct NearOps {
+  size_t rec_bytes = 0;  // sizeof(Rec)
+  int T = 1;             // targets per thread
+  int occ = 1;           // resident CTAs per SM
+  size_t smem = 0;       // dynamic shared memory of the persistent kernel
+  cudaError_t (*pack)(cudaStream_t, int64_t ns, const void* xs, const void* nrm, const void* f, const void* w,
+                      void* recs, const BBox* bb, int sms) = nullptr;
+  cudaError_t (*launch)(cudaStream_t, unsigned ctas, const NearParams& p) = nullptr;
+};
+
+// Internal arithmetic of a batched plan.
+enum { NEAR_F64 = 0, NEAR_F32 = 1, NEAR_MXLO = 2, NEAR_MXDF = 3 };
+NearOps near_ops_f64(int kernel, int newton);
+NearOps near_ops_f32(int kernel, int newton);
+NearOps near_ops_mixed(int kernel, int imode, int newton);
+
+// Runtime helpers of capi.cu shared with the other entry-point files.
+int runtime_device(int* dev, unsigned** status, int* sms);
+int runtime_record(cudaError_t e);
+int runtime_effective_digits(int mode, int digits);
+int runtime_steps(int mode, int digits);
+int runtime_mixed_df_max_digits();
+
+}  // namespace sctlgpu

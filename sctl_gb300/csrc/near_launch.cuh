@@ -1,0 +1,56 @@
+// Builds the NearOps table entry of one (kernel, arithmetic, Newton) variant.
+#pragma once
+
+#include "launch_direct.cuh"
+#include "near.cuh"
+
+namespace sctlgpu {
+
+template <int KER, int MODE, int NEWTON>
+NearOps make_near_ops() {
+  using RecT = Rec<KER, MODE>;
+  using Cfg = NearCfg<KER, MODE>;
+  using Real = typename std::conditional<MODE == MODE_F32, float, double>::type;
+  NearOps o;
+  o.rec_bytes = sizeof(RecT);
+  o.T = Cfg::T;
+  o.smem = 2 * Cfg::S * sizeof(RecT) + (size_t)NEAR_THREADS * Cfg::T * KDims<KER>::K1 * sizeof(double) +
+           2 * sizeof(uint64_t);
+  static int occ = [&] {
+    int v = 0;
+    if (o.smem > 48 * 1024)
+      cudaFuncSetAttribute(near_batch_kernel<KER, MODE, NEWTON>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)o.smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, near_batch_kernel<KER, MODE, NEWTON>, NEAR_THREADS, o.smem);
+    return v > 0 ? v : 1;
+  }();
+  o.occ = occ;
+  o.pack = [](cudaStream_t st, int64_t ns, const void* xs, const void* nrm, const void* f, const void* w, void* recs,
+              const BBox* bb, int sms) -> cudaError_t {
+    if (ns <= 0) return cudaSuccess;
+    pack_sources_kernel<KER, MODE, Real><<<grid_for(ns, 256, sms), 256, 0, st>>>(
+        ns, (const Real*)xs, (const Real*)nrm, (const Real*)f, (RecT*)recs, bb, (const Real*)w);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+  };
+  o.launch = [](cudaStream_t st, unsigned ctas, const NearParams& p) -> cudaError_t {
+    const size_t smem = 2 * Cfg::S * sizeof(RecT) + (size_t)NEAR_THREADS * Cfg::T * KDims<KER>::K1 * sizeof(double) +
+                        2 * sizeof(uint64_t);
+    near_batch_kernel<KER, MODE, NEWTON><<<ctas, NEAR_THREADS, smem, st>>>(p);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+  };
+  return o;
+}
+
+template <int MODE, int NEWTON>
+NearOps near_ops_for(int kernel) {
+  switch (kernel) {
+    case KER_LFXU: return make_near_ops<KER_LFXU, MODE, NEWTON>();
+    case KER_LDXU: return make_near_ops<KER_LDXU, MODE, NEWTON>();
+    case KER_SFXU: return make_near_ops<KER_SFXU, MODE, NEWTON>();
+    default: return make_near_ops<KER_SDXU, MODE, NEWTON>();
+  }
+}
+
+}  // namespace sctlgpu

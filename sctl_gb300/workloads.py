@@ -61,3 +61,47 @@ def clusters(n_src=1 << 20, n_trg=1 << 20, kernel=0, seed=0, n_clusters=64, sigm
 
 
 GENERATORS = {"cube": cube, "sphere_ball": sphere_ball, "clusters": clusters}
+
+
+def near_blocks(n_blocks=4096, kernel=1, seed=0, panel=False, diameter=0.1):
+    """Uneven near-field blocks: block b has Ns = round(100*64^u) sources
+    (or 100*k^2, k = 1..8, with panel=True: 10x10 panels upsampled k x per
+    side) on a random smooth patch of the given diameter, unit random normals,
+    and Nt = round(16*128^v) targets within one patch diameter off the patch;
+    u, v ~ U(0,1).  Blocks sit at random places in [0, 10]^3.
+
+    Returns concatenated arrays and an (n_blocks, 4) int64 block table of
+    (src_begin, src_count, trg_begin, trg_count)."""
+    rng = np.random.default_rng(seed)
+    sd = SRC_DIM[kernel]
+    if panel:
+        ns = 100 * rng.integers(1, 9, n_blocks) ** 2
+    else:
+        ns = np.rint(100.0 * 64.0 ** rng.uniform(0, 1, n_blocks)).astype(np.int64)
+    nt = np.rint(16.0 * 128.0 ** rng.uniform(0, 1, n_blocks)).astype(np.int64)
+    xs, xn, f, xt = [], [], [], []
+    for b in range(n_blocks):
+        c = rng.uniform(0.0, 10.0, 3)
+        q, _ = np.linalg.qr(rng.standard_normal((3, 3)))  # random orientation
+        kap = rng.uniform(-3.0, 3.0, 2)
+
+        def surf(m):
+            uv = rng.uniform(-0.5, 0.5, (m, 2)) * diameter
+            z = 0.5 * (kap[0] * uv[:, 0] ** 2 + kap[1] * uv[:, 1] ** 2)
+            p = np.stack([uv[:, 0], uv[:, 1], z], 1)
+            nrm = np.stack([-kap[0] * uv[:, 0], -kap[1] * uv[:, 1], np.ones(m)], 1)
+            return p, _unit(nrm)
+
+        p, _ = surf(int(ns[b]))
+        xs.append(c + p @ q.T)
+        xn.append(_unit(rng.standard_normal((int(ns[b]), 3))))
+        f.append(rng.standard_normal((int(ns[b]), sd)))
+        pt, nt_ = surf(int(nt[b]))
+        h = diameter * rng.uniform(0.01, 1.0, int(nt[b]))
+        xt.append(c + (pt + nt_ * h[:, None]) @ q.T)
+    sb = np.concatenate([[0], np.cumsum(ns)[:-1]])
+    tb = np.concatenate([[0], np.cumsum(nt)[:-1]])
+    blocks = np.stack([sb, ns, tb, nt], 1).astype(np.int64)
+    return dict(r_trg=np.concatenate(xt), r_src=np.concatenate(xs),
+                n_src=np.concatenate(xn) if NORMAL_DIM[kernel] else np.zeros((0, 3)),
+                v_src=np.concatenate(f), blocks=blocks)
