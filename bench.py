@@ -161,6 +161,101 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _ev_ms(torch, fn, reps=3):
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 1e30
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return best
+
+
+def near_field_section(torch, stream):
+    """4096 uneven Laplace3D_DxU near blocks (100..6400 sources, 16..2048 targets), one persistent
+    launch per plan execution (CUDA-graph replay), FP64 vs mixed digits 10."""
+    from oracle import oracle as O
+    from sctl_gb300 import workloads as W
+    from sctl_gb300.near import NearPlan
+    k = 1
+    d = W.near_blocks(4096, k, seed=0)
+    blocks = d["blocks"]
+    ns, nt = d["r_src"].shape[0], d["r_trg"].shape[0]
+    pairs = int((blocks[:, 1] * blocks[:, 3]).sum())
+    dd = {a: torch.from_numpy(np.ascontiguousarray(v)).cuda() for a, v in d.items() if a != "blocks"}
+    # algorithmic bytes of one execution (FP64 inputs): sources x, n, f; targets x in, potential out
+    alg_bytes = ns * (3 + 3 + 1) * 8 + nt * (3 * 8 + 8)
+    res = {"workload": "4096 blocks, Ns=round(100*64^u), Nt=round(16*128^v), Laplace3D_DxU, seed 0",
+           "interactions": pairs, "algorithmic_bytes": alg_bytes}
+    outs = {}
+    for mode, dg in (("mixed", 10), ("f64", -1)):
+        plan = NearPlan(k, blocks, ns, nt, mode=mode, digits=dg)
+        out = torch.zeros(nt, dtype=torch.float64, device="cuda")
+        run = lambda: plan.execute(dd["r_trg"], dd["r_src"], dd["n_src"], dd["v_src"], out)  # noqa: E731
+        run()
+        ms = _ev_ms(torch, run)
+        outs[mode] = out.cpu().numpy()
+        res[f"{mode}_d{dg}"] = {"ms": ms, "gint_s": pairs / (ms * 1e-3) / 1e9, "hbm_gb_s": alg_bytes / (ms * 1e-3) / 1e9,
+                               **plan.info()}
+    res["mixed_vs_f64_speedup"] = res["f64_d-1"]["ms"] / res["mixed_d10"]["ms"]
+    sel = blocks[:200]
+    ref = np.concatenate([O.eval(k, d["r_trg"][t0:t0 + m], d["r_src"][s0:s0 + n], d["n_src"][s0:s0 + n],
+                                 d["v_src"][s0:s0 + n]) for s0, n, t0, m in sel])
+    end = int(sel[-1, 2] + sel[-1, 3])
+    res["mixed_rel_l2_vs_fp64_oracle_200_blocks"] = O.rel_l2(outs["mixed"][:end], ref)
+    res["f64_rel_l2_vs_fp64_oracle_200_blocks"] = O.rel_l2(outs["f64"][:end], ref)
+    return res
+
+
+def cluster_section(torch, stream):
+    """64 Gaussian clusters (sigma 1e-3), 2^20 sources, Laplace FxU / Stokes FxU, error vs the FP64
+    oracle on 128 targets for digits 6, 8, 10, 12 (mixed) and the FP64 form."""
+    import sctl_gb300 as S
+    from oracle import oracle as O
+    from sctl_gb300 import workloads as W
+    res = {}
+    for k in (0, 2):
+        d = W.clusters(1 << 20, 1 << 10, k, seed=0)
+        sub = {a: (v[::8][:128] if a == "r_trg" else v) for a, v in d.items()}
+        ref = O.eval(k, sub["r_trg"], sub["r_src"], sub["n_src"], sub["v_src"])
+        dd = {a: torch.from_numpy(np.ascontiguousarray(v)).cuda() for a, v in sub.items()}
+        kern = [S.Laplace3D_FxU, S.Laplace3D_DxU, S.Stokes3D_FxU, S.Stokes3D_DxU][k]
+        row = {}
+        for mode, dg in (("mixed", 6), ("mixed", 8), ("mixed", 10), ("mixed", 12), ("f64", -1)):
+            out = kern.Eval(None, dd["r_trg"], dd["r_src"], dd["n_src"], dd["v_src"], digits=dg, mode=mode)
+            torch.cuda.synchronize()
+            row[f"{mode}_d{dg}_rel_l2"] = O.rel_l2(out.cpu().numpy(), ref)
+        res[NAMES[k]] = row
+    return res
+
+
+def cube_section(torch, stream):
+    """8192 x 8192 unit-cube Laplace FxU, FP64 digits 14: GPU vs the CPU port on all host cores."""
+    import sctl_gb300 as S
+    from oracle import oracle as O
+    from sctl_gb300 import workloads as W
+    d = W.cube(8192, 8192, 0, 0)
+    dd = {a: torch.from_numpy(np.ascontiguousarray(v)).cuda() for a, v in d.items()}
+    out = torch.zeros(8192, dtype=torch.float64, device="cuda")
+    run = lambda: S.Laplace3D_FxU.Eval(out, dd["r_trg"], dd["r_src"], dd["n_src"], dd["v_src"], digits=14,  # noqa
+                                       mode="f64")
+    run()
+    out.zero_()
+    run()
+    torch.cuda.synchronize()
+    gpu = out.cpu().numpy()
+    ms = _ev_ms(torch, run)
+    t0 = time.perf_counter()
+    ref = O.eval(0, d["r_trg"], d["r_src"], d["n_src"], d["v_src"])
+    cpu_s = time.perf_counter() - t0
+    return {"gpu_ms": ms, "gpu_gint_s": 8192 * 8192 / (ms * 1e-3) / 1e9, "cpu_port_s": cpu_s,
+            "cpu_port_gint_s": 8192 * 8192 / cpu_s / 1e9, "cpu_cores": O.max_threads(),
+            "rel_l2_vs_cpu": O.rel_l2(gpu, ref)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -168,7 +263,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--n", type=int, default=N_TRG, help="targets per rank (sources fixed at 2^20)")
+    ap.add_argument("--n", type=int, default=N_TRG, help="targets per rank")
+    ap.add_argument("--ns", type=int, default=N_SRC, help="sources")
+    ap.add_argument("--kernels", default="1,2,3", help="kernel ids of the step (default: the three sphere/ball kernels)")
+    ap.add_argument("--quick", action="store_true", help="timed region only (for profiler runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -181,6 +279,9 @@ def main():
     from sctl_gb300 import capi
     from sctl_gb300 import workloads as W
 
+    global KERNELS, N_SRC
+    KERNELS = [int(x) for x in args.kernels.split(",")]
+    N_SRC = args.ns
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     if world > 1:
@@ -237,6 +338,13 @@ def main():
     pairs_step = len(KERNELS) * N_SRC * args.n
     value = pairs_step * world / (ms * 1e-3) / 1e9
     clocks = clk.summary()
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": "Laplace/Stokes Ginteractions/s mixed vs FP64 @1e-10", "value": value,
+                              "unit": "Ginteractions/s", "ms_per_step": ms, "quick": True,
+                              "gpu_launches": launches, "kernels": KERNELS, "n_trg": args.n, "n_src": N_SRC}),
+                  flush=True)
+        return
 
     # --- everything below is outside the timed region ---
     # FP64 and FP32 plain forms on a 2^16-target slice, for the "mixed vs FP64" ratio.
@@ -330,6 +438,12 @@ def main():
                 "achieved_fp32_tflops_equiv": achieved * (ALG_OPS[dom][0]) / 1e12,
                 "launch_ms": dom_ms}
 
+    extras = {}
+    if rank == 0:
+        extras["near_field_blocks"] = near_field_section(torch, stream)
+        extras["precision_stress_clusters"] = cluster_section(torch, stream)
+        extras["cube8192_fp64_d14"] = cube_section(torch, stream)
+
     line = {"metric": "Laplace/Stokes Ginteractions/s mixed vs FP64 @1e-10", "value": value,
             "unit": "Ginteractions/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -340,7 +454,7 @@ def main():
                        "interactions_per_step_per_gpu": pairs_step, "parallelism": f"replicas x{world}",
                        "l2": "256 MB buffer written between timed steps; per-step inputs 0.4 GB > 129 MB L2"},
             "gpu_launches": launches, "clocks": clocks, "e2e": e2e, "roofline": roofline,
-            "per_kernel": detail}
+            "per_kernel": detail, **extras}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0:

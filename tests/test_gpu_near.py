@@ -30,8 +30,10 @@ def dev(torch, d, dtype=None):
 
 
 @pytest.mark.parametrize("k", range(4))
+# FP32: blocks sit at |x| ~ 10 with targets 1e-3 off the patch, so FP32 coordinates alone
+# carry ~1e-6 * 10 / 1e-3 = 1e-2 relative error on the closest double-layer pairs.
 @pytest.mark.parametrize("mode,digits,tol", [("f64", -1, 1e-12), ("mixed", 10, 1e-10), ("mixed", 6, 2e-6),
-                                             ("f32", -1, 5e-5)])
+                                             ("f32", -1, 2e-3)])
 def test_near_batch_matches_oracle(cuda, k, mode, digits, tol):
     torch = cuda
     d = W.near_blocks(160, k, seed=k)
