@@ -257,6 +257,7 @@ def cube_section(torch, stream):
 
 
 def main():
+    global KERNELS, N_SRC
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
@@ -279,7 +280,6 @@ def main():
     from sctl_gb300 import capi
     from sctl_gb300 import workloads as W
 
-    global KERNELS, N_SRC
     KERNELS = [int(x) for x in args.kernels.split(",")]
     N_SRC = args.ns
     rank, world, local = dist_env()
