@@ -1,0 +1,71 @@
+"""World-size-2 gloo runs of the multi-rank direct sum (ring over ranks, as
+ParticleFMM::EvalDirect) and the max-over-ranks timing reduction, on CPU with
+the oracle as the per-rank evaluator."""
+import os
+import socket
+
+import numpy as np
+import pytest
+import torch
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _worker(rank, world, port, kernel, out_q):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        from oracle import oracle as O
+        from sctl_gb300 import parallel as P
+        from sctl_gb300 import workloads as W
+        d = W.sphere_ball(701, 333, kernel, seed=5)
+        nd, sd, td = O.DIMS[kernel]
+        t0, t1 = P.partition_range(333, rank, world)
+        s0, s1 = P.partition_range(701, rank, world)
+        tt = lambda a: torch.from_numpy(np.ascontiguousarray(a))  # noqa: E731
+
+        def evaluator(v, xt, xs, xn, f):
+            res = O.eval(kernel, xt.numpy(), xs.numpy(), xn.numpy() if nd else None, f.numpy(),
+                         v_trg=v.numpy().copy())
+            v.copy_(torch.from_numpy(res))
+
+        v = P.eval_direct(evaluator, tt(d["r_trg"][t0:t1]), tt(d["r_src"][s0:s1]),
+                          tt(d["n_src"][s0:s1] if nd else np.zeros((0, 3))), tt(d["v_src"][s0:s1]), td)
+        ref = O.eval(kernel, d["r_trg"][t0:t1], d["r_src"], d["n_src"], d["v_src"])
+        m = P.max_over_ranks(float(rank + 1))
+        out_q.put((rank, float(O.rel_l2(v.numpy(), ref)), m))
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("kernel", [1, 2])
+def test_ring_eval_direct_world2(kernel):
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, kernel, q)) for r in range(2)]
+    [p.start() for p in procs]
+    res = [q.get(timeout=120) for _ in range(2)]
+    [p.join(timeout=60) for p in procs]
+    assert all(p.exitcode == 0 for p in procs)
+    for rank, err, m in res:
+        assert err < 1e-13, (rank, err)
+        assert m == 2.0
+
+
+def test_partition_range_matches_reference_rule():
+    from sctl_gb300.parallel import partition_range
+    n, world = 1001, 7
+    parts = [partition_range(n, r, world) for r in range(world)]
+    assert parts[0][0] == 0 and parts[-1][1] == n
+    assert all(parts[i][1] == parts[i + 1][0] for i in range(world - 1))
+    assert max(b - a for a, b in parts) - min(b - a for a, b in parts) <= 1
