@@ -279,6 +279,7 @@ def main():
     import sctl_gb300 as S
     from sctl_gb300 import capi
     from sctl_gb300 import workloads as W
+    from sctl_gb300.parallel import max_over_ranks
 
     KERNELS = [int(x) for x in args.kernels.split(",")]
     N_SRC = args.ns
@@ -331,10 +332,7 @@ def main():
     capi.set_timing(False)
     step_ms = [a.elapsed_time(b) for a, b in ev]
     ms = sum(step_ms) / len(step_ms)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms)
     pairs_step = len(KERNELS) * N_SRC * args.n
     value = pairs_step * world / (ms * 1e-3) / 1e9
     clocks = clk.summary()
@@ -409,10 +407,7 @@ def main():
             kern_objs[k].Eval(h["out"], h["r_trg"], h["r_src"], h["n_src"], h["v_src"], digits=DIGITS, mode="mixed")
     barrier()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s)
     e2e = {"value": pairs_step * world / e2e_s / 1e9, "unit": "Ginteractions/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h}
 
