@@ -143,6 +143,25 @@ int sctlgpu_near_plan_status(sctlgpu_near_plan plan, void* stream);
 int sctlgpu_near_plan_destroy(sctlgpu_near_plan plan);
 
 /*
+ * Near-singular correction of p x p (p = 10) Chebyshev panels -- the plugin point
+ * of ElementListBase::NearInterac / EvalNearInterac (boundary_integral.hpp:164-239)
+ * for a surface given only by its panel nodes.  For every (target, panel) pair
+ * the panel's geometry and density are interpolated from its nodes and
+ * integrated with adaptive dyadic refinement (boxes accepted at distance >=
+ * alpha x diameter, 10 x 10 Gauss-Legendre per box, at most max_depth levels),
+ * the panel's smooth-rule part (nodes X, normals N, weights Q) is subtracted
+ * (KNearSubtract, boundary_integral.txx:1165-1240), and scale x the result is
+ * atomically added to v_out[trg_map ? trg_map[t] : t].  Kernels: Laplace3D_FxU,
+ * Laplace3D_DxU (double arrays, FP64 arithmetic); device pointers, asynchronous on
+ * `stream`.  Out-of-range pair indices are skipped and flagged in the device status.
+ */
+int sctlgpu_panel_near_correction(int kernel, int64_t n_pairs, const int64_t* pair_trg, const int64_t* pair_panel,
+                                  int64_t nt, const double* r_trg, int64_t n_panels, const double* X,
+                                  const double* N, const double* Q, const double* sigma,
+                                  const int64_t* trg_map, int64_t n_out, double alpha, int max_depth,
+                                  double* v_out, void* stream);
+
+/*
  * Runs (or returns the cached result of) the tile autotuner for the batched
  * path on the current device: for each block-size class it times the source
  * split factors 1, 2, 4, 8 on synthetic blocks and keeps the fastest.  Fills

@@ -1,0 +1,342 @@
+// Near-singular panel quadrature for the Laplace double layer (and single
+// layer) on p x p Chebyshev panels: the "upsampled" near-field path of a
+// boundary element list (the NearInterac plugin contract,
+// boundary_integral.hpp:164-239), done adaptively on the GPU.
+//
+// For a (target, panel) pair the kernel refines the panel's parameter square
+// [0,1]^2 level by level (a box is accepted once its distance to the target is
+// at least `alpha` times its physical diameter; the legacy quadrature's dyadic
+// refinement toward the target, boundary_quadrature.hpp:364-478, is the model),
+// integrates every accepted box with a 10 x 10 Gauss-Legendre rule on geometry
+// and density interpolated from the panel's nodes (barycentric Lagrange,
+// as LagrangeInterp does on the CPU), and subtracts the panel's own smooth-rule
+// contribution (the KNearSubtract convention, boundary_integral.txx:1165-1240).
+// The result is the correction that turns the far-field smooth sum into the
+// accurate value; it is added into v_out[map[target]].
+//
+// One warp per pair; each round, each lane tests one queued box (interpolation
+// at the box centre), then the lanes share the Gauss nodes of the accepted
+// boxes.  FP64 throughout; loops are bounded by the depth and queue limits.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/sctlgpu.h"
+#include "launch.h"
+
+namespace sctlgpu {
+namespace {
+
+constexpr int PQ_P = 10;          // panel order
+constexpr int PQ_NODES = PQ_P * PQ_P;
+constexpr int PQ_GL = 10;         // Gauss-Legendre points per box side
+constexpr int PQ_WARPS = 4;       // warps per CTA
+constexpr int PQ_QUEUE = 128;     // boxes per round (per warp)
+constexpr int PQ_MAX_DEPTH = 22;  // box corners k * 2^-depth stay exact in FP32
+
+struct PanelWarpSmem {
+  double F[4][PQ_NODES];          // x, y, z, sigma at the panel nodes
+  float box[2][PQ_QUEUE][3];      // (s0, t0, size) of the boxes of this and the next round (dyadic: exact)
+  float leaf[PQ_QUEUE][3];
+};
+
+__constant__ double c_gl_x[PQ_GL], c_gl_w[PQ_GL];
+
+struct Basis {
+  double l[PQ_P], d[PQ_P];
+};
+
+// Barycentric Lagrange basis on the first-kind Chebyshev points of [0,1] and
+// its derivative: l_a(s) = (w_a/(s-x_a)) / sum_b w_b/(s-x_b),
+// l_a'(s) = l_a(s) * (sum_b w_b/(s-x_b)^2 / sum_b w_b/(s-x_b) - 1/(s-x_a)).
+__device__ void basis(double s, Basis& B) {
+  double xs[PQ_P], ws[PQ_P];
+  int hit = -1;
+#pragma unroll
+  for (int a = 0; a < PQ_P; ++a) {
+    xs[a] = 0.5 - 0.5 * cospi((2.0 * a + 1.0) / (2.0 * PQ_P));
+    ws[a] = ((a & 1) ? -1.0 : 1.0) * sinpi((2.0 * a + 1.0) / (2.0 * PQ_P));
+    if (s == xs[a]) hit = a;
+  }
+  if (hit >= 0) {  // at a node: l is a unit vector; l' from the differentiation matrix row
+#pragma unroll
+    for (int a = 0; a < PQ_P; ++a) {
+      B.l[a] = (a == hit) ? 1.0 : 0.0;
+      B.d[a] = 0.0;
+    }
+    double diag = 0.0;
+#pragma unroll
+    for (int a = 0; a < PQ_P; ++a)
+      if (a != hit) {
+        B.d[a] = (ws[a] / ws[hit]) / (xs[hit] - xs[a]);
+        diag -= B.d[a];
+      }
+    B.d[hit] = diag;
+    return;
+  }
+  double T = 0.0, U = 0.0, t[PQ_P];
+#pragma unroll
+  for (int a = 0; a < PQ_P; ++a) {
+    const double r = 1.0 / (s - xs[a]);
+    t[a] = ws[a] * r;
+    T += t[a];
+    U += t[a] * r;
+  }
+  const double iT = 1.0 / T, UT = U * iT;
+#pragma unroll
+  for (int a = 0; a < PQ_P; ++a) {
+    const double r = 1.0 / (s - xs[a]);
+    B.l[a] = t[a] * iT;
+    B.d[a] = B.l[a] * (UT - r);  // d/ds of t_a/T = (-t_a r T + t_a U) / T^2
+  }
+}
+
+// Geometry and density at (s, t): position, tangents (per unit s, t) and sigma.
+__device__ void interp(const double (*F)[PQ_NODES], double s, double t, double X[3], double Xs[3], double Xt[3],
+                       double& sig, bool need_sig) {
+  Basis A, B;
+  basis(s, A);
+  basis(t, B);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    if (c == 3 && !need_sig) break;
+    double v = 0, vs = 0, vt = 0;
+    for (int a = 0; a < PQ_P; ++a) {
+      double r = 0, rt = 0;
+#pragma unroll
+      for (int b = 0; b < PQ_P; ++b) {
+        const double f = F[c][a * PQ_P + b];
+        r = fma(B.l[b], f, r);
+        rt = fma(B.d[b], f, rt);
+      }
+      v = fma(A.l[a], r, v);
+      vs = fma(A.d[a], r, vs);
+      vt = fma(A.l[a], rt, vt);
+    }
+    if (c < 3) {
+      X[c] = v;
+      Xs[c] = vs;
+      Xt[c] = vt;
+    } else {
+      sig = v;
+    }
+  }
+}
+
+template <int KER>
+__device__ __forceinline__ double kernel_val(const double r[3], const double n[3]) {
+  const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+  if (!(r2 > 0)) return 0.0;
+  const double ri = 1.0 / sqrt(r2);
+  if (KER == 0) return ri;  // Laplace3D_FxU
+  return (r[0] * n[0] + r[1] * n[1] + r[2] * n[2]) * ri * ri * ri;
+}
+
+struct PanelParams {
+  int64_t n_pairs, n_panels, nt, n_out;
+  const int64_t* pair_trg;
+  const int64_t* pair_panel;
+  const int64_t* trg_map;   // output index of a target (or null: identity)
+  const double* r_trg;      // AoS targets
+  const double* X;          // [np][100][3] node coordinates
+  const double* N;          // [np][100][3] unit normals
+  const double* Q;          // [np][100]    smooth-rule weights
+  const double* sigma;      // [np][100]    density
+  double alpha;
+  int max_depth;
+  double scale;
+  double* out;
+  unsigned* status;
+};
+
+template <int KER>
+__global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel(PanelParams p) {
+  __shared__ PanelWarpSmem sm_all[PQ_WARPS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  PanelWarpSmem& sm = sm_all[warp];
+  for (int64_t pr = (int64_t)blockIdx.x * PQ_WARPS + warp; pr < p.n_pairs; pr += (int64_t)gridDim.x * PQ_WARPS) {
+    const int64_t tix = p.pair_trg[pr], pix = p.pair_panel[pr];
+    const int64_t oix = p.trg_map ? (tix >= 0 && tix < p.nt ? p.trg_map[tix] : -1) : tix;
+    if (tix < 0 || tix >= p.nt || pix < 0 || pix >= p.n_panels || oix < 0 || oix >= p.n_out) {
+      if (lane == 0 && p.status) atomicOr(p.status, 4u);  // index out of range: pair skipped
+      continue;
+    }
+    const double xt[3] = {p.r_trg[tix * 3], p.r_trg[tix * 3 + 1], p.r_trg[tix * 3 + 2]};
+    __syncwarp();
+    for (int q = lane; q < PQ_NODES; q += 32) {
+      sm.F[0][q] = p.X[(pix * PQ_NODES + q) * 3 + 0];
+      sm.F[1][q] = p.X[(pix * PQ_NODES + q) * 3 + 1];
+      sm.F[2][q] = p.X[(pix * PQ_NODES + q) * 3 + 2];
+      sm.F[3][q] = p.sigma[pix * PQ_NODES + q];
+    }
+    __syncwarp();
+    double acc = 0.0;
+    // Smooth-rule part of this panel, to be subtracted.
+    for (int q = lane; q < PQ_NODES; q += 32) {
+      const double r[3] = {xt[0] - sm.F[0][q], xt[1] - sm.F[1][q], xt[2] - sm.F[2][q]};
+      const double n[3] = {p.N[(pix * PQ_NODES + q) * 3], p.N[(pix * PQ_NODES + q) * 3 + 1],
+                           p.N[(pix * PQ_NODES + q) * 3 + 2]};
+      acc -= kernel_val<KER>(r, n) * sm.F[3][q] * p.Q[pix * PQ_NODES + q];
+    }
+    // Level-by-level refinement.
+    int cur = 0, ncur = 1, nleaf = 0;
+    if (lane == 0) {
+      sm.box[0][0][0] = 0.0f;
+      sm.box[0][0][1] = 0.0f;
+      sm.box[0][0][2] = 1.0f;
+    }
+    __syncwarp();
+    for (int depth = 0; depth <= p.max_depth && ncur > 0; ++depth) {
+      // each lane tests boxes of the current round
+      int nnext = 0;
+      nleaf = 0;
+      for (int base = 0; base < ncur; base += 32) {
+        const int i = base + lane;
+        bool accept = false, valid = i < ncur;
+        double bs = 0, bt = 0, bz = 0;
+        if (valid) {
+          bs = sm.box[cur][i][0];
+          bt = sm.box[cur][i][1];
+          bz = sm.box[cur][i][2];
+          double X[3], Xs[3], Xt[3], sg;
+          interp(sm.F, bs + 0.5 * bz, bt + 0.5 * bz, X, Xs, Xt, sg, false);
+          const double ls = sqrt(Xs[0] * Xs[0] + Xs[1] * Xs[1] + Xs[2] * Xs[2]);
+          const double lt = sqrt(Xt[0] * Xt[0] + Xt[1] * Xt[1] + Xt[2] * Xt[2]);
+          const double diam = bz * sqrt(ls * ls + lt * lt);
+          const double d = sqrt((xt[0] - X[0]) * (xt[0] - X[0]) + (xt[1] - X[1]) * (xt[1] - X[1]) +
+                                (xt[2] - X[2]) * (xt[2] - X[2]));
+          accept = d >= p.alpha * diam || depth == p.max_depth;
+        }
+        const unsigned acc_mask = __ballot_sync(0xffffffffu, valid && accept);
+        const unsigned ref_mask = __ballot_sync(0xffffffffu, valid && !accept);
+        const unsigned lt_mask = (1u << lane) - 1u;
+        if (valid && accept) {
+          const int slot = nleaf + __popc(acc_mask & lt_mask);
+          if (slot < PQ_QUEUE) {
+            sm.leaf[slot][0] = (float)bs;
+            sm.leaf[slot][1] = (float)bt;
+            sm.leaf[slot][2] = (float)bz;
+          }
+        }
+        if (valid && !accept) {
+          const int slot = nnext + 4 * __popc(ref_mask & lt_mask);
+          const double h = 0.5 * bz;
+          for (int c = 0; c < 4; ++c)
+            if (slot + c < PQ_QUEUE) {
+              sm.box[cur ^ 1][slot + c][0] = (float)(bs + (c & 1) * h);
+              sm.box[cur ^ 1][slot + c][1] = (float)(bt + (c >> 1) * h);
+              sm.box[cur ^ 1][slot + c][2] = (float)h;
+            }
+        }
+        nleaf = min(PQ_QUEUE, nleaf + __popc(acc_mask));
+        nnext = min(PQ_QUEUE, nnext + 4 * __popc(ref_mask));
+        if (nleaf >= PQ_QUEUE || nnext >= PQ_QUEUE) {
+          if (lane == 0 && p.status) atomicOr(p.status, 2u);  // queue overflow: result truncated
+        }
+      }
+      __syncwarp();
+      // integrate this round's leaves: 100 Gauss nodes each, spread over the lanes
+      const int total = nleaf * PQ_GL * PQ_GL;
+      for (int k = lane; k < total; k += 32) {
+        const int lf = k / (PQ_GL * PQ_GL), g = k % (PQ_GL * PQ_GL);
+        const double bs = sm.leaf[lf][0], bt = sm.leaf[lf][1], bz = sm.leaf[lf][2];
+        const int ga = g / PQ_GL, gb = g % PQ_GL;
+        const double s = bs + bz * c_gl_x[ga], t = bt + bz * c_gl_x[gb];
+        double X[3], Xs[3], Xt[3], sg;
+        interp(sm.F, s, t, X, Xs, Xt, sg, true);
+        double n[3] = {Xs[1] * Xt[2] - Xs[2] * Xt[1], Xs[2] * Xt[0] - Xs[0] * Xt[2], Xs[0] * Xt[1] - Xs[1] * Xt[0]};
+        const double J = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        const double iJ = 1.0 / J;
+        n[0] *= iJ;
+        n[1] *= iJ;
+        n[2] *= iJ;
+        const double r[3] = {xt[0] - X[0], xt[1] - X[1], xt[2] - X[2]};
+        acc += kernel_val<KER>(r, n) * sg * J * (bz * bz * c_gl_w[ga] * c_gl_w[gb]);
+      }
+      __syncwarp();
+      cur ^= 1;
+      ncur = nnext;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) atomicAdd(&p.out[oix], acc * p.scale);
+  }
+}
+
+// Gauss-Legendre nodes and weights on [0,1] (Newton iteration on P_n).
+void gauss_legendre01(int n, double* x, double* w) {
+  const double pi = 3.14159265358979323846264338327950288;
+  for (int i = 0; i < n; ++i) {
+    double z = cos(pi * (i + 0.75) / (n + 0.5)), dp = 0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1, p1 = z;
+      for (int k = 2; k <= n; ++k) {
+        const double p2 = ((2.0 * k - 1) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = n * (z * p1 - p0) / (z * z - 1);
+      const double dz = p1 / dp;
+      z -= dz;
+      if (fabs(dz) < 1e-16) break;
+    }
+    x[n - 1 - i] = 0.5 * (1 + z);
+    w[n - 1 - i] = 1.0 / ((1 - z * z) * dp * dp);  // 2/((1-z^2) P'^2) on [-1,1], halved for [0,1]
+  }
+}
+
+}  // namespace
+}  // namespace sctlgpu
+
+using namespace sctlgpu;
+
+extern "C" int sctlgpu_panel_near_correction(int kernel, int64_t n_pairs, const int64_t* pair_trg,
+                                             const int64_t* pair_panel, int64_t nt, const double* r_trg,
+                                             int64_t n_panels, const double* X, const double* N, const double* Q,
+                                             const double* sigma, const int64_t* trg_map, int64_t n_out, double alpha,
+                                             int max_depth, double* v_out, void* stream) {
+  if (kernel != SCTLGPU_LAPLACE3D_FXU && kernel != SCTLGPU_LAPLACE3D_DXU) return SCTLGPU_ERR_INVALID_KERNEL;
+  if (n_pairs < 0 || max_depth < 0 || nt < 0 || n_panels < 0 || (trg_map && n_out < 0)) return SCTLGPU_ERR_INVALID_SIZE;
+  if (!(alpha > 0)) return SCTLGPU_ERR_INVALID_ARGUMENT;
+  if (n_pairs == 0) return SCTLGPU_OK;
+  if (!pair_trg || !pair_panel || !r_trg || !X || !N || !Q || !sigma || !v_out) return SCTLGPU_ERR_NULL_POINTER;
+  int dev;
+  unsigned* status;
+  int sms;
+  int rc = runtime_device(&dev, &status, &sms);
+  if (rc) return rc;
+  static bool have_gl[64] = {};
+  if (!have_gl[dev]) {
+    double gx[PQ_GL], gw[PQ_GL];
+    gauss_legendre01(PQ_GL, gx, gw);
+    cudaError_t e = cudaMemcpyToSymbol(c_gl_x, gx, sizeof(gx));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gl_w, gw, sizeof(gw));
+    if (e != cudaSuccess) return runtime_record(e);
+    have_gl[dev] = true;
+  }
+  PanelParams p;
+  p.n_pairs = n_pairs;
+  p.n_panels = n_panels;
+  p.nt = nt;
+  p.n_out = trg_map ? n_out : nt;
+  p.pair_trg = pair_trg;
+  p.pair_panel = pair_panel;
+  p.trg_map = trg_map;
+  p.r_trg = r_trg;
+  p.X = X;
+  p.N = N;
+  p.Q = Q;
+  p.sigma = sigma;
+  p.alpha = alpha;
+  p.max_depth = max_depth < PQ_MAX_DEPTH ? max_depth : PQ_MAX_DEPTH;
+  p.scale = sctlgpu_scale_factor(kernel);
+  p.out = v_out;
+  p.status = status;
+  const int64_t ctas = (n_pairs + PQ_WARPS - 1) / PQ_WARPS;
+  const unsigned grid = (unsigned)(ctas < (int64_t)sms * 16 ? ctas : (int64_t)sms * 16);
+  if (kernel == SCTLGPU_LAPLACE3D_FXU)
+    panel_near_kernel<0><<<grid, 32 * PQ_WARPS, 0, (cudaStream_t)stream>>>(p);
+  else
+    panel_near_kernel<1><<<grid, 32 * PQ_WARPS, 0, (cudaStream_t)stream>>>(p);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  return runtime_record(cudaGetLastError());
+}

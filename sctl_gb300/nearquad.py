@@ -1,0 +1,88 @@
+"""Boundary-integral evaluation on a panel surface: smooth far field plus
+near-singular panel corrections -- BoundaryIntegralOp::ComputePotential
+(boundary_integral.txx:716-722) with its two halves,
+
+* far field: every node is a source with weight Q (ComputeFarField,
+  :1248-1309: F_far = F * wts, then the direct sum), evaluated by
+  `sctlgpu_eval`;
+* near field: for every (target, panel) pair closer than `near_factor` panel
+  sizes, the panel's accurate contribution minus its smooth-rule part
+  (SetupNear / ComputeNearInterac, :927-1381), evaluated by
+  `sctlgpu_panel_near_correction` (adaptive refinement, FP64) or by
+  upsampled sub-panel sources through a batched near plan.
+
+All arrays are torch tensors on the GPU; the work runs in libsctlgpu.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import capi
+
+
+class PanelSurface:
+    def __init__(self, X, N, Q, size, device="cuda"):
+        """X, N: (np, p*p, 3) node coordinates and unit normals; Q: (np, p*p) smooth weights;
+        size: (np,) panel sizes (near-field radius unit)."""
+        t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=device)  # noqa: E731
+        self.X, self.N, self.Q, self.size = t(X), t(N), t(Q), t(size)
+        self.np, self.nn = self.X.shape[0], self.X.shape[1]
+        self.center = self.X.mean(1)
+        self.radius = (self.X - self.center[:, None]).norm(dim=2).max(1).values
+
+    # ------------------------------------------------------------ near list
+    def near_pairs(self, r_trg, near_factor=1.0, chunk=1 << 15):
+        """(target, panel) pairs with |x_t - c_P| < radius_P + near_factor * size_P (a brute-force
+        GPU form of BuildNearList, boundary_integral.txx:50-522).  Sorted by panel."""
+        xt = r_trg.reshape(-1, 3)
+        lim = self.radius + near_factor * self.size
+        tt, pp = [], []
+        for a in range(0, xt.shape[0], chunk):
+            d = torch.cdist(xt[a:a + chunk], self.center)
+            i, j = torch.nonzero(d < lim[None], as_tuple=True)
+            tt.append(i + a)
+            pp.append(j)
+        t = torch.cat(tt).to(torch.int64)
+        p = torch.cat(pp).to(torch.int64)
+        order = torch.argsort(p * xt.shape[0] + t)
+        return t[order].contiguous(), p[order].contiguous()
+
+    # ------------------------------------------------------------ far field
+    def far_field(self, r_trg, sigma, kernel=1, mode="mixed", digits=10, out=None):
+        xt = r_trg.reshape(-1)
+        nt = xt.numel() // 3
+        src = self.X.reshape(-1)
+        nrm = self.N.reshape(-1)
+        f = (sigma.reshape(-1) * self.Q.reshape(-1)).contiguous()
+        if out is None:
+            out = torch.zeros(nt, dtype=torch.float64, device=xt.device)
+        flags = capi.DEVICE_PTRS | (capi.ACCUMULATE if out is not None else 0)
+        stream = torch.cuda.current_stream().cuda_stream
+        capi.check(capi.load().sctlgpu_eval(kernel, capi.MODE_IDS[mode], digits, nt, xt.data_ptr(), src.numel() // 3,
+                                            src.data_ptr(), nrm.data_ptr() if kernel in (1, 3) else None,
+                                            f.data_ptr(), out.data_ptr(), flags, stream), "far field")
+        return out
+
+    # ------------------------------------------------------------ near field
+    def near_correction(self, r_trg, sigma, pairs, kernel=1, alpha=1.5, max_depth=22, out=None):
+        """Adaptive near-singular correction for every (target, panel) pair."""
+        xt = r_trg.reshape(-1).contiguous()
+        nt = xt.numel() // 3
+        t, p = pairs
+        sig = sigma.reshape(self.np, self.nn).contiguous()
+        if out is None:
+            out = torch.zeros(nt, dtype=torch.float64, device=xt.device)
+        stream = torch.cuda.current_stream().cuda_stream
+        capi.check(capi.load().sctlgpu_panel_near_correction(
+            kernel, t.numel(), t.data_ptr(), p.data_ptr(), nt, xt.data_ptr(), self.np, self.X.data_ptr(),
+            self.N.data_ptr(), self.Q.data_ptr(), sig.data_ptr(), None, -1, float(alpha), int(max_depth),
+            out.data_ptr(), stream), "near correction")
+        return out
+
+    def evaluate(self, r_trg, sigma, kernel=1, mode="mixed", digits=10, near_factor=1.0, alpha=1.5, pairs=None):
+        out = self.far_field(r_trg, sigma, kernel, mode, digits)
+        if pairs is None:
+            pairs = self.near_pairs(r_trg, near_factor)
+        self.near_correction(r_trg, sigma, pairs, kernel, alpha, out=out)
+        return out

@@ -1,0 +1,131 @@
+"""Torus test surface for the near-singular double-layer quadrature.
+
+Torus (R = 1, r = 0.3) split into 64 x 32 panels in (theta, phi); each panel
+carries 10 x 10 nodes on the reference's Chebyshev rule (ChebQuadRule,
+quadrule.txx:71-101: nodes (1 - cos((2i+1) pi / 2N)) / 2 on [0, 1], weights
+from the integrals of the Chebyshev polynomials) -- 204,800 nodes in FP64.
+The Laplace double-layer density is a sum of 8 random low-order Fourier
+modes a cos(m theta + n phi + psi), |m|, |n| <= 3.  Targets sit at off-surface
+distances log-uniform in [1e-4, 1] panel sizes on either side of a random
+panel point.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+R_MAJOR, R_MINOR = 1.0, 0.3
+
+
+def cheb_rule(n: int):
+    """ChebQuadRule<Real>::ComputeNdsWts: nodes and weights on [0, 1]."""
+    i = np.arange(n)
+    nds = (1.0 - np.cos((2 * i + 1) * np.pi / (2 * n))) / 2.0
+    theta = (2 * i + 1) * np.pi / (2 * n)
+    Minv = np.cos(np.outer(theta, np.arange(n))) / n
+    Minv[:, 1:] *= 2.0
+    b = np.array([0.0 if k % 2 else -1.0 / (k * k - 1.0) for k in range(n)])
+    return nds, Minv @ b
+
+
+def cheb_bary_weights(n: int):
+    """Barycentric weights of the first-kind Chebyshev points (up to a common factor)."""
+    i = np.arange(n)
+    return (-1.0) ** i * np.sin((2 * i + 1) * np.pi / (2 * n))
+
+
+def lagrange_matrix(x_nodes, bw, x):
+    """L[k, a] = l_a(x_k): barycentric Lagrange basis at points x (exact at nodes)."""
+    x = np.asarray(x, np.float64)
+    d = x[:, None] - x_nodes[None, :]
+    hit = np.isclose(d, 0.0, atol=0.0, rtol=0.0)
+    d = np.where(hit, 1.0, d)
+    t = bw[None, :] / d
+    L = t / t.sum(1, keepdims=True)
+    rows = hit.any(1)
+    L[rows] = hit[rows].astype(np.float64)
+    return L
+
+
+def surface(theta, phi):
+    c, s = np.cos(phi), np.sin(phi)
+    rho = R_MAJOR + R_MINOR * c
+    X = np.stack([rho * np.cos(theta), rho * np.sin(theta), R_MINOR * s], -1)
+    n = np.stack([c * np.cos(theta), c * np.sin(theta), s], -1)  # outward unit normal
+    jac = R_MINOR * rho  # |X_theta x X_phi|
+    return X, n, jac
+
+
+class Torus:
+    """Panels, nodes, normals, smooth-quadrature weights and density."""
+
+    def __init__(self, n_theta=64, n_phi=32, order=10, seed=0):
+        self.n_theta, self.n_phi, self.p = n_theta, n_phi, order
+        self.np = n_theta * n_phi
+        self.dth, self.dph = 2 * np.pi / n_theta, 2 * np.pi / n_phi
+        x, w = cheb_rule(order)
+        self.x1d, self.w1d = x, w
+        self.bw = cheb_bary_weights(order)
+        # panel p = i * n_phi + j ; node q = a * order + b  (a along theta, b along phi)
+        i, j = np.divmod(np.arange(self.np), n_phi)
+        th = (i[:, None, None] + x[None, :, None]) * self.dth + 0 * x[None, None, :]
+        ph = (j[:, None, None] + x[None, None, :]) * self.dph + 0 * x[None, :, None]
+        X, n, jac = surface(th, ph)
+        self.X = X.reshape(self.np, order * order, 3)
+        self.N = n.reshape(self.np, order * order, 3)
+        self.Q = (np.outer(w, w)[None] * jac * self.dth * self.dph).reshape(self.np, order * order)
+        self.theta0, self.phi0 = i * self.dth, j * self.dph
+        self.area = self.Q.sum(1)
+        self.size = np.sqrt(self.area)  # panel size used for target distances
+        rng = np.random.default_rng(seed)
+        self.modes = [(int(rng.integers(-3, 4)), int(rng.integers(-3, 4)), float(rng.standard_normal()),
+                       float(rng.uniform(0, 2 * np.pi))) for _ in range(8)]
+        self.sigma = self.density(th, ph).reshape(self.np, order * order)
+
+    def density(self, theta, phi):
+        s = np.zeros(np.broadcast(theta, phi).shape)
+        for m, n, a, psi in self.modes:
+            s = s + a * np.cos(m * theta + n * phi + psi)
+        return s
+
+    def nodes(self):
+        """Flat arrays of all nodes: coordinates, normals, weights, density."""
+        return (self.X.reshape(-1, 3), self.N.reshape(-1, 3), self.Q.reshape(-1), self.sigma.reshape(-1))
+
+    def targets(self, n: int, seed=1, hmin=1e-4, hmax=1.0, panels=None):
+        """n targets: random panel, random (s, t), distance h = size * 10^U(log10 hmin, log10 hmax),
+        random side.  Returns coordinates, owning panel, (s, t), h / size."""
+        rng = np.random.default_rng(seed)
+        p = rng.integers(0, self.np, n) if panels is None else np.asarray(panels)
+        st = rng.uniform(0, 1, (n, 2))
+        i, j = np.divmod(p, self.n_phi)
+        X, nrm, _ = surface((i + st[:, 0]) * self.dth, (j + st[:, 1]) * self.dph)
+        hr = 10.0 ** rng.uniform(np.log10(hmin), np.log10(hmax), n)
+        side = np.where(rng.uniform(size=n) < 0.5, -1.0, 1.0)
+        xt = X + (side * hr * self.size[p])[:, None] * nrm
+        return dict(r_trg=xt, panel=p, st=st, h=hr, side=side)
+
+    def near_pairs(self, xt, factor=1.0):
+        """(target, panel) pairs with the target within factor * panel size of the panel's
+        node set (the smooth rule is not trusted there).  Returns int64 arrays."""
+        cen = self.X.mean(1)
+        rad = np.linalg.norm(self.X - cen[:, None, :], axis=2).max(1)
+        pairs_t, pairs_p = [], []
+        chunk = 4096
+        for a in range(0, xt.shape[0], chunk):
+            d = np.linalg.norm(xt[a:a + chunk, None, :] - cen[None], axis=2)
+            tt, pp = np.nonzero(d < rad[None] + factor * self.size[None])
+            pairs_t.append(tt + a)
+            pairs_p.append(pp)
+        return np.concatenate(pairs_t).astype(np.int64), np.concatenate(pairs_p).astype(np.int64)
+
+    def upsample_matrix(self, k: int):
+        """Interpolation matrix (k*k*p*p, p*p) from a panel's nodes to k x k sub-panels with
+        p x p Chebyshev nodes each, the sub-panel weights (fraction of the panel rule), and the
+        local coordinates (s, t) of the new nodes."""
+        p = self.p
+        sub = (np.arange(k)[:, None] + self.x1d[None, :]).reshape(-1) / k  # k*p points in [0,1]
+        L = lagrange_matrix(self.x1d, self.bw, sub)                        # (k*p, p)
+        Lu = np.einsum("ia,jb->ijab", L, L).reshape(k * p * k * p, p * p)
+        w = np.outer(np.tile(self.w1d, k) / k, np.tile(self.w1d, k) / k).reshape(-1)
+        s, t = np.meshgrid(sub, sub, indexing="ij")
+        return Lu, w, np.stack([s.reshape(-1), t.reshape(-1)], 1)
