@@ -133,6 +133,19 @@ int sctlgpu_near_plan_create(sctlgpu_near_plan* plan, int kernel, int mode, int 
                              int64_t nblk, const sctlgpu_block* blocks, /* host array */
                              int64_t ns, int64_t nt,
                              const int64_t* trg_map, int64_t n_out); /* host array or NULL */
+/*
+ * Same, with a target index list (the reference's near lists): block target
+ * ranges select entries of trg_index (n_index entries, each a target in
+ * [0, nt)), and results are added into v_out[trg_map ? trg_map[k] : trg_index[k]]
+ * for list entry k.  Because the coordinate arrays are the full target and
+ * source sets, a mixed-precision plan uses the same frame as a sctlgpu_eval of
+ * those arrays, so a smooth-rule subtraction cancels the far field's terms
+ * consistently (the KNearSubtract convention, boundary_integral.txx:1165-1240).
+ */
+int sctlgpu_near_plan_create_indexed(sctlgpu_near_plan* plan, int kernel, int mode, int digits,
+                                     int64_t nblk, const sctlgpu_block* blocks, int64_t ns, int64_t nt,
+                                     const int64_t* trg_index, int64_t n_index,
+                                     const int64_t* trg_map, int64_t n_out);
 int sctlgpu_near_plan_execute(sctlgpu_near_plan plan, const void* r_trg, const void* r_src, const void* n_src,
                               const void* v_src, const void* w_src, void* v_out, unsigned flags, void* stream);
 /* Work items, interactions per execution, and CUDA-graph kernel nodes of a plan. */
@@ -150,7 +163,9 @@ int sctlgpu_near_plan_destroy(sctlgpu_near_plan plan);
  * integrated with adaptive dyadic refinement (boxes accepted at distance >=
  * alpha x diameter, 10 x 10 Gauss-Legendre per box, at most max_depth levels),
  * the panel's smooth-rule part (nodes X, normals N, weights Q) is subtracted
- * (KNearSubtract, boundary_integral.txx:1165-1240), and scale x the result is
+ * when subtract_smooth != 0 (KNearSubtract, boundary_integral.txx:1165-1240; pass
+ * 0 and subtract with a near plan in the far field's arithmetic when the far field
+ * is mixed precision), and scale x the result is
  * atomically added to v_out[trg_map ? trg_map[t] : t].  Kernels: Laplace3D_FxU,
  * Laplace3D_DxU (double arrays, FP64 arithmetic); device pointers, asynchronous on
  * `stream`.  Out-of-range pair indices are skipped and flagged in the device status.
@@ -159,7 +174,7 @@ int sctlgpu_panel_near_correction(int kernel, int64_t n_pairs, const int64_t* pa
                                   int64_t nt, const double* r_trg, int64_t n_panels, const double* X,
                                   const double* N, const double* Q, const double* sigma,
                                   const int64_t* trg_map, int64_t n_out, double alpha, int max_depth,
-                                  double* v_out, void* stream);
+                                  int subtract_smooth, double* v_out, void* stream);
 
 /*
  * Runs (or returns the cached result of) the tile autotuner for the batched

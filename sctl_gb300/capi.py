@@ -41,13 +41,15 @@ SIGNATURES = {
     "sctlgpu_newton_steps": (_i, [_i, _i]),
     "sctlgpu_eval_mixed_noalloc": (_i, [_i, _i, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _u, _vp]),
     "sctlgpu_near_plan_create": (_i, [ctypes.POINTER(_vp), _i, _i, _i, _i64, _vp, _i64, _i64, _vp, _i64]),
+    "sctlgpu_near_plan_create_indexed": (_i, [ctypes.POINTER(_vp), _i, _i, _i, _i64, _vp, _i64, _i64, _vp, _i64,
+                                              _vp, _i64]),
     "sctlgpu_near_plan_execute": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _u, _vp]),
     "sctlgpu_near_plan_info": (_i, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64), _ip]),
     "sctlgpu_near_plan_status": (_i, [_vp, _vp]),
     "sctlgpu_near_plan_destroy": (_i, [_vp]),
     "sctlgpu_near_autotune": (_i, [_i, _i, _i, _ip]),
     "sctlgpu_panel_near_correction": (_i, [_i, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _d,
-                                           _i, _vp, _vp]),
+                                           _i, _i, _vp, _vp]),
 }
 NEAR_CLASSES = 10
 NOALLOC_SCRATCH_BYTES = 64 << 20

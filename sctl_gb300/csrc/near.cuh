@@ -7,7 +7,9 @@
 // which applies the blocks and scatters into per-target sums): each block b
 // adds  scale * sum_{s in block b} K(x_t - y_s, n_s) * w_s * f_s  to each of its
 // targets t, either in place (v_out[t]) or scattered through a target map
-// (atomic FP64 adds: several blocks may feed one physical target).
+// (atomic FP64 adds: several blocks may feed one physical target).  With a
+// target index list, a block's targets are entries of that list (the
+// reference's near lists) and results scatter to the listed targets.
 //
 // Work decomposition.  The host splits every block into items (block, first
 // target, target count, source split) and sorts them by cost, largest first.
@@ -40,7 +42,8 @@ struct NearParams {
   const NearItem* items;
   int64_t n_items;
   const NearBlock* blocks;
-  const void* r_trg;      // AoS targets (Real), concatenated over blocks
+  const void* r_trg;      // AoS targets (Real), concatenated over blocks, or indexed through tidx
+  const int64_t* tidx;    // optional: block target positions -> target indices (near lists)
   const void* recs;       // packed source records, concatenated over blocks
   const int64_t* map;     // optional: output index of every target
   double* out;            // results (double); Real out when !map handled by `out_f`
@@ -102,7 +105,8 @@ __global__ void __launch_bounds__(NEAR_THREADS) near_batch_kernel(NearParams p) 
 #pragma unroll
     for (int j = 0; j < T; ++j) {
       const int lt = lane + j * gsize;
-      P::load_trg(tg[j], rt, tbase + (lt < item.nt ? lt : 0), fr);
+      const int64_t k = tbase + (lt < item.nt ? lt : 0);
+      P::load_trg(tg[j], rt, p.tidx ? p.tidx[k] : k, fr);
     }
 
     const RecT* src = recs + blk.s0;
@@ -170,8 +174,8 @@ __global__ void __launch_bounds__(NEAR_THREADS) near_batch_kernel(NearParams p) 
 #pragma unroll
         for (int c = 0; c < K1; ++c) {
           const double v = P::result(tg[j], c) * scale;
-          if (p.map) {
-            atomicAdd(&p.out[p.map[t] * K1 + c], v);
+          if (p.map || p.tidx) {
+            atomicAdd(&p.out[(p.map ? p.map[t] : p.tidx[t]) * K1 + c], v);
           } else if (MODE == MODE_F32) {
             float* o = &p.out_f[t * K1 + c];
             *o = p.accumulate ? (float)((double)*o + v) : (float)v;

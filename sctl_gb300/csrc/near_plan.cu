@@ -25,6 +25,8 @@ struct sctlgpu_near_plan_s {
   NearItem* d_items = nullptr;
   NearBlock* d_blocks = nullptr;
   int64_t* d_map = nullptr;
+  int64_t* d_tidx = nullptr;
+  int64_t n_index = 0;
   char* d_scratch = nullptr;
   void* d_recs = nullptr;
   BBox* d_bbox = nullptr;
@@ -247,7 +249,7 @@ cudaError_t enqueue(sctlgpu_near_plan_s* P, const void* const* k, unsigned flags
   e = P->ops.pack(s, P->ns, r_src, P->ND ? n_src : nullptr, v_src, w_src, P->d_recs, P->d_bbox, P->sms);
   if (e != cudaSuccess) return e;
   const bool accumulate = flags & SCTLGPU_ACCUMULATE;
-  if (P->has_map && !accumulate) {
+  if ((P->has_map || P->d_tidx) && !accumulate) {
     e = cudaMemsetAsync(v_out, 0, (size_t)P->n_out * P->K1 * sizeof(double), s);
     if (e != cudaSuccess) return e;
   }
@@ -258,6 +260,7 @@ cudaError_t enqueue(sctlgpu_near_plan_s* P, const void* const* k, unsigned flags
   p.r_trg = r_trg;
   p.recs = P->d_recs;
   p.map = P->d_map;
+  p.tidx = P->d_tidx;
   p.out = (double*)v_out;
   p.out_f = (float*)v_out;
   p.counter = P->d_counter;
@@ -275,6 +278,7 @@ void free_plan(sctlgpu_near_plan_s* P) {
   cudaFree(P->d_items);
   cudaFree(P->d_blocks);
   cudaFree(P->d_map);
+  cudaFree(P->d_tidx);
   cudaFree(P->d_scratch);
   delete P;
 }
@@ -306,6 +310,12 @@ int sctlgpu_near_autotune(int kernel, int mode, int digits, int* splits) {
 int sctlgpu_near_plan_create(sctlgpu_near_plan* out, int kernel, int mode, int digits, int64_t nblk,
                              const sctlgpu_block* blocks, int64_t ns, int64_t nt, const int64_t* trg_map,
                              int64_t n_out) {
+  return sctlgpu_near_plan_create_indexed(out, kernel, mode, digits, nblk, blocks, ns, nt, nullptr, 0, trg_map, n_out);
+}
+
+int sctlgpu_near_plan_create_indexed(sctlgpu_near_plan* out, int kernel, int mode, int digits, int64_t nblk,
+                                     const sctlgpu_block* blocks, int64_t ns, int64_t nt, const int64_t* trg_index,
+                                     int64_t n_index, const int64_t* trg_map, int64_t n_out) {
   if (!out) return SCTLGPU_ERR_NULL_POINTER;
   *out = nullptr;
   int nd, sd, td;
@@ -313,22 +323,27 @@ int sctlgpu_near_plan_create(sctlgpu_near_plan* out, int kernel, int mode, int d
   if (mode != SCTLGPU_F64 && mode != SCTLGPU_F32 && mode != SCTLGPU_MIXED) return SCTLGPU_ERR_INVALID_MODE;
   if (nblk < 0 || ns < 0 || nt < 0 || nblk > INT32_MAX) return SCTLGPU_ERR_INVALID_SIZE;
   if (nblk > 0 && !blocks) return SCTLGPU_ERR_NULL_POINTER;
-  if (trg_map && mode == SCTLGPU_F32) return SCTLGPU_ERR_INVALID_ARGUMENT;  // scattered outputs are FP64
+  if ((trg_map || trg_index) && mode == SCTLGPU_F32) return SCTLGPU_ERR_INVALID_ARGUMENT;  // scattered outputs are FP64
+  if (trg_index && n_index < 0) return SCTLGPU_ERR_INVALID_SIZE;
+  const int64_t nlist = trg_index ? n_index : nt;  // block target ranges index this list
   int64_t pairs = 0;
   std::vector<NearBlock> hb((size_t)nblk);
   for (int64_t b = 0; b < nblk; ++b) {
     const sctlgpu_block& B = blocks[b];
     if (B.src_count < 0 || B.trg_count < 0 || B.src_begin < 0 || B.trg_begin < 0 || B.src_begin + B.src_count > ns ||
-        B.trg_begin + B.trg_count > nt || B.trg_count > INT32_MAX)
+        B.trg_begin + B.trg_count > nlist || B.trg_count > INT32_MAX)
       return SCTLGPU_ERR_INVALID_SIZE;
     hb[b] = {B.src_begin, B.src_count, B.trg_begin, B.trg_count};
     pairs += B.src_count * B.trg_count;
   }
   if (trg_map) {
     if (n_out < 0) return SCTLGPU_ERR_INVALID_SIZE;
-    for (int64_t t = 0; t < nt; ++t)
+    for (int64_t t = 0; t < nlist; ++t)
       if (trg_map[t] < 0 || trg_map[t] >= n_out) return SCTLGPU_ERR_INVALID_ARGUMENT;
   }
+  if (trg_index)
+    for (int64_t k = 0; k < n_index; ++k)
+      if (trg_index[k] < 0 || trg_index[k] >= nt) return SCTLGPU_ERR_INVALID_ARGUMENT;
   int dev;
   unsigned* status;
   int sms;
@@ -347,7 +362,7 @@ int sctlgpu_near_plan_create(sctlgpu_near_plan* out, int kernel, int mode, int d
   P->nblk = nblk;
   P->ns = ns;
   P->nt = nt;
-  P->n_out = trg_map ? n_out : nt;
+  P->n_out = trg_map ? n_out : nt;  // outputs: mapped, or one per target (direct or through the index list)
   P->has_map = trg_map != nullptr;
   P->device = dev;
   P->sms = sms;
@@ -381,8 +396,13 @@ int sctlgpu_near_plan_create(sctlgpu_near_plan* out, int kernel, int mode, int d
       break;
     if ((e = cudaMemset(P->d_status, 0, sizeof(unsigned)))) break;
     if (trg_map) {
-      if ((e = cudaMalloc(&P->d_map, std::max<int64_t>(1, nt) * sizeof(int64_t)))) break;
-      if (nt && (e = cudaMemcpy(P->d_map, trg_map, nt * sizeof(int64_t), cudaMemcpyHostToDevice))) break;
+      if ((e = cudaMalloc(&P->d_map, std::max<int64_t>(1, nlist) * sizeof(int64_t)))) break;
+      if (nlist && (e = cudaMemcpy(P->d_map, trg_map, nlist * sizeof(int64_t), cudaMemcpyHostToDevice))) break;
+    }
+    if (trg_index) {
+      if ((e = cudaMalloc(&P->d_tidx, std::max<int64_t>(1, n_index) * sizeof(int64_t)))) break;
+      if (n_index && (e = cudaMemcpy(P->d_tidx, trg_index, n_index * sizeof(int64_t), cudaMemcpyHostToDevice))) break;
+      P->n_index = n_index;
     }
   } while (0);
   if (e != cudaSuccess) {

@@ -30,11 +30,14 @@ constexpr int PQ_P = 10;          // panel order
 constexpr int PQ_NODES = PQ_P * PQ_P;
 constexpr int PQ_GL = 10;         // Gauss-Legendre points per box side
 constexpr int PQ_WARPS = 4;       // warps per CTA
-constexpr int PQ_QUEUE = 128;     // boxes per round (per warp)
+constexpr int PQ_QUEUE = 256;     // boxes per round (per warp)
 constexpr int PQ_MAX_DEPTH = 22;  // box corners k * 2^-depth stay exact in FP32
 
+// Per-warp shared state (dynamic shared memory).
 struct PanelWarpSmem {
-  double F[4][PQ_NODES];          // x, y, z, sigma at the panel nodes
+  double F[4][PQ_NODES];          // x, y, z, sigma at the panel nodes (a-major: F[c][a*P+b])
+  double Ls[PQ_GL][PQ_P], Lds[PQ_GL][PQ_P], Lt[PQ_GL][PQ_P], Ldt[PQ_GL][PQ_P];  // basis at a box's Gauss points
+  double A[7][PQ_GL][PQ_P];       // L_s F (x,y,z,sigma) and L_s' F (x,y,z)
   float box[2][PQ_QUEUE][3];      // (s0, t0, size) of the boxes of this and the next round (dyadic: exact)
   float leaf[PQ_QUEUE][3];
 };
@@ -143,6 +146,7 @@ struct PanelParams {
   const double* sigma;      // [np][100]    density
   double alpha;
   int max_depth;
+  int subtract_smooth;
   double scale;
   double* out;
   unsigned* status;
@@ -150,9 +154,9 @@ struct PanelParams {
 
 template <int KER>
 __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel(PanelParams p) {
-  __shared__ PanelWarpSmem sm_all[PQ_WARPS];
+  extern __shared__ __align__(16) unsigned char pq_smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  PanelWarpSmem& sm = sm_all[warp];
+  PanelWarpSmem& sm = reinterpret_cast<PanelWarpSmem*>(pq_smem)[warp];
   for (int64_t pr = (int64_t)blockIdx.x * PQ_WARPS + warp; pr < p.n_pairs; pr += (int64_t)gridDim.x * PQ_WARPS) {
     const int64_t tix = p.pair_trg[pr], pix = p.pair_panel[pr];
     const int64_t oix = p.trg_map ? (tix >= 0 && tix < p.nt ? p.trg_map[tix] : -1) : tix;
@@ -170,8 +174,9 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel(PanelParams p
     }
     __syncwarp();
     double acc = 0.0;
-    // Smooth-rule part of this panel, to be subtracted.
-    for (int q = lane; q < PQ_NODES; q += 32) {
+    // Smooth-rule part of this panel, to be subtracted (unless the caller
+    // subtracts it in the arithmetic of its far field).
+    for (int q = lane; q < PQ_NODES && p.subtract_smooth; q += 32) {
       const double r[3] = {xt[0] - sm.F[0][q], xt[1] - sm.F[1][q], xt[2] - sm.F[2][q]};
       const double n[3] = {p.N[(pix * PQ_NODES + q) * 3], p.N[(pix * PQ_NODES + q) * 3 + 1],
                            p.N[(pix * PQ_NODES + q) * 3 + 2]};
@@ -234,25 +239,63 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel(PanelParams p
         }
       }
       __syncwarp();
-      // integrate this round's leaves: 100 Gauss nodes each, spread over the lanes
-      const int total = nleaf * PQ_GL * PQ_GL;
-      for (int k = lane; k < total; k += 32) {
-        const int lf = k / (PQ_GL * PQ_GL), g = k % (PQ_GL * PQ_GL);
+      // Integrate this round's leaves.  Per box, tensor-product interpolation:
+      // basis matrices at the box's Gauss points (lanes 0-19), then A = L_s F and
+      // L_s' F (stage 1), then every node from two 10-term dot products per field.
+      for (int lf = 0; lf < nleaf; ++lf) {
         const double bs = sm.leaf[lf][0], bt = sm.leaf[lf][1], bz = sm.leaf[lf][2];
-        const int ga = g / PQ_GL, gb = g % PQ_GL;
-        const double s = bs + bz * c_gl_x[ga], t = bt + bz * c_gl_x[gb];
-        double X[3], Xs[3], Xt[3], sg;
-        interp(sm.F, s, t, X, Xs, Xt, sg, true);
-        double n[3] = {Xs[1] * Xt[2] - Xs[2] * Xt[1], Xs[2] * Xt[0] - Xs[0] * Xt[2], Xs[0] * Xt[1] - Xs[1] * Xt[0]};
-        const double J = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-        const double iJ = 1.0 / J;
-        n[0] *= iJ;
-        n[1] *= iJ;
-        n[2] *= iJ;
-        const double r[3] = {xt[0] - X[0], xt[1] - X[1], xt[2] - X[2]};
-        acc += kernel_val<KER>(r, n) * sg * J * (bz * bz * c_gl_w[ga] * c_gl_w[gb]);
+        if (lane < 2 * PQ_GL) {
+          const int i = lane % PQ_GL;
+          Basis Bq;
+          basis((lane < PQ_GL ? bs : bt) + bz * c_gl_x[i], Bq);
+#pragma unroll
+          for (int a = 0; a < PQ_P; ++a) {
+            if (lane < PQ_GL) {
+              sm.Ls[i][a] = Bq.l[a];
+              sm.Lds[i][a] = Bq.d[a];
+            } else {
+              sm.Lt[i][a] = Bq.l[a];
+              sm.Ldt[i][a] = Bq.d[a];
+            }
+          }
+        }
+        __syncwarp();
+        for (int e = lane; e < 7 * PQ_GL * PQ_P; e += 32) {
+          const int m = e / (PQ_GL * PQ_P), i = (e / PQ_P) % PQ_GL, b = e % PQ_P;
+          const int c = m < 4 ? m : m - 4;  // m = 0..3: L_s F_c ; m = 4..6: L_s' F_c
+          const double* L = m < 4 ? sm.Ls[i] : sm.Lds[i];
+          double v = 0.0;
+#pragma unroll
+          for (int a = 0; a < PQ_P; ++a) v = fma(L[a], sm.F[c][a * PQ_P + b], v);
+          sm.A[m][i][b] = v;
+        }
+        __syncwarp();
+        for (int g = lane; g < PQ_GL * PQ_GL; g += 32) {
+          const int i = g / PQ_GL, j = g % PQ_GL;
+          double X[3] = {0, 0, 0}, Xs[3] = {0, 0, 0}, Xt[3] = {0, 0, 0}, sg = 0;
+#pragma unroll
+          for (int b = 0; b < PQ_P; ++b) {
+            const double lt = sm.Lt[j][b], ldt = sm.Ldt[j][b];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              X[c] = fma(sm.A[c][i][b], lt, X[c]);
+              Xt[c] = fma(sm.A[c][i][b], ldt, Xt[c]);
+              Xs[c] = fma(sm.A[4 + c][i][b], lt, Xs[c]);
+            }
+            sg = fma(sm.A[3][i][b], lt, sg);
+          }
+          double n[3] = {Xs[1] * Xt[2] - Xs[2] * Xt[1], Xs[2] * Xt[0] - Xs[0] * Xt[2],
+                         Xs[0] * Xt[1] - Xs[1] * Xt[0]};
+          const double J = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+          const double iJ = 1.0 / J;
+          n[0] *= iJ;
+          n[1] *= iJ;
+          n[2] *= iJ;
+          const double r[3] = {xt[0] - X[0], xt[1] - X[1], xt[2] - X[2]};
+          acc += kernel_val<KER>(r, n) * sg * J * (bz * bz * c_gl_w[i] * c_gl_w[j]);
+        }
+        __syncwarp();
       }
-      __syncwarp();
       cur ^= 1;
       ncur = nnext;
     }
@@ -293,7 +336,7 @@ extern "C" int sctlgpu_panel_near_correction(int kernel, int64_t n_pairs, const 
                                              const int64_t* pair_panel, int64_t nt, const double* r_trg,
                                              int64_t n_panels, const double* X, const double* N, const double* Q,
                                              const double* sigma, const int64_t* trg_map, int64_t n_out, double alpha,
-                                             int max_depth, double* v_out, void* stream) {
+                                             int max_depth, int subtract_smooth, double* v_out, void* stream) {
   if (kernel != SCTLGPU_LAPLACE3D_FXU && kernel != SCTLGPU_LAPLACE3D_DXU) return SCTLGPU_ERR_INVALID_KERNEL;
   if (n_pairs < 0 || max_depth < 0 || nt < 0 || n_panels < 0 || (trg_map && n_out < 0)) return SCTLGPU_ERR_INVALID_SIZE;
   if (!(alpha > 0)) return SCTLGPU_ERR_INVALID_ARGUMENT;
@@ -328,15 +371,23 @@ extern "C" int sctlgpu_panel_near_correction(int kernel, int64_t n_pairs, const 
   p.sigma = sigma;
   p.alpha = alpha;
   p.max_depth = max_depth < PQ_MAX_DEPTH ? max_depth : PQ_MAX_DEPTH;
+  p.subtract_smooth = subtract_smooth ? 1 : 0;
   p.scale = sctlgpu_scale_factor(kernel);
   p.out = v_out;
   p.status = status;
   const int64_t ctas = (n_pairs + PQ_WARPS - 1) / PQ_WARPS;
   const unsigned grid = (unsigned)(ctas < (int64_t)sms * 16 ? ctas : (int64_t)sms * 16);
+  const size_t smem = PQ_WARPS * sizeof(PanelWarpSmem);
+  static bool attr[64] = {};
+  if (!attr[dev]) {
+    cudaFuncSetAttribute(panel_near_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(panel_near_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr[dev] = true;
+  }
   if (kernel == SCTLGPU_LAPLACE3D_FXU)
-    panel_near_kernel<0><<<grid, 32 * PQ_WARPS, 0, (cudaStream_t)stream>>>(p);
+    panel_near_kernel<0><<<grid, 32 * PQ_WARPS, smem, (cudaStream_t)stream>>>(p);
   else
-    panel_near_kernel<1><<<grid, 32 * PQ_WARPS, 0, (cudaStream_t)stream>>>(p);
+    panel_near_kernel<1><<<grid, 32 * PQ_WARPS, smem, (cudaStream_t)stream>>>(p);
   g_launches.fetch_add(1, std::memory_order_relaxed);
   return runtime_record(cudaGetLastError());
 }

@@ -18,7 +18,9 @@ from . import capi
 
 class NearPlan:
     def __init__(self, kernel, blocks, ns: int, nt: int, mode="mixed", digits: int = -1, trg_map=None,
-                 n_out: int | None = None):
+                 n_out: int | None = None, trg_index=None):
+        """trg_index (optional): block target ranges index this list of target indices in [0, nt)
+        (a near list); results then scatter to the listed targets."""
         self.kernel = capi.KERNEL_IDS[kernel] if isinstance(kernel, str) else int(kernel)
         self.mode = capi.MODE_IDS[mode] if isinstance(mode, str) else int(mode)
         self.blocks = np.ascontiguousarray(blocks, dtype=np.int64).reshape(-1, 4)
@@ -29,9 +31,15 @@ class NearPlan:
         if trg_map is not None:
             self._map = np.ascontiguousarray(trg_map, dtype=np.int64)
             tm = self._map.ctypes.data
-        rc = lib.sctlgpu_near_plan_create(ctypes.byref(h), self.kernel, self.mode, int(digits),
-                                          self.blocks.shape[0], self.blocks.ctypes.data if self.blocks.size else None,
-                                          self.ns, self.nt, tm, int(n_out if n_out is not None else -1))
+        ti, n_index = None, 0
+        if trg_index is not None:
+            self._index = np.ascontiguousarray(trg_index, dtype=np.int64)
+            ti, n_index = self._index.ctypes.data, self._index.size
+        rc = lib.sctlgpu_near_plan_create_indexed(ctypes.byref(h), self.kernel, self.mode, int(digits),
+                                                  self.blocks.shape[0],
+                                                  self.blocks.ctypes.data if self.blocks.size else None,
+                                                  self.ns, self.nt, ti, n_index, tm,
+                                                  int(n_out if n_out is not None else -1))
         capi.check(rc, "sctlgpu_near_plan_create")
         self._h = h
 

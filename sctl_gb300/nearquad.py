@@ -65,8 +65,10 @@ class PanelSurface:
         return out
 
     # ------------------------------------------------------------ near field
-    def near_correction(self, r_trg, sigma, pairs, kernel=1, alpha=1.5, max_depth=22, out=None):
-        """Adaptive near-singular correction for every (target, panel) pair."""
+    def near_correction(self, r_trg, sigma, pairs, kernel=1, alpha=1.0, max_depth=22, out=None,
+                        subtract_smooth=True):
+        """Adaptive near-singular integral of every (target, panel) pair, minus (optionally) the
+        panel's smooth-rule part in FP64."""
         xt = r_trg.reshape(-1).contiguous()
         nt = xt.numel() // 3
         t, p = pairs
@@ -77,12 +79,33 @@ class PanelSurface:
         capi.check(capi.load().sctlgpu_panel_near_correction(
             kernel, t.numel(), t.data_ptr(), p.data_ptr(), nt, xt.data_ptr(), self.np, self.X.data_ptr(),
             self.N.data_ptr(), self.Q.data_ptr(), sig.data_ptr(), None, -1, float(alpha), int(max_depth),
-            out.data_ptr(), stream), "near correction")
+            1 if subtract_smooth else 0, out.data_ptr(), stream), "near correction")
         return out
 
-    def evaluate(self, r_trg, sigma, kernel=1, mode="mixed", digits=10, near_factor=1.0, alpha=1.5, pairs=None):
-        out = self.far_field(r_trg, sigma, kernel, mode, digits)
+    def smooth_subtraction_plan(self, nt, pairs, kernel=1, mode="mixed", digits=10):
+        """Near plan that subtracts each near panel's smooth-rule part in the arithmetic and
+        coordinate frame of the far field (blocks: panel nodes x that panel's near list)."""
+        from .near import NearPlan
+        t, p = (a.cpu().numpy() for a in pairs)
+        counts = np.bincount(p, minlength=self.np)
+        starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+        live = np.nonzero(counts)[0]
+        blocks = np.stack([live * self.nn, np.full(live.size, self.nn), starts[live], counts[live]], 1)
+        return NearPlan(kernel, blocks, self.np * self.nn, nt, mode=mode, digits=digits, trg_index=t)
+
+    def evaluate(self, r_trg, sigma, kernel=1, mode="mixed", digits=10, near_factor=1.0, alpha=1.0, pairs=None,
+                 plan=None):
+        """Far field (smooth rule over every node) + near corrections.  The smooth part of the near
+        panels is subtracted with a near plan in the far field's arithmetic, so the large
+        near-singular smooth terms cancel exactly as in the reference's FP64 flow."""
+        xt = r_trg.reshape(-1).contiguous()
+        out = self.far_field(xt, sigma, kernel, mode, digits)
         if pairs is None:
-            pairs = self.near_pairs(r_trg, near_factor)
-        self.near_correction(r_trg, sigma, pairs, kernel, alpha, out=out)
+            pairs = self.near_pairs(xt, near_factor)
+        if plan is None:
+            plan = self.smooth_subtraction_plan(xt.numel() // 3, pairs, kernel, mode, digits)
+        negq = (-self.Q).reshape(-1).contiguous()
+        plan.execute(xt, self.X.reshape(-1), self.N.reshape(-1), sigma.reshape(-1).contiguous(), out, w_src=negq,
+                     accumulate=True)
+        self.near_correction(xt, sigma, pairs, kernel, alpha, out=out, subtract_smooth=False)
         return out

@@ -30,6 +30,8 @@ def test_gauss_law_double_layer(setup):
     exact = np.where(tg["side"] < 0, -1.0, 0.0)
     err = np.abs(v - exact)
     assert err.max() < 1e-8, (err.max(), tg["h"][err.argmax()])
+    from sctl_gb300 import capi
+    assert capi.load().sctlgpu_device_status(None) == capi.OK  # no queue overflow / bad index
 
 
 def test_smooth_rule_alone_is_wrong_near_and_right_far(setup):
@@ -50,6 +52,6 @@ def test_self_convergence_fourier_density(setup):
     tg = T.targets(2000, seed=14)
     xt = torch.from_numpy(tg["r_trg"]).cuda()
     sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()
-    a = S.evaluate(xt, sig, alpha=1.5).cpu().numpy()
-    b = S.evaluate(xt, sig, alpha=3.0, near_factor=2.0).cpu().numpy()
+    a = S.evaluate(xt, sig, alpha=1.0).cpu().numpy()
+    b = S.evaluate(xt, sig, alpha=2.0, near_factor=1.5).cpu().numpy()
     assert np.abs(a - b).max() / np.abs(b).max() < 1e-9
