@@ -177,6 +177,18 @@ int sctlgpu_panel_near_correction(int kernel, int64_t n_pairs, const int64_t* pa
                                   int subtract_smooth, double* v_out, void* stream);
 
 /*
+ * C[M x N] = act(A[M x K] . Bt[N x K]^T + bias) on the tcgen05 tensor cores: A and Bt
+ * row-major BF16 (K contiguous, 16-byte aligned), FP32 accumulation in tensor memory,
+ * act 0 = none, 1 = GELU (tanh form).  Outputs (any may be NULL, not all): C32 (FP32,
+ * after act; added into when accumulate32), pre32 (FP32 before act), C16 (BF16 after
+ * act).  M % 128 == 0, N % 16 == 0 and N <= 256, K % 64 == 0.  The building block of
+ * the near-field correction MLP; no counterpart in the reference.  Device pointers,
+ * asynchronous on `stream`.
+ */
+int sctlgpu_tc_gemm_bf16(int M, int N, int K, const void* A, const void* Bt, const float* bias, int act,
+                         float* C32, float* pre32, void* C16, int accumulate32, void* stream);
+
+/*
  * Runs (or returns the cached result of) the tile autotuner for the batched
  * path on the current device: for each block-size class it times the source
  * split factors 1, 2, 4, 8 on synthetic blocks and keeps the fastest.  Fills

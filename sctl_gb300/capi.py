@@ -48,6 +48,7 @@ SIGNATURES = {
     "sctlgpu_near_plan_status": (_i, [_vp, _vp]),
     "sctlgpu_near_plan_destroy": (_i, [_vp]),
     "sctlgpu_near_autotune": (_i, [_i, _i, _i, _ip]),
+    "sctlgpu_tc_gemm_bf16": (_i, [_i, _i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _vp]),
     "sctlgpu_panel_near_correction": (_i, [_i, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _d,
                                            _i, _i, _vp, _vp]),
 }
