@@ -177,6 +177,18 @@ int sctlgpu_panel_near_correction(int kernel, int64_t n_pairs, const int64_t* pa
                                   int subtract_smooth, double* v_out, void* stream);
 
 /*
+ * Accurate near-singular weights of (target, panel) pairs: for each pair the
+ * 100 values scale * int_P K(x_t - y) l_a(s) l_b(t) dA(y) (l the Lagrange basis of
+ * the panel's 10 x 10 Chebyshev nodes) are written to w_out[pair * 100 + a * 10 + b],
+ * by the same adaptive refinement as sctlgpu_panel_near_correction.  These are
+ * the weights a NearInterac plugin returns (boundary_integral.hpp:164-221) and the
+ * training labels of the correction network.  Device pointers, asynchronous.
+ */
+int sctlgpu_panel_near_weights(int kernel, int64_t n_pairs, const int64_t* pair_trg, const int64_t* pair_panel,
+                               int64_t nt, const double* r_trg, int64_t n_panels, const double* X,
+                               double alpha, int max_depth, double* w_out, void* stream);
+
+/*
  * C[M x N] = act(A[M x K] . Bt[N x K]^T + bias) on the tcgen05 tensor cores: A and Bt
  * row-major BF16 (K contiguous, 16-byte aligned), FP32 accumulation in tensor memory,
  * act 0 = none, 1 = GELU (tanh form).  Outputs (any may be NULL, not all): C32 (FP32,
@@ -187,6 +199,34 @@ int sctlgpu_panel_near_correction(int kernel, int64_t n_pairs, const int64_t* pa
  */
 int sctlgpu_tc_gemm_bf16(int M, int N, int K, const void* A, const void* Bt, const float* bias, int act,
                          float* C32, float* pre32, void* C16, int accumulate32, void* stream);
+
+/*
+ * The near-field correction network: in_dim -> 256 -> 256 -> 256 -> out_dim
+ * (in_dim <= 64, out_dim <= 128), GELU between layers, BF16 weights and
+ * activations with FP32 accumulation on the tcgen05 tensor cores, FP32 master
+ * weights and Adam.  No counterpart in the reference (it predicts the weights a
+ * NearInterac plugin returns, boundary_integral.hpp:164-221).  Batches are
+ * multiples of 128 up to max_batch; x, y, t are FP32 device arrays (row-major,
+ * B x in_dim / B x out_dim).  Parameters are one flat FP32 vector: per layer
+ * W (N x K, row-major; layer-1 K padded to 64, last-layer N padded to 128) then b.
+ */
+typedef struct sctlgpu_mlp_s* sctlgpu_mlp;
+int sctlgpu_mlp_create(sctlgpu_mlp* mlp, int in_dim, int out_dim, int max_batch, uint64_t seed);
+int sctlgpu_mlp_destroy(sctlgpu_mlp mlp);
+int64_t sctlgpu_mlp_num_params(sctlgpu_mlp mlp);
+int sctlgpu_mlp_get_params(sctlgpu_mlp mlp, float* host_out);
+int sctlgpu_mlp_set_params(sctlgpu_mlp mlp, const float* host_in);
+int sctlgpu_mlp_forward(sctlgpu_mlp mlp, int B, const float* x, float* y, void* stream);
+/* Inference with the output dotted in the last GEMM's epilogue:
+ * out[b] += sum_j y[b][j] * dens[index[b] * out_dim + j]  (rows with index[b] < 0 are skipped). */
+int sctlgpu_mlp_forward_dot(sctlgpu_mlp mlp, int B, const float* x, const double* dens, const int64_t* index,
+                            double* out, void* stream);
+/* One Adam step on the mean squared error against t; loss_host (optional) receives the loss (synchronises). */
+int sctlgpu_mlp_train_step(sctlgpu_mlp mlp, int B, const float* x, const float* t, float lr, float* loss_host,
+                           void* stream);
+/* Gradient of the loss with respect to the flat parameters (host output), for checks.  Synchronous. */
+int sctlgpu_mlp_gradients(sctlgpu_mlp mlp, int B, const float* x, const float* t, float* grads_host,
+                          float* loss_host);
 
 /*
  * Runs (or returns the cached result of) the tile autotuner for the batched

@@ -48,6 +48,16 @@ SIGNATURES = {
     "sctlgpu_near_plan_status": (_i, [_vp, _vp]),
     "sctlgpu_near_plan_destroy": (_i, [_vp]),
     "sctlgpu_near_autotune": (_i, [_i, _i, _i, _ip]),
+    "sctlgpu_panel_near_weights": (_i, [_i, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _d, _i, _vp, _vp]),
+    "sctlgpu_mlp_create": (_i, [ctypes.POINTER(_vp), _i, _i, _i, ctypes.c_uint64]),
+    "sctlgpu_mlp_destroy": (_i, [_vp]),
+    "sctlgpu_mlp_num_params": (_i64, [_vp]),
+    "sctlgpu_mlp_get_params": (_i, [_vp, _vp]),
+    "sctlgpu_mlp_set_params": (_i, [_vp, _vp]),
+    "sctlgpu_mlp_forward": (_i, [_vp, _i, _vp, _vp, _vp]),
+    "sctlgpu_mlp_forward_dot": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp]),
+    "sctlgpu_mlp_train_step": (_i, [_vp, _i, _vp, _vp, ctypes.c_float, _vp, _vp]),
+    "sctlgpu_mlp_gradients": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
     "sctlgpu_tc_gemm_bf16": (_i, [_i, _i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _vp]),
     "sctlgpu_panel_near_correction": (_i, [_i, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _d,
                                            _i, _i, _vp, _vp]),

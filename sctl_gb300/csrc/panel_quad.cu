@@ -38,6 +38,9 @@ struct PanelWarpSmem {
   double F[4][PQ_NODES];          // x, y, z, sigma at the panel nodes (a-major: F[c][a*P+b])
   double Ls[PQ_GL][PQ_P], Lds[PQ_GL][PQ_P], Lt[PQ_GL][PQ_P], Ldt[PQ_GL][PQ_P];  // basis at a box's Gauss points
   double A[7][PQ_GL][PQ_P];       // L_s F (x,y,z,sigma) and L_s' F (x,y,z)
+  double Kd[PQ_GL][PQ_GL];        // weights mode: K * dA at a box's Gauss nodes
+  double T[PQ_GL][PQ_P];          // weights mode: Kd . L_t
+  double W[PQ_NODES];             // weights mode: accumulated node weights
   float box[2][PQ_QUEUE][3];      // (s0, t0, size) of the boxes of this and the next round (dyadic: exact)
   float leaf[PQ_QUEUE][3];
 };
@@ -152,7 +155,11 @@ struct PanelParams {
   unsigned* status;
 };
 
-template <int KER>
+// WEIGHTS = false: potential correction added into out[target].  WEIGHTS =
+// true: the accurate weights W_ab = int_P K(x_t - y) l_a(s) l_b(t) dA(y) of the
+// pair's panel (times scale) are written to out[pair * 100 + a * 10 + b]; per
+// box W += L_s^T (K dA) L_t.
+template <int KER, bool WEIGHTS>
 __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel(PanelParams p) {
   extern __shared__ __align__(16) unsigned char pq_smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -174,9 +181,11 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel(PanelParams p
     }
     __syncwarp();
     double acc = 0.0;
+    if (WEIGHTS)
+      for (int q = lane; q < PQ_NODES; q += 32) sm.W[q] = 0.0;
     // Smooth-rule part of this panel, to be subtracted (unless the caller
     // subtracts it in the arithmetic of its far field).
-    for (int q = lane; q < PQ_NODES && p.subtract_smooth; q += 32) {
+    for (int q = lane; q < PQ_NODES && p.subtract_smooth && !WEIGHTS; q += 32) {
       const double r[3] = {xt[0] - sm.F[0][q], xt[1] - sm.F[1][q], xt[2] - sm.F[2][q]};
       const double n[3] = {p.N[(pix * PQ_NODES + q) * 3], p.N[(pix * PQ_NODES + q) * 3 + 1],
                            p.N[(pix * PQ_NODES + q) * 3 + 2]};
@@ -292,16 +301,43 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel(PanelParams p
           n[1] *= iJ;
           n[2] *= iJ;
           const double r[3] = {xt[0] - X[0], xt[1] - X[1], xt[2] - X[2]};
-          acc += kernel_val<KER>(r, n) * sg * J * (bz * bz * c_gl_w[i] * c_gl_w[j]);
+          const double kda = kernel_val<KER>(r, n) * J * (bz * bz * c_gl_w[i] * c_gl_w[j]);
+          if (WEIGHTS)
+            sm.Kd[i][j] = kda;
+          else
+            acc += kda * sg;
         }
         __syncwarp();
+        if (WEIGHTS) {
+          for (int e = lane; e < PQ_GL * PQ_P; e += 32) {
+            const int i = e / PQ_P, b = e % PQ_P;
+            double v = 0.0;
+#pragma unroll
+            for (int j = 0; j < PQ_GL; ++j) v = fma(sm.Kd[i][j], sm.Lt[j][b], v);
+            sm.T[i][b] = v;
+          }
+          __syncwarp();
+          for (int e = lane; e < PQ_NODES; e += 32) {  // each entry owned by one lane
+            const int a = e / PQ_P, b = e % PQ_P;
+            double v = sm.W[e];
+#pragma unroll
+            for (int i = 0; i < PQ_GL; ++i) v = fma(sm.Ls[i][a], sm.T[i][b], v);
+            sm.W[e] = v;
+          }
+          __syncwarp();
+        }
       }
       cur ^= 1;
       ncur = nnext;
     }
+    if (WEIGHTS) {
+      __syncwarp();
+      for (int q = lane; q < PQ_NODES; q += 32) p.out[pr * PQ_NODES + q] = sm.W[q] * p.scale;
+    } else {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) atomicAdd(&p.out[oix], acc * p.scale);
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) atomicAdd(&p.out[oix], acc * p.scale);
+    }
   }
 }
 
@@ -327,6 +363,45 @@ void gauss_legendre01(int n, double* x, double* w) {
   }
 }
 
+int ensure_gl(int dev) {
+  static bool have_gl[64] = {};
+  if (dev < 0 || dev >= 64) return SCTLGPU_ERR_NO_DEVICE;
+  if (!have_gl[dev]) {
+    double gx[PQ_GL], gw[PQ_GL];
+    gauss_legendre01(PQ_GL, gx, gw);
+    cudaError_t e = cudaMemcpyToSymbol(c_gl_x, gx, sizeof(gx));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gl_w, gw, sizeof(gw));
+    if (e != cudaSuccess) return runtime_record(e);
+    have_gl[dev] = true;
+  }
+  return SCTLGPU_OK;
+}
+
+int launch_panel(int kernel, bool weights, const PanelParams& p, unsigned grid, int dev, cudaStream_t st) {
+  const size_t smem = PQ_WARPS * sizeof(PanelWarpSmem);
+  static bool attr[64] = {};
+  if (!attr[dev]) {
+    cudaFuncSetAttribute(panel_near_kernel<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(panel_near_kernel<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(panel_near_kernel<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(panel_near_kernel<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr[dev] = true;
+  }
+  if (kernel == SCTLGPU_LAPLACE3D_FXU) {
+    if (weights)
+      panel_near_kernel<0, true><<<grid, 32 * PQ_WARPS, smem, st>>>(p);
+    else
+      panel_near_kernel<0, false><<<grid, 32 * PQ_WARPS, smem, st>>>(p);
+  } else {
+    if (weights)
+      panel_near_kernel<1, true><<<grid, 32 * PQ_WARPS, smem, st>>>(p);
+    else
+      panel_near_kernel<1, false><<<grid, 32 * PQ_WARPS, smem, st>>>(p);
+  }
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  return runtime_record(cudaGetLastError());
+}
+
 }  // namespace
 }  // namespace sctlgpu
 
@@ -347,15 +422,7 @@ extern "C" int sctlgpu_panel_near_correction(int kernel, int64_t n_pairs, const 
   int sms;
   int rc = runtime_device(&dev, &status, &sms);
   if (rc) return rc;
-  static bool have_gl[64] = {};
-  if (!have_gl[dev]) {
-    double gx[PQ_GL], gw[PQ_GL];
-    gauss_legendre01(PQ_GL, gx, gw);
-    cudaError_t e = cudaMemcpyToSymbol(c_gl_x, gx, sizeof(gx));
-    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gl_w, gw, sizeof(gw));
-    if (e != cudaSuccess) return runtime_record(e);
-    have_gl[dev] = true;
-  }
+  if ((rc = ensure_gl(dev))) return rc;
   PanelParams p;
   p.n_pairs = n_pairs;
   p.n_panels = n_panels;
@@ -377,17 +444,42 @@ extern "C" int sctlgpu_panel_near_correction(int kernel, int64_t n_pairs, const 
   p.status = status;
   const int64_t ctas = (n_pairs + PQ_WARPS - 1) / PQ_WARPS;
   const unsigned grid = (unsigned)(ctas < (int64_t)sms * 16 ? ctas : (int64_t)sms * 16);
-  const size_t smem = PQ_WARPS * sizeof(PanelWarpSmem);
-  static bool attr[64] = {};
-  if (!attr[dev]) {
-    cudaFuncSetAttribute(panel_near_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(panel_near_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr[dev] = true;
-  }
-  if (kernel == SCTLGPU_LAPLACE3D_FXU)
-    panel_near_kernel<0><<<grid, 32 * PQ_WARPS, smem, (cudaStream_t)stream>>>(p);
-  else
-    panel_near_kernel<1><<<grid, 32 * PQ_WARPS, smem, (cudaStream_t)stream>>>(p);
-  g_launches.fetch_add(1, std::memory_order_relaxed);
-  return runtime_record(cudaGetLastError());
+  return launch_panel(kernel, false, p, grid, dev, (cudaStream_t)stream);
+}
+
+extern "C" int sctlgpu_panel_near_weights(int kernel, int64_t n_pairs, const int64_t* pair_trg,
+                                          const int64_t* pair_panel, int64_t nt, const double* r_trg,
+                                          int64_t n_panels, const double* X, double alpha, int max_depth,
+                                          double* w_out, void* stream) {
+  if (kernel != SCTLGPU_LAPLACE3D_FXU && kernel != SCTLGPU_LAPLACE3D_DXU) return SCTLGPU_ERR_INVALID_KERNEL;
+  if (n_pairs < 0 || max_depth < 0 || nt < 0 || n_panels < 0) return SCTLGPU_ERR_INVALID_SIZE;
+  if (!(alpha > 0)) return SCTLGPU_ERR_INVALID_ARGUMENT;
+  if (n_pairs == 0) return SCTLGPU_OK;
+  if (!pair_trg || !pair_panel || !r_trg || !X || !w_out) return SCTLGPU_ERR_NULL_POINTER;
+  int dev;
+  unsigned* status;
+  int sms;
+  int rc = runtime_device(&dev, &status, &sms);
+  if (rc) return rc;
+  if ((rc = ensure_gl(dev))) return rc;
+  PanelParams p{};
+  p.n_pairs = n_pairs;
+  p.n_panels = n_panels;
+  p.nt = nt;
+  p.n_out = nt;
+  p.pair_trg = pair_trg;
+  p.pair_panel = pair_panel;
+  p.r_trg = r_trg;
+  p.X = X;
+  p.N = X;       // unused in weights mode
+  p.Q = X;       // unused in weights mode
+  p.sigma = X;   // unused in weights mode (the interpolated sigma is not needed)
+  p.alpha = alpha;
+  p.max_depth = max_depth < PQ_MAX_DEPTH ? max_depth : PQ_MAX_DEPTH;
+  p.scale = sctlgpu_scale_factor(kernel);
+  p.out = w_out;
+  p.status = status;
+  const int64_t ctas = (n_pairs + PQ_WARPS - 1) / PQ_WARPS;
+  const unsigned grid = (unsigned)(ctas < (int64_t)sms * 16 ? ctas : (int64_t)sms * 16);
+  return launch_panel(kernel, true, p, grid, dev, (cudaStream_t)stream);
 }

@@ -1,0 +1,187 @@
+"""Learned near-singular quadrature: a small MLP predicts the 100 accurate
+weights W_ab(t) = int_P K(x_t - y) l_a(s) l_b(t) dA(y) of a (target, panel)
+pair from the target's local coordinates (s, t, h) and 12 panel-geometry
+features; the pair's correction is then sum_ab (W_ab - W^smooth_ab) sigma_ab.
+
+* Labels come from the adaptive quadrature (`sctlgpu_panel_near_weights`).
+* Training and inference run on the tcgen05 kernels of libsctlgpu
+  (`sctlgpu_mlp_*`): BF16 weights and activations, FP32 accumulation.
+* Two networks trained from different seeds form the a-posteriori check: where
+  their predicted corrections differ by more than the tolerance, or the pair is
+  outside the trained range, the plain adaptive path (the judge of the error)
+  is used instead.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import capi
+
+IN_DIM, OUT_DIM = 15, 100
+
+
+class MLP:
+    """in -> 256 -> 256 -> 256 -> out network living on the GPU (libsctlgpu)."""
+
+    def __init__(self, in_dim=IN_DIM, out_dim=OUT_DIM, max_batch=1 << 14, seed=0):
+        self.in_dim, self.out_dim, self.max_batch = in_dim, out_dim, max_batch
+        h = ctypes.c_void_p()
+        capi.check(capi.load().sctlgpu_mlp_create(ctypes.byref(h), in_dim, out_dim, max_batch, seed), "mlp_create")
+        self._h = h
+        self.n_params = int(capi.load().sctlgpu_mlp_num_params(h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            capi.load().sctlgpu_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.n_params, np.float32)
+        capi.check(capi.load().sctlgpu_mlp_get_params(self._h, out.ctypes.data), "mlp_get_params")
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        capi.check(capi.load().sctlgpu_mlp_set_params(self._h, p.ctypes.data), "mlp_set_params")
+
+    def layers(self, p=None):
+        """Split the flat parameters into [(W, b)] with W (N x K) as stored."""
+        p = self.get_params() if p is None else p
+        dims = [(256, 64), (256, 256), (256, 256), (128, 256)]
+        out, o = [], 0
+        for n, k in dims:
+            W = p[o:o + n * k].reshape(n, k)
+            o += n * k
+            b = p[o:o + n]
+            o += n
+            out.append((W, b))
+        return out
+
+    def _pad(self, x):
+        B = x.shape[0]
+        Bp = (B + 127) // 128 * 128
+        if Bp != B:
+            x = torch.cat([x, torch.zeros(Bp - B, x.shape[1], dtype=x.dtype, device=x.device)])
+        return x.contiguous(), B, Bp
+
+    def forward(self, x: torch.Tensor) -> torch.Tensor:
+        """x: (B, in_dim) FP32 CUDA -> (B, out_dim) FP32."""
+        outs = []
+        for a in range(0, x.shape[0], self.max_batch):
+            xb, B, Bp = self._pad(x[a:a + self.max_batch].float())
+            y = torch.empty(Bp, self.out_dim, dtype=torch.float32, device=x.device)
+            capi.check(capi.load().sctlgpu_mlp_forward(self._h, Bp, xb.data_ptr(), y.data_ptr(),
+                                                       torch.cuda.current_stream().cuda_stream), "mlp_forward")
+            outs.append(y[:B])
+        return torch.cat(outs)
+
+    def forward_dot(self, x: torch.Tensor, dens: torch.Tensor, index: torch.Tensor, out: torch.Tensor):
+        """out[b] += sum_j y[b, j] * dens[index[b], j] (fused into the last GEMM's epilogue)."""
+        for a in range(0, x.shape[0], self.max_batch):
+            xb, B, Bp = self._pad(x[a:a + self.max_batch].float())
+            idx = torch.full((Bp,), -1, dtype=torch.int64, device=x.device)
+            idx[:B] = index[a:a + B]
+            o = torch.zeros(Bp, dtype=torch.float64, device=x.device)
+            capi.check(capi.load().sctlgpu_mlp_forward_dot(self._h, Bp, xb.data_ptr(), dens.data_ptr(), idx.data_ptr(),
+                                                           o.data_ptr(), torch.cuda.current_stream().cuda_stream),
+                       "mlp_forward_dot")
+            out[a:a + B] += o[:B]
+        return out
+
+    def train_step(self, x: torch.Tensor, t: torch.Tensor, lr: float, want_loss=False):
+        loss = ctypes.c_float(0.0)
+        capi.check(capi.load().sctlgpu_mlp_train_step(self._h, x.shape[0], x.data_ptr(), t.data_ptr(), float(lr),
+                                                      ctypes.byref(loss) if want_loss else None,
+                                                      torch.cuda.current_stream().cuda_stream), "mlp_train_step")
+        return loss.value if want_loss else None
+
+    def gradients(self, x: torch.Tensor, t: torch.Tensor):
+        g = np.empty(self.n_params, np.float32)
+        loss = ctypes.c_float(0.0)
+        capi.check(capi.load().sctlgpu_mlp_gradients(self._h, x.shape[0], x.data_ptr(), t.data_ptr(), g.ctypes.data,
+                                                     ctypes.byref(loss)), "mlp_gradients")
+        return g, loss.value
+
+
+def panel_weights(kernel, pairs_t, pairs_p, r_trg, X, alpha=1.0, max_depth=22):
+    """Accurate weights (n_pairs, 100) of (target, panel) pairs by adaptive quadrature."""
+    n = pairs_t.numel()
+    w = torch.empty(n, 100, dtype=torch.float64, device=r_trg.device)
+    if n:
+        capi.check(capi.load().sctlgpu_panel_near_weights(
+            kernel, n, pairs_t.data_ptr(), pairs_p.data_ptr(), r_trg.numel() // 3, r_trg.data_ptr(), X.shape[0],
+            X.data_ptr(), float(alpha), int(max_depth), w.data_ptr(), torch.cuda.current_stream().cuda_stream),
+            "panel_near_weights")
+    return w
+
+
+def smooth_weights(kernel, pairs_t, pairs_p, r_trg, X, N, Q):
+    """Smooth-rule weights (n_pairs, 100): scale * K(x_t - X_ab, N_ab) * Q_ab."""
+    xt = r_trg.reshape(-1, 3)[pairs_t]                       # (n, 3)
+    Xp, Np, Qp = X[pairs_p], N[pairs_p], Q[pairs_p]          # (n, 100, 3), (n, 100)
+    r = xt[:, None, :] - Xp
+    r2 = (r * r).sum(-1)
+    ri = torch.where(r2 > 0, r2.rsqrt(), torch.zeros_like(r2))
+    k = ri if kernel == 0 else (r * Np).sum(-1) * ri ** 3
+    return k * Qp * capi.load().sctlgpu_scale_factor(kernel)
+
+
+class Standardizer:
+    def __init__(self, x: torch.Tensor):
+        self.mu = x.mean(0)
+        self.sd = x.std(0).clamp_min(1e-12)
+
+    def fwd(self, x):
+        return ((x - self.mu) / self.sd).float()
+
+    def inv(self, y):
+        return y.double() * self.sd + self.mu
+
+
+class LearnedCorrection:
+    """Ensemble of correction networks with range gating and a disagreement check."""
+
+    def __init__(self, n_models=2, max_batch=1 << 14, seeds=(1, 2)):
+        self.models = [MLP(max_batch=max_batch, seed=s) for s in seeds[:n_models]]
+        self.fx = self.fy = None
+        self.range = None
+
+    def fit(self, feats: torch.Tensor, w: torch.Tensor, steps=2000, batch=1 << 14, lr=2e-3, seed=0, log=None):
+        """Train every model on (features, accurate weights); returns the final losses."""
+        self.fx, self.fy = Standardizer(feats), Standardizer(w)
+        self.range = (feats.min(0).values, feats.max(0).values)
+        X, Y = self.fx.fwd(feats).contiguous(), self.fy.fwd(w).contiguous()
+        n = X.shape[0]
+        g = torch.Generator(device=X.device).manual_seed(seed)
+        losses = []
+        for mi, m in enumerate(self.models):
+            last = None
+            for it in range(steps):
+                idx = torch.randint(0, n, (batch,), device=X.device, generator=g)
+                lr_t = lr * 0.5 * (1 + np.cos(np.pi * it / steps))
+                want = it == steps - 1 or (log and it % 500 == 0)
+                loss = m.train_step(X[idx].contiguous(), Y[idx].contiguous(), lr_t, want_loss=want)
+                if want:
+                    last = loss
+                    if log:
+                        log(f"model {mi} step {it} loss {loss:.4e}")
+            losses.append(last)
+        return losses
+
+    def in_range(self, feats):
+        lo, hi = self.range
+        return ((feats >= lo) & (feats <= hi)).all(1)
+
+    def predict(self, feats: torch.Tensor):
+        """Per-model predicted accurate weights, (n_models, n, 100) FP64."""
+        x = self.fx.fwd(feats).contiguous()
+        return torch.stack([self.fy.inv(m.forward(x)) for m in self.models])
