@@ -185,3 +185,47 @@ class LearnedCorrection:
         """Per-model predicted accurate weights, (n_models, n, 100) FP64."""
         x = self.fx.fwd(feats).contiguous()
         return torch.stack([self.fy.inv(m.forward(x)) for m in self.models])
+
+
+def learned_near_field(S, T, L: LearnedCorrection, r_trg: torch.Tensor, sigma: torch.Tensor, tol: float,
+                       kernel=1, mode="mixed", digits=10, near_factor=1.0, alpha=1.0, pairs=None, plan=None,
+                       stats=None):
+    """Potential with learned near corrections where the two networks agree to `tol` (per pair) and
+    the pair is inside the trained feature range; the plain adaptive path elsewhere."""
+    from .torus import pair_features
+    xt = r_trg.reshape(-1).contiguous()
+    nt = xt.numel() // 3
+    out = S.far_field(xt, sigma, kernel, mode, digits)
+    if pairs is None:
+        pairs = S.near_pairs(xt, near_factor)
+    if plan is None:
+        plan = S.smooth_subtraction_plan(nt, pairs, kernel, mode, digits)
+    negq = (-S.Q).reshape(-1).contiguous()
+    plan.execute(xt, S.X.reshape(-1), S.N.reshape(-1), sigma.reshape(-1).contiguous(), out, w_src=negq,
+                 accumulate=True)
+    pt, pp = pairs
+    f = torch.from_numpy(pair_features(T, xt.reshape(-1, 3).cpu().numpy(), pt.cpu().numpy(),
+                                       pp.cpu().numpy())).to(xt.device)
+    ok = L.in_range(f)
+    sig = sigma.reshape(S.np, S.nn)
+    dens = (sig * L.fy.sd[None]).contiguous()
+    const = (sig * L.fy.mu[None]).sum(1)
+    idx = torch.nonzero(ok, as_tuple=True)[0]
+    x = L.fx.fwd(f[idx]).contiguous()
+    preds = []
+    for m in L.models:
+        o = torch.zeros(idx.numel(), dtype=torch.float64, device=xt.device)
+        m.forward_dot(x, dens, pp[idx].contiguous(), o)
+        preds.append(o + const[pp[idx]])
+    agree = (preds[0] - preds[1]).abs() <= tol
+    acc_idx = idx[agree]
+    out.index_add_(0, pt[acc_idx], 0.5 * (preds[0][agree] + preds[1][agree]))
+    rej = torch.ones(pt.numel(), dtype=torch.bool, device=xt.device)
+    rej[acc_idx] = False
+    rt, rp = pt[rej].contiguous(), pp[rej].contiguous()
+    if rt.numel():
+        S.near_correction(xt, sigma, (rt, rp), kernel, alpha, out=out, subtract_smooth=False)
+    if stats is not None:
+        stats.update(pairs=int(pt.numel()), in_range=int(ok.sum()), accepted=int(acc_idx.numel()),
+                     fallback=int(rt.numel()))
+    return out

@@ -129,3 +129,34 @@ class Torus:
         w = np.outer(np.tile(self.w1d, k) / k, np.tile(self.w1d, k) / k).reshape(-1)
         s, t = np.meshgrid(sub, sub, indexing="ij")
         return Lu, w, np.stack([s.reshape(-1), t.reshape(-1)], 1)
+
+
+def foot_point(xt):
+    """Closest point on the torus of each target: angles (theta, phi) and signed distance (+ outside)."""
+    x, y, z = xt[..., 0], xt[..., 1], xt[..., 2]
+    th = np.arctan2(y, x)
+    rho = np.hypot(x, y)
+    ph = np.arctan2(z, rho - R_MAJOR)
+    d = np.hypot(rho - R_MAJOR, z) - R_MINOR
+    return th, ph, d
+
+
+def pair_features(T: "Torus", xt, pt, pp):
+    """15 features of (target, panel) pairs: local coordinates (s, t) of the target's foot point in
+    the panel's parameter square (outside [0,1] for neighbouring panels), the signed log distance
+    in panel sizes, and 12 panel-geometry features (metric, curvatures, size; constant per ring)."""
+    th, ph, d = foot_point(xt[pt])
+    th0, ph0 = T.theta0[pp], T.phi0[pp]
+    s = np.remainder(th - th0 + np.pi, 2 * np.pi) - np.pi
+    t = np.remainder(ph - ph0 + np.pi, 2 * np.pi) - np.pi
+    s, t = s / T.dth, t / T.dph
+    size = T.size[pp]
+    hr = np.abs(d) / size
+    hf = np.sign(d) * (np.log10(np.maximum(hr, 1e-6)) + 6.0) / 6.0
+    phc = ph0 + 0.5 * T.dph
+    rho = R_MAJOR + R_MINOR * np.cos(phc)
+    lth, lph = rho * T.dth / size, R_MINOR * T.dph / size
+    k1, k2 = np.cos(phc) / rho * size, size / R_MINOR
+    geo = np.stack([np.cos(phc), np.sin(phc), rho, lth, lph, k1, k2, size * 10.0, T.area[pp] / size ** 2,
+                    lth / lph, k1 * k2, 0.5 * (k1 + k2)], 1)
+    return np.concatenate([np.stack([s, t, hf], 1), geo], 1)

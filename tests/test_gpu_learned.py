@@ -1,0 +1,61 @@
+"""Learned near-singular correction on the torus: trained on the GPU from
+adaptive-quadrature labels, it must remove most of the smooth rule's
+near-field error at negligible cost (the gain over the method without it),
+and with a tight tolerance the disagreement check must hand the pairs back to
+the plain path so the result still meets it."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def trained(cuda):
+    torch = cuda
+    from sctl_gb300.learned import LearnedCorrection, panel_weights
+    from sctl_gb300.nearquad import PanelSurface
+    from sctl_gb300.torus import Torus, pair_features
+    T = Torus(seed=0)
+    S = PanelSurface(T.X, T.N, T.Q, T.size)
+    tg = T.targets(24000, seed=100)
+    xt = torch.from_numpy(tg["r_trg"]).cuda().reshape(-1).contiguous()
+    pt, pp = S.near_pairs(xt, 1.0)
+    W = panel_weights(1, pt, pp, xt, S.X)
+    f = torch.from_numpy(pair_features(T, tg["r_trg"], pt.cpu().numpy(), pp.cpu().numpy())).cuda()
+    L = LearnedCorrection(max_batch=8192)
+    losses = L.fit(f, W, steps=1200, batch=8192, lr=2e-3)
+    return torch, T, S, L, losses
+
+
+def test_training_converged(trained):
+    _, _, _, _, losses = trained
+    assert all(l < 0.05 for l in losses), losses  # standardized MSE
+
+
+def test_learned_correction_gain_over_smooth_rule(trained):
+    torch, T, S, L, _ = trained
+    from sctl_gb300.learned import learned_near_field
+    tg = T.targets(2000, seed=200)
+    xt = torch.from_numpy(tg["r_trg"]).cuda()
+    sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()
+    plain = S.evaluate(xt, sig).cpu().numpy()
+    smooth = S.far_field(xt.reshape(-1), sig).cpu().numpy()
+    st = {}
+    learned = learned_near_field(S, T, L, xt, sig, tol=1e30, stats=st).cpu().numpy()
+    e_smooth = np.abs(smooth - plain).max()
+    e_learned = np.abs(learned - plain).max()
+    assert st["fallback"] <= st["pairs"] - st["in_range"]
+    assert e_learned < 1e-2 * e_smooth, (e_learned, e_smooth)
+
+
+def test_tight_tolerance_falls_back_to_plain_path(trained):
+    torch, T, S, L, _ = trained
+    from sctl_gb300.learned import learned_near_field
+    tg = T.targets(1000, seed=300)
+    xt = torch.from_numpy(tg["r_trg"]).cuda()
+    sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()
+    plain = S.evaluate(xt, sig).cpu().numpy()
+    st = {}
+    out = learned_near_field(S, T, L, xt, sig, tol=1e-12, stats=st).cpu().numpy()
+    assert st["fallback"] >= 0.99 * st["pairs"]
+    assert np.abs(out - plain).max() / np.abs(plain).max() < 1e-8
