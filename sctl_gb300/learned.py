@@ -189,9 +189,11 @@ class LearnedCorrection:
 
 def learned_near_field(S, T, L: LearnedCorrection, r_trg: torch.Tensor, sigma: torch.Tensor, tol: float,
                        kernel=1, mode="mixed", digits=10, near_factor=1.0, alpha=1.0, pairs=None, plan=None,
-                       stats=None):
-    """Potential with learned near corrections where the two networks agree to `tol` (per pair) and
-    the pair is inside the trained feature range; the plain adaptive path elsewhere."""
+                       stats=None, h_cut=0.1):
+    """Potential with learned near corrections where the pair is near-singular (the target's foot point
+    inside the panel and its distance below h_cut panel sizes -- elsewhere the smooth rule is already
+    accurate and the network would only add its own error), inside the trained feature range, and the
+    two networks agree to `tol`; the plain adaptive path for every other near pair."""
     from .torus import pair_features
     xt = r_trg.reshape(-1).contiguous()
     nt = xt.numel() // 3
@@ -206,7 +208,9 @@ def learned_near_field(S, T, L: LearnedCorrection, r_trg: torch.Tensor, sigma: t
     pt, pp = pairs
     f = torch.from_numpy(pair_features(T, xt.reshape(-1, 3).cpu().numpy(), pt.cpu().numpy(),
                                        pp.cpu().numpy())).to(xt.device)
-    ok = L.in_range(f)
+    hfeat_cut = (np.log10(h_cut) + 6.0) / 6.0
+    singular = (f[:, 0] >= 0) & (f[:, 0] <= 1) & (f[:, 1] >= 0) & (f[:, 1] <= 1) & (f[:, 2].abs() < hfeat_cut)
+    ok = L.in_range(f) & singular
     sig = sigma.reshape(S.np, S.nn)
     dens = (sig * L.fy.sd[None]).contiguous()
     const = (sig * L.fy.mu[None]).sum(1)
@@ -226,6 +230,6 @@ def learned_near_field(S, T, L: LearnedCorrection, r_trg: torch.Tensor, sigma: t
     if rt.numel():
         S.near_correction(xt, sigma, (rt, rp), kernel, alpha, out=out, subtract_smooth=False)
     if stats is not None:
-        stats.update(pairs=int(pt.numel()), in_range=int(ok.sum()), accepted=int(acc_idx.numel()),
+        stats.update(pairs=int(pt.numel()), candidates=int(ok.sum()), accepted=int(acc_idx.numel()),
                      fallback=int(rt.numel()))
     return out
