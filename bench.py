@@ -256,6 +256,57 @@ def cube_section(torch, stream):
             "rel_l2_vs_cpu": O.rel_l2(gpu, ref)}
 
 
+def torus_section(torch, n_eval=1 << 16, n_train=48000, steps=2000):
+    """Near-singular Laplace double layer on the 64 x 32-panel torus (204,800 nodes): plain path
+    (far field + smooth subtraction + adaptive panel corrections) vs the learned path (two
+    tcgen05 networks, gated, plain-path fallback).  n_eval targets stand in for the 2^20 of the
+    workload (cost is linear in targets); labels from n_train targets' near pairs."""
+    from sctl_gb300.learned import LearnedCorrection, learned_near_field, panel_weights
+    from sctl_gb300.nearquad import PanelSurface
+    from sctl_gb300.torus import Torus, pair_features
+    T = Torus(seed=0)
+    S = PanelSurface(T.X, T.N, T.Q, T.size)
+    res = {"workload": f"torus R=1 r=0.3, 64x32 panels x 10x10 Chebyshev nodes, {n_eval} targets at h in "
+                       f"[1e-4,1] panel sizes (log-uniform), Laplace3D_DxU, far field mixed digits 10"}
+    tg = T.targets(n_eval, seed=7)
+    xt = torch.from_numpy(tg["r_trg"]).cuda().reshape(-1).contiguous()
+    one = torch.ones(T.np * 100, dtype=torch.float64, device="cuda")
+    sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()
+    pairs = S.near_pairs(xt, 1.0)
+    plan = S.smooth_subtraction_plan(n_eval, pairs)
+    res["near_pairs"] = int(pairs[0].numel())
+    v1 = S.evaluate(xt, one, pairs=pairs, plan=plan).cpu().numpy()
+    exact = np.where(tg["side"] < 0, -1.0, 0.0)
+    res["plain_gauss_law_max_abs_err"] = float(np.abs(v1 - exact).max())
+    t_plain = _ev_ms(torch, lambda: S.evaluate(xt, sig, pairs=pairs, plan=plan), reps=2)
+    plain = S.evaluate(xt, sig, pairs=pairs, plan=plan)
+    res["plain_ms"] = t_plain
+    res["plain_far_field_ms"] = _ev_ms(torch, lambda: S.far_field(xt, sig), reps=2)
+    # learned path
+    tt = T.targets(n_train, seed=100)
+    xtr = torch.from_numpy(tt["r_trg"]).cuda().reshape(-1).contiguous()
+    pt, pp = S.near_pairs(xtr, 1.0)
+    t0 = time.perf_counter()
+    W = panel_weights(1, pt, pp, xtr, S.X)
+    torch.cuda.synchronize()
+    res["labels"] = int(pt.numel())
+    res["label_s"] = time.perf_counter() - t0
+    f = torch.from_numpy(pair_features(T, tt["r_trg"], pt.cpu().numpy(), pp.cpu().numpy())).cuda()
+    L = LearnedCorrection(max_batch=1 << 14)
+    t0 = time.perf_counter()
+    res["train_losses"] = L.fit(f, W, steps=steps, batch=1 << 14, lr=3e-3)
+    torch.cuda.synchronize()
+    res["train_s"] = time.perf_counter() - t0
+    for tol in (1e-8, 1e-3):
+        st = {}
+        out = learned_near_field(S, T, L, xt, sig, tol, pairs=pairs, plan=plan, stats=st)
+        ms = _ev_ms(torch, lambda: learned_near_field(S, T, L, xt, sig, tol, pairs=pairs, plan=plan), reps=2)
+        err = (out - plain).abs().max().item() / plain.abs().max().item()
+        res[f"learned_tol{tol:g}"] = {"ms": ms, "speedup_vs_plain": t_plain / ms, "max_rel_err_vs_plain": err,
+                                      **st}
+    return res
+
+
 def main():
     global KERNELS, N_SRC
     ap = argparse.ArgumentParser()
@@ -268,6 +319,7 @@ def main():
     ap.add_argument("--ns", type=int, default=N_SRC, help="sources")
     ap.add_argument("--kernels", default="1,2,3", help="kernel ids of the step (default: the three sphere/ball kernels)")
     ap.add_argument("--quick", action="store_true", help="timed region only (for profiler runs)")
+    ap.add_argument("--skip-torus", action="store_true", help="omit the near-singular torus section")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -438,6 +490,8 @@ def main():
         extras["near_field_blocks"] = near_field_section(torch, stream)
         extras["precision_stress_clusters"] = cluster_section(torch, stream)
         extras["cube8192_fp64_d14"] = cube_section(torch, stream)
+        if not args.skip_torus:
+            extras["torus_near_singular"] = torus_section(torch)
 
     line = {"metric": "Laplace/Stokes Ginteractions/s mixed vs FP64 @1e-10", "value": value,
             "unit": "Ginteractions/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
