@@ -256,7 +256,57 @@ def cube_section(torch, stream):
             "rel_l2_vs_cpu": O.rel_l2(gpu, ref)}
 
 
-def torus_section(torch, n_eval=1 << 16, n_train=48000, steps=2000):
+def mlp_section(torch, stream):
+    """tcgen05 BF16 tensor-core path: one large GEMM (65536 x 256 x 4096) and the correction network
+    (15 -> 256 -> 256 -> 256 -> 100, GELU) forward on 2^17 pairs and training steps on 2^14 pairs,
+    against the measured cuBLAS bf16 peak."""
+    import math
+
+    from sctl_gb300 import capi
+    from sctl_gb300.learned import MLP
+    pk = peaks()
+    peak_tf = pk.get("bf16_tflops", 1900.0)
+    res = {}
+    M, N, K = 65536, 256, 4096
+    g = torch.Generator(device="cuda").manual_seed(0)
+    A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
+    Bt = (torch.randn(N, K, device="cuda", generator=g) / math.sqrt(K)).to(torch.bfloat16)
+    C = torch.empty(M, N, device="cuda")
+    lib = capi.load()
+    gemm = lambda: capi.check(lib.sctlgpu_tc_gemm_bf16(M, N, K, A.data_ptr(), Bt.data_ptr(), None, 0,  # noqa: E731
+                                                       C.data_ptr(), None, None, 0, stream.cuda_stream), "tc_gemm")
+    gemm()
+    ms = _ev_ms(torch, gemm, reps=5)
+    ref = A[:256].float() @ Bt.float().T
+    flops = 2.0 * M * N * K
+    res["gemm_65536x256x4096"] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12,
+                                  "frac_of_measured_bf16": flops / (ms * 1e-3) / 1e12 / peak_tf,
+                                  "rel_err_vs_fp32": ((C[:256] - ref).abs().max() / ref.abs().max()).item()}
+    del A, Bt, C
+    net = MLP(max_batch=1 << 17, seed=3)
+    alg = 2.0 * (15 * 256 + 2 * 256 * 256 + 256 * 100)  # algorithmic flops per pair (unpadded layers)
+    padded = 2.0 * (64 * 256 + 2 * 256 * 256 + 256 * 128)
+    B = 1 << 17
+    x = torch.randn(B, 15, device="cuda", generator=g)
+    fwd = lambda: net.forward(x)  # noqa: E731
+    fwd()
+    ms = _ev_ms(torch, fwd, reps=5)
+    res["forward_2p17"] = {"ms": ms, "pairs_per_s": B / (ms * 1e-3), "tflops_alg": alg * B / (ms * 1e-3) / 1e12,
+                           "tflops_padded": padded * B / (ms * 1e-3) / 1e12,
+                           "frac_of_measured_bf16": padded * B / (ms * 1e-3) / 1e12 / peak_tf}
+    Bt_ = 1 << 14
+    xt, yt = torch.randn(Bt_, 15, device="cuda", generator=g), torch.randn(Bt_, 100, device="cuda", generator=g)
+    train = lambda: net.train_step(xt, yt, 1e-4)  # noqa: E731
+    train()
+    ms = _ev_ms(torch, train, reps=5)
+    res["train_step_2p14"] = {"ms": ms, "tflops_padded": 3 * padded * Bt_ / (ms * 1e-3) / 1e12,
+                              "frac_of_measured_bf16": 3 * padded * Bt_ / (ms * 1e-3) / 1e12 / peak_tf}
+    net.close()
+    res["peak_basis"] = f"bf16_tflops {peak_tf} of MEASURED_PEAKS.json (cuBLAS 8192^3 burst)"
+    return res
+
+
+def torus_section(torch, n_eval=1 << 16, n_train=48000, steps=2000, learned=True):
     """Near-singular Laplace double layer on the 64 x 32-panel torus (204,800 nodes): plain path
     (far field + smooth subtraction + adaptive panel corrections) vs the learned path (two
     tcgen05 networks, gated, plain-path fallback).  n_eval targets stand in for the 2^20 of the
@@ -282,6 +332,8 @@ def torus_section(torch, n_eval=1 << 16, n_train=48000, steps=2000):
     plain = S.evaluate(xt, sig, pairs=pairs, plan=plan)
     res["plain_ms"] = t_plain
     res["plain_far_field_ms"] = _ev_ms(torch, lambda: S.far_field(xt, sig), reps=2)
+    if not learned:
+        return res
     # learned path
     tt = T.targets(n_train, seed=100)
     xtr = torch.from_numpy(tt["r_trg"]).cuda().reshape(-1).contiguous()
@@ -320,10 +372,24 @@ def main():
     ap.add_argument("--kernels", default="1,2,3", help="kernel ids of the step (default: the three sphere/ball kernels)")
     ap.add_argument("--quick", action="store_true", help="timed region only (for profiler runs)")
     ap.add_argument("--skip-torus", action="store_true", help="omit the near-singular torus section")
+    ap.add_argument("--section", choices=["near", "clusters", "cube", "torus", "torus_plain", "mlp"],
+                    help="run only this secondary workload and print its JSON (profiling of one kernel family)")
+    ap.add_argument("--torus-n", type=int, default=1 << 16, help="targets of the torus section")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.section:
+        import torch
+        from sctl_gb300 import capi
+        capi.load()
+        stream = torch.cuda.current_stream()
+        fn = {"near": lambda: near_field_section(torch, stream), "clusters": lambda: cluster_section(torch, stream),
+              "cube": lambda: cube_section(torch, stream), "mlp": lambda: mlp_section(torch, stream),
+              "torus": lambda: torus_section(torch, n_eval=args.torus_n),
+              "torus_plain": lambda: torus_section(torch, n_eval=args.torus_n, learned=False)}[args.section]
+        print(json.dumps({"section": args.section, **fn()}), flush=True)
+        return
 
     import torch
     import torch.distributed as dist
@@ -490,6 +556,7 @@ def main():
         extras["near_field_blocks"] = near_field_section(torch, stream)
         extras["precision_stress_clusters"] = cluster_section(torch, stream)
         extras["cube8192_fp64_d14"] = cube_section(torch, stream)
+        extras["tensor_core_mlp"] = mlp_section(torch, stream)
         if not args.skip_torus:
             extras["torus_near_singular"] = torus_section(torch)
 

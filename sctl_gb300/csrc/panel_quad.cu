@@ -46,6 +46,9 @@ struct PanelWarpSmem {
 };
 
 __constant__ double c_gl_x[PQ_GL], c_gl_w[PQ_GL];
+// First-kind Chebyshev points of [0,1] (ChebQuadRule's nodes) and their
+// barycentric weights (-1)^a sin((2a+1) pi / 2P), computed once on the host.
+__constant__ double c_ch_x[PQ_P], c_ch_w[PQ_P];
 
 struct Basis {
   double l[PQ_P], d[PQ_P];
@@ -54,15 +57,11 @@ struct Basis {
 // Barycentric Lagrange basis on the first-kind Chebyshev points of [0,1] and
 // its derivative: l_a(s) = (w_a/(s-x_a)) / sum_b w_b/(s-x_b),
 // l_a'(s) = l_a(s) * (sum_b w_b/(s-x_b)^2 / sum_b w_b/(s-x_b) - 1/(s-x_a)).
-__device__ void basis(double s, Basis& B) {
-  double xs[PQ_P], ws[PQ_P];
+__device__ __forceinline__ void basis(double s, Basis& B) {
   int hit = -1;
 #pragma unroll
-  for (int a = 0; a < PQ_P; ++a) {
-    xs[a] = 0.5 - 0.5 * cospi((2.0 * a + 1.0) / (2.0 * PQ_P));
-    ws[a] = ((a & 1) ? -1.0 : 1.0) * sinpi((2.0 * a + 1.0) / (2.0 * PQ_P));
-    if (s == xs[a]) hit = a;
-  }
+  for (int a = 0; a < PQ_P; ++a)
+    if (s == c_ch_x[a]) hit = a;
   if (hit >= 0) {  // at a node: l is a unit vector; l' from the differentiation matrix row
 #pragma unroll
     for (int a = 0; a < PQ_P; ++a) {
@@ -70,34 +69,36 @@ __device__ void basis(double s, Basis& B) {
       B.d[a] = 0.0;
     }
     double diag = 0.0;
+    const double xh = c_ch_x[hit], iwh = 1.0 / c_ch_w[hit];
 #pragma unroll
     for (int a = 0; a < PQ_P; ++a)
       if (a != hit) {
-        B.d[a] = (ws[a] / ws[hit]) / (xs[hit] - xs[a]);
+        B.d[a] = (c_ch_w[a] * iwh) / (xh - c_ch_x[a]);
         diag -= B.d[a];
       }
-    B.d[hit] = diag;
+#pragma unroll
+    for (int a = 0; a < PQ_P; ++a)  // static indices keep B in registers
+      if (a == hit) B.d[a] = diag;
     return;
   }
-  double T = 0.0, U = 0.0, t[PQ_P];
+  double T = 0.0, U = 0.0, t[PQ_P], r[PQ_P];
 #pragma unroll
   for (int a = 0; a < PQ_P; ++a) {
-    const double r = 1.0 / (s - xs[a]);
-    t[a] = ws[a] * r;
+    r[a] = 1.0 / (s - c_ch_x[a]);
+    t[a] = c_ch_w[a] * r[a];
     T += t[a];
-    U += t[a] * r;
+    U += t[a] * r[a];
   }
   const double iT = 1.0 / T, UT = U * iT;
 #pragma unroll
   for (int a = 0; a < PQ_P; ++a) {
-    const double r = 1.0 / (s - xs[a]);
     B.l[a] = t[a] * iT;
-    B.d[a] = B.l[a] * (UT - r);  // d/ds of t_a/T = (-t_a r T + t_a U) / T^2
+    B.d[a] = B.l[a] * (UT - r[a]);  // d/ds of t_a/T = (-t_a r T + t_a U) / T^2
   }
 }
 
 // Geometry and density at (s, t): position, tangents (per unit s, t) and sigma.
-__device__ void interp(const double (*F)[PQ_NODES], double s, double t, double X[3], double Xs[3], double Xt[3],
+__device__ __forceinline__ void interp(const double (*F)[PQ_NODES], double s, double t, double X[3], double Xs[3], double Xt[3],
                        double& sig, bool need_sig) {
   Basis A, B;
   basis(s, A);
@@ -106,6 +107,7 @@ __device__ void interp(const double (*F)[PQ_NODES], double s, double t, double X
   for (int c = 0; c < 4; ++c) {
     if (c == 3 && !need_sig) break;
     double v = 0, vs = 0, vt = 0;
+#pragma unroll
     for (int a = 0; a < PQ_P; ++a) {
       double r = 0, rt = 0;
 #pragma unroll
@@ -367,10 +369,17 @@ int ensure_gl(int dev) {
   static bool have_gl[64] = {};
   if (dev < 0 || dev >= 64) return SCTLGPU_ERR_NO_DEVICE;
   if (!have_gl[dev]) {
-    double gx[PQ_GL], gw[PQ_GL];
+    double gx[PQ_GL], gw[PQ_GL], cx[PQ_P], cw[PQ_P];
     gauss_legendre01(PQ_GL, gx, gw);
+    const double pi = 3.14159265358979323846264338327950288;
+    for (int a = 0; a < PQ_P; ++a) {
+      cx[a] = 0.5 - 0.5 * cos((2.0 * a + 1.0) * pi / (2.0 * PQ_P));
+      cw[a] = ((a & 1) ? -1.0 : 1.0) * sin((2.0 * a + 1.0) * pi / (2.0 * PQ_P));
+    }
     cudaError_t e = cudaMemcpyToSymbol(c_gl_x, gx, sizeof(gx));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gl_w, gw, sizeof(gw));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_ch_x, cx, sizeof(cx));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_ch_w, cw, sizeof(cw));
     if (e != cudaSuccess) return runtime_record(e);
     have_gl[dev] = true;
   }

@@ -55,3 +55,25 @@ def test_self_convergence_fourier_density(setup):
     a = S.evaluate(xt, sig, alpha=1.0).cpu().numpy()
     b = S.evaluate(xt, sig, alpha=2.0, near_factor=1.5).cpu().numpy()
     assert np.abs(a - b).max() / np.abs(b).max() < 1e-9
+
+
+def test_green_identity_point_source(setup):
+    """Green's representation on the solid torus: for u = 1/|y - x0| with x0 in the hole (harmonic
+    inside the tube), SL[du/dn](x) - DL[u](x) = u(x) for targets inside the tube and 0 outside,
+    with SL = Laplace3D_FxU and DL = Laplace3D_DxU through the near-singular path (near targets
+    at 1e-4 .. 1 panel sizes)."""
+    torch, T, S = setup
+    x0 = np.array([0.0, 0.05, 0.02])
+    Y, Nrm = T.X.reshape(-1, 3), T.N.reshape(-1, 3)
+    d = Y - x0
+    rr = np.linalg.norm(d, axis=1)
+    u = 1.0 / rr
+    dudn = -(d * Nrm).sum(1) / rr ** 3
+    tg = T.targets(3000, seed=15, hmin=1e-4, hmax=1.0)
+    xt = torch.from_numpy(tg["r_trg"]).cuda()
+    sl = S.evaluate(xt, torch.from_numpy(dudn).cuda(), kernel=0, mode="mixed", digits=10).cpu().numpy()
+    dl = S.evaluate(xt, torch.from_numpy(u).cuda(), kernel=1, mode="mixed", digits=10).cpu().numpy()
+    ut = 1.0 / np.linalg.norm(tg["r_trg"] - x0, axis=1)
+    exact = np.where(tg["side"] < 0, ut, 0.0)
+    err = np.abs(sl - dl - exact) / np.abs(ut).max()
+    assert err.max() < 1e-8, (err.max(), tg["h"][err.argmax()], tg["side"][err.argmax()])
