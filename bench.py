@@ -332,6 +332,26 @@ def torus_section(torch, n_eval=1 << 16, n_train=48000, steps=2000, learned=True
     plain = S.evaluate(xt, sig, pairs=pairs, plan=plan)
     res["plain_ms"] = t_plain
     res["plain_far_field_ms"] = _ev_ms(torch, lambda: S.far_field(xt, sig), reps=2)
+    # SetupNear once, ComputeNearInterac per application: stored accurate weights
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    M = S.near_matrix(xt, pairs)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    acc = torch.zeros(n_eval, dtype=torch.float64, device="cuda")
+    apply_ms = _ev_ms(torch, lambda: M.apply(sig, acc), reps=5)
+    hbm = peaks().get("hbm_gbs", 6800.0)
+    # bytes per application: the stored blocks, plus per pair its panel index and order entry, plus
+    # per target its offsets and the read-modify-write of the potential (densities stay in L2)
+    alg = M.nbytes + M.n_pairs * 16 + n_eval * (8 + 16)
+    with_m = S.evaluate(xt, sig, pairs=pairs, plan=plan, matrix=M)
+    res["near_matrix"] = {"setup_s": setup_s, "matrix_bytes": M.nbytes, "apply_ms": apply_ms,
+                          "apply_gb_s": alg / (apply_ms * 1e-3) / 1e9,
+                          "apply_frac_of_measured_hbm": alg / (apply_ms * 1e-3) / 1e9 / hbm,
+                          "evaluate_ms": _ev_ms(torch, lambda: S.evaluate(xt, sig, pairs=pairs, plan=plan, matrix=M),
+                                                reps=2),
+                          "max_rel_diff_vs_adaptive": ((with_m - plain).abs().max() / plain.abs().max()).item()}
+    del M
     if not learned:
         return res
     # learned path

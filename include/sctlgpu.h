@@ -189,6 +189,28 @@ int sctlgpu_panel_near_weights(int kernel, int64_t n_pairs, const int64_t* pair_
                                double alpha, int max_depth, double* w_out, void* stream);
 
 /*
+ * Applies precomputed near-interaction matrices and sums them per target:
+ * replaces BoundaryIntegralOp::ComputeNearInterac's per-block GEMV, ScatterForward
+ * and per-target accumulation (boundary_integral.txx:1311-1381) with one pass.
+ *
+ *   U[t*k1 + c] += sum over j in [trg_dsp[t], trg_dsp[t+1]) of
+ *                  sum_i K[pair_kdsp[p] + c*n + i] * F[elem_nds_dsp[e]*k0 + i],
+ *   p = trg_pair[j] (or j when trg_pair is NULL), e = pair_elem[p],
+ *   n = elem_nds_cnt[e] * k0.
+ *
+ * k0 = SrcDim, k1 = TrgDim (1, 2, 3, 4 or 9).  A pair's block is k1 rows of n entries
+ * (row-major), as one target's rows of the reference's target-major K_near.  Each
+ * target's pairs are summed in the given order by one warp (deterministic).  Indices
+ * out of range skip the pair and set bit 4 of the device status word.  Device
+ * pointers, asynchronous on `stream`; targets without pairs are left untouched.
+ */
+int sctlgpu_near_matrix_apply(int k0, int k1, int64_t n_trg, const int64_t* trg_dsp, int64_t n_near,
+                              const int64_t* trg_pair, int64_t n_pairs, const int64_t* pair_elem,
+                              const int64_t* pair_kdsp, int64_t n_elem, const int64_t* elem_nds_dsp,
+                              const int64_t* elem_nds_cnt, int64_t n_k, const double* K, int64_t n_f,
+                              const double* F, double* U, void* stream);
+
+/*
  * C[M x N] = act(A[M x K] . Bt[N x K]^T + bias) on the tcgen05 tensor cores: A and Bt
  * row-major BF16 (K contiguous, 16-byte aligned), FP32 accumulation in tensor memory,
  * act 0 = none, 1 = GELU (tanh form).  Outputs (any may be NULL, not all): C32 (FP32,

@@ -93,11 +93,18 @@ class PanelSurface:
         blocks = np.stack([live * self.nn, np.full(live.size, self.nn), starts[live], counts[live]], 1)
         return NearPlan(kernel, blocks, self.np * self.nn, nt, mode=mode, digits=digits, trg_index=t)
 
+    def near_matrix(self, r_trg, pairs, kernel=1, alpha=1.0, max_depth=22):
+        """SetupNear's precomputation for repeated applications (e.g. every iteration of an
+        iterative solver): the accurate weights of every (target, panel) pair, see NearMatrix."""
+        return NearMatrix(self, r_trg, pairs, kernel, alpha, max_depth)
+
     def evaluate(self, r_trg, sigma, kernel=1, mode="mixed", digits=10, near_factor=1.0, alpha=1.0, pairs=None,
-                 plan=None):
+                 plan=None, matrix=None):
         """Far field (smooth rule over every node) + near corrections.  The smooth part of the near
         panels is subtracted with a near plan in the far field's arithmetic, so the large
-        near-singular smooth terms cancel exactly as in the reference's FP64 flow."""
+        near-singular smooth terms cancel exactly as in the reference's FP64 flow.  With `matrix`
+        (a NearMatrix of the same pairs) the accurate near part is applied from the stored
+        weights instead of being integrated again."""
         xt = r_trg.reshape(-1).contiguous()
         out = self.far_field(xt, sigma, kernel, mode, digits)
         if pairs is None:
@@ -107,5 +114,54 @@ class PanelSurface:
         negq = (-self.Q).reshape(-1).contiguous()
         plan.execute(xt, self.X.reshape(-1), self.N.reshape(-1), sigma.reshape(-1).contiguous(), out, w_src=negq,
                      accumulate=True)
-        self.near_correction(xt, sigma, pairs, kernel, alpha, out=out, subtract_smooth=False)
+        if matrix is not None:
+            matrix.apply(sigma, out)
+        else:
+            self.near_correction(xt, sigma, pairs, kernel, alpha, out=out, subtract_smooth=False)
+        return out
+
+
+class NearMatrix:
+    """Precomputed near interactions of a panel surface (SetupNear, boundary_integral.txx:927-1241,
+    with the NearInterac weights of every pair) and their application (ComputeNearInterac,
+    :1311-1381) by `sctlgpu_near_matrix_apply`.
+
+    Blocks are stored element-major like the reference's K_near: pair j (panel p_j, target t_j)
+    owns the 100 accurate weights W_j = scale * int K(x_t - y) l_a l_b dA (adaptive quadrature in
+    FP64, `sctlgpu_panel_near_weights`).  The target-major order in which each target's pairs are
+    summed (the reference's near_trg_dsp and scatter order) is a stable sort by target."""
+
+    def __init__(self, S: PanelSurface, r_trg, pairs, kernel=1, alpha=1.0, max_depth=22):
+        xt = r_trg.reshape(-1).contiguous()
+        self.nt = xt.numel() // 3
+        t, p = pairs
+        self.n_pairs, self.nn, self.np = int(t.numel()), S.nn, S.np
+        dev = xt.device
+        self.W = torch.empty(self.n_pairs, S.nn, dtype=torch.float64, device=dev)
+        stream = torch.cuda.current_stream().cuda_stream
+        if self.n_pairs:
+            capi.check(capi.load().sctlgpu_panel_near_weights(
+                kernel, self.n_pairs, t.data_ptr(), p.data_ptr(), self.nt, xt.data_ptr(), S.np, S.X.data_ptr(),
+                float(alpha), int(max_depth), self.W.data_ptr(), stream), "panel_near_weights")
+        self.trg_pair = torch.argsort(t, stable=True).contiguous()
+        counts = torch.bincount(t, minlength=self.nt)
+        self.trg_dsp = torch.cat([torch.zeros(1, dtype=torch.int64, device=dev), counts.cumsum(0)]).contiguous()
+        self.pair_elem = p.contiguous()
+        self.pair_kdsp = (torch.arange(self.n_pairs, dtype=torch.int64, device=dev) * S.nn).contiguous()
+        self.elem_nds_dsp = (torch.arange(S.np, dtype=torch.int64, device=dev) * S.nn).contiguous()
+        self.elem_nds_cnt = torch.full((S.np,), S.nn, dtype=torch.int64, device=dev)
+
+    @property
+    def nbytes(self):
+        """Bytes one application reads from the stored blocks (the HBM-bound part)."""
+        return self.W.numel() * 8
+
+    def apply(self, sigma, out):
+        """out[t] += sum over t's near pairs of W_j . sigma[panel_j]."""
+        f = sigma.reshape(-1).contiguous()
+        capi.check(capi.load().sctlgpu_near_matrix_apply(
+            1, 1, self.nt, self.trg_dsp.data_ptr(), self.n_pairs, self.trg_pair.data_ptr(), self.n_pairs,
+            self.pair_elem.data_ptr(), self.pair_kdsp.data_ptr(), self.np, self.elem_nds_dsp.data_ptr(),
+            self.elem_nds_cnt.data_ptr(), self.W.numel(), self.W.data_ptr(), f.numel(), f.data_ptr(),
+            out.data_ptr(), torch.cuda.current_stream().cuda_stream), "near_matrix_apply")
         return out

@@ -57,6 +57,14 @@ def test_argument_errors_without_gpu():
     assert lib.sctlgpu_kernel_matrix(0, 0, -1, 1, p, 1, p, None, None, 0, None) == capi.ERR_NULL_POINTER
     # zero targets is a no-op that needs no device
     assert lib.sctlgpu_eval(0, 0, -1, 0, None, 5, p, None, p, None, 0, None) == capi.OK
+    # near-matrix application: TrgDim must be 1, 2, 3, 4 or 9; pointers checked before any launch
+    na = lambda k1, nt, tdsp, n_near=0, tp=None: lib.sctlgpu_near_matrix_apply(  # noqa: E731
+        1, k1, nt, tdsp, n_near, tp, 1, p, p, 1, p, p, 6, p, 6, p, p, None)
+    assert na(5, 1, p) == capi.ERR_INVALID_SIZE
+    assert na(1, -1, p) == capi.ERR_INVALID_SIZE
+    assert na(1, 1, p, n_near=2) == capi.ERR_INVALID_SIZE  # identity order needs n_near <= n_pairs
+    assert na(1, 1, None) == capi.ERR_NULL_POINTER
+    assert na(1, 0, None) == capi.OK
     for code in (0, -1, -2, -3, -4, -5, -6, -7, -8, -9):
         assert lib.sctlgpu_strerror(code)
 

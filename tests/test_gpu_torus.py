@@ -77,3 +77,62 @@ def test_green_identity_point_source(setup):
     exact = np.where(tg["side"] < 0, ut, 0.0)
     err = np.abs(sl - dl - exact) / np.abs(ut).max()
     assert err.max() < 1e-8, (err.max(), tg["h"][err.argmax()], tg["side"][err.argmax()])
+
+
+def test_near_matrix_path_equals_adaptive_path(setup):
+    """SetupNear once (stored accurate weights), ComputeNearInterac per application: the
+    stored-matrix evaluation equals the matrix-free adaptive one, and keeps Gauss's law."""
+    torch, T, S = setup
+    tg = T.targets(3000, seed=16, hmin=1e-4, hmax=1.0)
+    xt = torch.from_numpy(tg["r_trg"]).cuda().reshape(-1).contiguous()
+    pairs = S.near_pairs(xt, 1.0)
+    plan = S.smooth_subtraction_plan(3000, pairs)
+    M = S.near_matrix(xt, pairs)
+    sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()
+    a = S.evaluate(xt, sig, pairs=pairs, plan=plan, matrix=M)
+    b = S.evaluate(xt, sig, pairs=pairs, plan=plan)
+    assert ((a - b).abs().max() / b.abs().max()).item() < 1e-12
+    one = torch.ones_like(sig)
+    v = S.evaluate(xt, one, pairs=pairs, plan=plan, matrix=M).cpu().numpy()
+    assert np.abs(v - np.where(tg["side"] < 0, -1.0, 0.0)).max() < 1e-8
+    from sctl_gb300 import capi
+    assert capi.load().sctlgpu_device_status(None) == capi.OK
+
+
+@pytest.mark.parametrize("k0,k1", [(1, 1), (3, 3), (1, 9), (4, 3)])
+def test_near_matrix_apply_general_layout(cuda, k0, k1):
+    """sctlgpu_near_matrix_apply against a numpy restatement of ComputeNearInterac: uneven
+    elements (1..7 nodes), element-major blocks, a permuted target-major order, targets without
+    pairs (left untouched), accumulation into U."""
+    torch = cuda
+    from sctl_gb300 import capi
+    rng = np.random.default_rng(k0 * 10 + k1)
+    n_elem, nt, n_pairs = 37, 53, 300
+    cnt = rng.integers(1, 8, n_elem)
+    dsp = np.concatenate([[0], np.cumsum(cnt)[:-1]])
+    F = rng.standard_normal(int(cnt.sum()) * k0)
+    pe = rng.integers(0, n_elem, n_pairs)
+    pt = rng.integers(0, nt - 5, n_pairs)          # the last 5 targets have no pairs
+    sizes = cnt[pe] * k0 * k1
+    kdsp = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+    K = rng.standard_normal(int(sizes.sum()))
+    order = np.argsort(pt, kind="stable")
+    tdsp = np.concatenate([[0], np.cumsum(np.bincount(pt, minlength=nt))])
+    U0 = rng.standard_normal(nt * k1)
+    want = U0.copy()
+    for j in range(n_pairs):
+        n = cnt[pe[j]] * k0
+        blk = K[kdsp[j]:kdsp[j] + n * k1].reshape(k1, n)
+        want[pt[j] * k1:(pt[j] + 1) * k1] += blk @ F[dsp[pe[j]] * k0:dsp[pe[j]] * k0 + n]
+    d = lambda a, dt=torch.int64: torch.from_numpy(np.ascontiguousarray(a)).to(dt).cuda()  # noqa: E731
+    g = {"tdsp": d(tdsp), "ord": d(order), "pe": d(pe), "kd": d(kdsp), "ed": d(dsp), "ec": d(cnt),
+         "K": d(K, torch.float64), "F": d(F, torch.float64), "U": d(U0, torch.float64)}
+    rc = capi.load().sctlgpu_near_matrix_apply(k0, k1, nt, g["tdsp"].data_ptr(), n_pairs, g["ord"].data_ptr(),
+                                               n_pairs, g["pe"].data_ptr(), g["kd"].data_ptr(), n_elem,
+                                               g["ed"].data_ptr(), g["ec"].data_ptr(), K.size, g["K"].data_ptr(),
+                                               F.size, g["F"].data_ptr(), g["U"].data_ptr(), None)
+    assert rc == capi.OK
+    got = g["U"].cpu().numpy()
+    np.testing.assert_allclose(got, want, rtol=1e-13, atol=1e-13)
+    np.testing.assert_array_equal(got[(nt - 5) * k1:], U0[(nt - 5) * k1:])
+    assert capi.load().sctlgpu_device_status(None) == capi.OK
