@@ -189,6 +189,36 @@ int sctlgpu_panel_near_weights(int kernel, int64_t n_pairs, const int64_t* pair_
                                double alpha, int max_depth, double* w_out, void* stream);
 
 /*
+ * Near lists (replaces BuildNearList, boundary_integral.txx:50-522, single rank).
+ * Target t is near element e when some node s of e (nodes elem_nds_dsp[e] ..
+ * elem_nds_dsp[e] + elem_nds_cnt[e] - 1 of r_src) has |x_t - x_s|^2 < src_radius[s]^2,
+ * the reference's test.  The handle holds, on the device:
+ *   near_elem_cnt/dsp[n_elem]   near targets per element (element-major list sorted by
+ *                               (element, target));
+ *   near_trg_idx[n_near]        the element-major list's target indices (the reference
+ *                               returns their coordinates, Xtrg_near = r_trg[near_trg_idx]);
+ *   near_scatter_index[n_near]  for entry i of the target-major order, its position in
+ *                               the element-major list (the reference's ScatterForward
+ *                               index; entries of one target in element order);
+ *   near_trg_cnt/dsp[nt]        per target, its entries in the target-major order (dsp 0
+ *                               where cnt is 0, as the reference);
+ *   near_trg_elem[n_near]       the target-major order's element indices.
+ * Inputs are host arrays, or device arrays with SCTLGPU_DEVICE_PTRS.  The build
+ * synchronises `stream`.  Nodes with a negative or non-finite radius, and elements with
+ * invalid node ranges, are skipped and set bit 4 of the device status word.
+ */
+typedef struct sctlgpu_near_list_s* sctlgpu_near_list;
+int sctlgpu_near_list_build(sctlgpu_near_list* out, int64_t nt, const double* r_trg, int64_t n_elem,
+                            const int64_t* elem_nds_cnt, const int64_t* elem_nds_dsp, int64_t ns,
+                            const double* r_src, const double* src_radius, unsigned flags, void* stream);
+int sctlgpu_near_list_sizes(sctlgpu_near_list list, int64_t* n_near, int64_t* nt, int64_t* n_elem);
+/* Copies the arrays out (host or device destinations; NULL skips one), synchronously. */
+int sctlgpu_near_list_get(sctlgpu_near_list list, int64_t* near_elem_cnt, int64_t* near_elem_dsp,
+                          int64_t* near_trg_idx, int64_t* near_scatter_index, int64_t* near_trg_cnt,
+                          int64_t* near_trg_dsp, int64_t* near_trg_elem, void* stream);
+int sctlgpu_near_list_destroy(sctlgpu_near_list list);
+
+/*
  * Applies precomputed near-interaction matrices and sums them per target:
  * replaces BoundaryIntegralOp::ComputeNearInterac's per-block GEMV, ScatterForward
  * and per-target accumulation (boundary_integral.txx:1311-1381) with one pass.

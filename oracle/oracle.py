@@ -55,6 +55,8 @@ def lib():
         L.oracle_scale_factor.argtypes = [i32]
         L.oracle_scale_factor.restype = ctypes.c_double
         L.oracle_max_threads.restype = i32
+        L.oracle_near_pairs.argtypes = [i64, vp, i64, vp, vp, vp, vp, i64, vp, vp]
+        L.oracle_near_pairs.restype = i64
         _lib = L
     return _lib
 
@@ -76,6 +78,10 @@ def ref():
         L.ref_kernel_matrix.restype = i32
         L.ref_vec_len.argtypes = [i32]
         L.ref_vec_len.restype = i32
+        L.ref_near_list.argtypes = [i64, vp, i64, vp, vp, i64, vp, vp]
+        L.ref_near_list.restype = i64
+        L.ref_near_list_get.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.ref_near_list_get.restype = i32
         _ref = L
     return _ref
 
@@ -184,3 +190,56 @@ def max_rel(a, b):
     a = np.asarray(a, np.float64).ravel()
     b = np.asarray(b, np.float64).ravel()
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+# ------------------------------------------------------------------ near lists
+def near_pairs(r_trg, elem_nds_cnt, elem_nds_dsp, r_src, src_radius):
+    """Element-major (element, target) near pairs by brute force (sctl_oracle.c oracle_near_pairs)."""
+    xt = np.ascontiguousarray(r_trg, np.float64).reshape(-1)
+    xs = np.ascontiguousarray(r_src, np.float64).reshape(-1)
+    rad = np.ascontiguousarray(src_radius, np.float64)
+    cnt = np.ascontiguousarray(elem_nds_cnt, np.int64)
+    dsp = np.ascontiguousarray(elem_nds_dsp, np.int64)
+    L = lib()
+    args = (xt.size // 3, _ptr(xt), cnt.size, _ptr(cnt), _ptr(dsp), _ptr(xs), _ptr(rad))
+    n = L.oracle_near_pairs(*args, 0, None, None)
+    pe, pt = np.empty(max(n, 1), np.int64), np.empty(max(n, 1), np.int64)
+    m = L.oracle_near_pairs(*args, n, pe.ctypes.data, pt.ctypes.data)
+    assert m == n
+    return pe[:n], pt[:n]
+
+
+def near_list_from_pairs(pe, pt, nt, n_elem):
+    """BuildNearList's outputs (boundary_integral.txx:423-521) from element-major sorted pairs:
+    near_elem_cnt/dsp, near_trg_idx, near_scatter_index (target-major order, ties in element
+    order), near_trg_cnt/dsp (dsp 0 where cnt is 0)."""
+    elem_cnt = np.bincount(pe, minlength=n_elem).astype(np.int64)
+    elem_dsp = np.concatenate([[0], np.cumsum(elem_cnt)[:-1]]).astype(np.int64)
+    scatter = np.argsort(pt, kind="stable").astype(np.int64)
+    trg_cnt = np.bincount(pt, minlength=nt).astype(np.int64)
+    trg_dsp = np.concatenate([[0], np.cumsum(trg_cnt)[:-1]]).astype(np.int64)
+    trg_dsp[trg_cnt == 0] = 0
+    return dict(near_elem_cnt=elem_cnt, near_elem_dsp=elem_dsp[:n_elem], near_trg_idx=pt.astype(np.int64),
+                near_scatter_index=scatter, near_trg_cnt=trg_cnt, near_trg_dsp=trg_dsp)
+
+
+def ref_near_list(r_trg, elem_nds_cnt, elem_nds_dsp, r_src, src_radius):
+    """The reference's own BuildNearList<double,3> on one rank (oracle/_ref)."""
+    xt = np.ascontiguousarray(r_trg, np.float64).reshape(-1)
+    xs = np.ascontiguousarray(r_src, np.float64).reshape(-1)
+    rad = np.ascontiguousarray(src_radius, np.float64)
+    cnt = np.ascontiguousarray(elem_nds_cnt, np.int64)
+    dsp = np.ascontiguousarray(elem_nds_dsp, np.int64)
+    nt, ne = xt.size // 3, cnt.size
+    L = ref()
+    n = L.ref_near_list(nt, _ptr(xt), ne, _ptr(cnt), _ptr(dsp), xs.size // 3, _ptr(xs), _ptr(rad))
+    out = dict(xtrg_near=np.zeros(max(n, 1) * 3), near_elem_cnt=np.zeros(max(ne, 1), np.int64),
+               near_elem_dsp=np.zeros(max(ne, 1), np.int64), near_scatter_index=np.zeros(max(n, 1), np.int64),
+               near_trg_cnt=np.zeros(max(nt, 1), np.int64), near_trg_dsp=np.zeros(max(nt, 1), np.int64))
+    L.ref_near_list_get(*(out[k].ctypes.data for k in ("xtrg_near", "near_elem_cnt", "near_elem_dsp",
+                                                       "near_scatter_index", "near_trg_cnt", "near_trg_dsp")))
+    out["xtrg_near"] = out["xtrg_near"][:n * 3].reshape(-1, 3)
+    out["near_elem_cnt"], out["near_elem_dsp"] = out["near_elem_cnt"][:ne], out["near_elem_dsp"][:ne]
+    out["near_scatter_index"] = out["near_scatter_index"][:n]
+    out["near_trg_cnt"], out["near_trg_dsp"] = out["near_trg_cnt"][:nt], out["near_trg_dsp"][:nt]
+    return out

@@ -90,6 +90,40 @@ int ref_kernel_matrix(int kernel, int is_double, int64_t nt, const void* r_trg, 
   return kmat_dispatch<float>(kernel, nt, (const float*)r_trg, ns, (const float*)r_src, (const float*)n_src, (float*)M);
 }
 
+// BuildNearList<double,3> (boundary_integral.txx:50-522) on one rank
+// (Comm::Self), as BoundaryIntegralOp::SetupNear calls it (:948).  The first
+// call computes and keeps the result and returns the number of near entries;
+// ref_near_list_get copies it out.
+static sctl::Vector<double> g_xtrg_near, g_xn_near;
+static sctl::Vector<sctl::Long> g_elem_cnt, g_elem_dsp, g_scatter, g_trg_cnt, g_trg_dsp;
+
+int64_t ref_near_list(int64_t nt, const double* r_trg, int64_t n_elem, const int64_t* elem_nds_cnt,
+                      const int64_t* elem_nds_dsp, int64_t ns, const double* r_src, const double* src_radius) {
+  sctl::Vector<double> Xt(nt * 3, sctl::Ptr2Itr<double>((double*)r_trg, nt * 3), false);
+  sctl::Vector<double> Xn;
+  sctl::Vector<double> Xs(ns * 3, sctl::Ptr2Itr<double>((double*)r_src, ns * 3), false);
+  sctl::Vector<double> rad(ns, sctl::Ptr2Itr<double>((double*)src_radius, ns), false);
+  sctl::Vector<sctl::Long> cnt(n_elem), dsp(n_elem);
+  for (int64_t i = 0; i < n_elem; ++i) {
+    cnt[i] = elem_nds_cnt[i];
+    dsp[i] = elem_nds_dsp[i];
+  }
+  sctl::BuildNearList<double, 3>(g_xtrg_near, g_xn_near, g_elem_cnt, g_elem_dsp, g_scatter, g_trg_cnt, g_trg_dsp, Xt,
+                                 Xn, Xs, rad, cnt, dsp, sctl::Comm::Self());
+  return (int64_t)g_scatter.Dim();
+}
+
+int ref_near_list_get(double* xtrg_near, int64_t* elem_cnt, int64_t* elem_dsp, int64_t* scatter, int64_t* trg_cnt,
+                      int64_t* trg_dsp) {
+  for (sctl::Long i = 0; i < g_xtrg_near.Dim(); ++i) xtrg_near[i] = g_xtrg_near[i];
+  for (sctl::Long i = 0; i < g_elem_cnt.Dim(); ++i) elem_cnt[i] = g_elem_cnt[i];
+  for (sctl::Long i = 0; i < g_elem_dsp.Dim(); ++i) elem_dsp[i] = g_elem_dsp[i];
+  for (sctl::Long i = 0; i < g_scatter.Dim(); ++i) scatter[i] = g_scatter[i];
+  for (sctl::Long i = 0; i < g_trg_cnt.Dim(); ++i) trg_cnt[i] = g_trg_cnt[i];
+  for (sctl::Long i = 0; i < g_trg_dsp.Dim(); ++i) trg_dsp[i] = g_trg_dsp[i];
+  return 0;
+}
+
 // Which SIMD path the reference was compiled for (DefaultVecLen, vec.txx:27-42).
 int ref_vec_len(int is_double) {
   return is_double ? (int)sctl::DefaultVecLen<double>() : (int)sctl::DefaultVecLen<float>();

@@ -215,3 +215,66 @@ DEFINE_EVAL(oracle_eval_ld, double, long double, sqrtl)
 
 DEFINE_KMAT(oracle_kernel_matrix_f64, double, sqrt)
 DEFINE_KMAT(oracle_kernel_matrix_f32, float, sqrtf)
+
+/* ---------------------------------------------------------------- near lists */
+static int near_test(const double* xt, const double* xs, double r) {
+  /* node_dist2: dist2 += dX * dX over x, y, z, then dist2 < rad * rad */
+  volatile double d2 = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    volatile double dx = xs[k] - xt[k];
+    volatile double sq = dx * dx;
+    d2 = d2 + sq;
+  }
+  volatile double r2 = r * r;
+  return d2 < r2;
+}
+
+int64_t oracle_near_pairs(int64_t nt, const double* r_trg, int64_t n_elem, const int64_t* elem_nds_cnt,
+                          const int64_t* elem_nds_dsp, const double* r_src, const double* src_radius, int64_t cap,
+                          int64_t* pair_elem, int64_t* pair_trg) {
+  int64_t* cnt = (int64_t*)calloc((size_t)(n_elem > 0 ? n_elem : 1), sizeof(int64_t));
+  if (!cnt) return -1;
+#pragma omp parallel for schedule(dynamic)
+  for (int64_t e = 0; e < n_elem; ++e) {
+    int64_t c = 0;
+    for (int64_t t = 0; t < nt; ++t)
+      for (int64_t j = 0; j < elem_nds_cnt[e]; ++j) {
+        const int64_t s = elem_nds_dsp[e] + j;
+        if (near_test(r_trg + t * 3, r_src + s * 3, src_radius[s])) {
+          ++c;
+          break;
+        }
+      }
+    cnt[e] = c;
+  }
+  int64_t total = 0;
+  for (int64_t e = 0; e < n_elem; ++e) total += cnt[e];
+  if (pair_elem && pair_trg) {
+    if (total > cap) {
+      free(cnt);
+      return -1;
+    }
+    int64_t off = 0;
+    for (int64_t e = 0; e < n_elem; ++e) {
+      const int64_t o = off;
+      off += cnt[e];
+      cnt[e] = o;
+    }
+#pragma omp parallel for schedule(dynamic)
+    for (int64_t e = 0; e < n_elem; ++e) {
+      int64_t k = cnt[e];
+      for (int64_t t = 0; t < nt; ++t)
+        for (int64_t j = 0; j < elem_nds_cnt[e]; ++j) {
+          const int64_t s = elem_nds_dsp[e] + j;
+          if (near_test(r_trg + t * 3, r_src + s * 3, src_radius[s])) {
+            pair_elem[k] = e;
+            pair_trg[k] = t;
+            ++k;
+            break;
+          }
+        }
+    }
+  }
+  free(cnt);
+  return total;
+}

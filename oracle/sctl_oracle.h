@@ -74,6 +74,17 @@ double oracle_rsqrt_newton(double x, double y0, int steps);
 /* Number of OpenMP threads an oracle call with nthreads <= 0 would use. */
 int oracle_max_threads(void);
 
+/* BuildNearList's near test (boundary_integral.txx:50-522; the test itself is
+ * node_dist2(src, trg) < rad * rad at :394): target t is near element e when
+ * some node s of e has |x_s - x_t|^2 < rad_s^2, squared distance summed
+ * x, y, z in FP64 without contraction.  Brute force over all (element, target)
+ * pairs, written element-major sorted by (element, target): pair_elem[k],
+ * pair_trg[k].  With pair arrays NULL only counts.  Returns the number of
+ * pairs, or -1 when more than `cap`. */
+int64_t oracle_near_pairs(int64_t nt, const double* r_trg, int64_t n_elem, const int64_t* elem_nds_cnt,
+                          const int64_t* elem_nds_dsp, const double* r_src, const double* src_radius, int64_t cap,
+                          int64_t* pair_elem, int64_t* pair_trg);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,6 +58,10 @@ SIGNATURES = {
     "sctlgpu_mlp_forward_dot": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp]),
     "sctlgpu_mlp_train_step": (_i, [_vp, _i, _vp, _vp, ctypes.c_float, _vp, _vp]),
     "sctlgpu_mlp_gradients": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
+    "sctlgpu_near_list_build": (_i, [ctypes.POINTER(_vp), _i64, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _u, _vp]),
+    "sctlgpu_near_list_sizes": (_i, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "sctlgpu_near_list_get": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "sctlgpu_near_list_destroy": (_i, [_vp]),
     "sctlgpu_near_matrix_apply": (_i, [_i, _i, _i64, _vp, _i64, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp,
                                       _vp, _vp]),
     "sctlgpu_tc_gemm_bf16": (_i, [_i, _i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _vp]),

@@ -48,6 +48,19 @@ class PanelSurface:
         order = torch.argsort(p * xt.shape[0] + t)
         return t[order].contiguous(), p[order].contiguous()
 
+    def near_pairs_grid(self, r_trg, near_factor=1.0):
+        """(target, panel) pairs from the GPU near list (`NearList`, BuildNearList's test): a
+        target is near a panel when it is within near_factor * size_P of one of the panel's
+        nodes.  Sorted by panel, then target."""
+        from .nearlist import NearList
+        xt = r_trg.reshape(-1).contiguous()
+        cnt = torch.full((self.np,), self.nn, dtype=torch.int64, device=xt.device)
+        dsp = torch.arange(self.np, dtype=torch.int64, device=xt.device) * self.nn
+        rad = (near_factor * self.size).repeat_interleave(self.nn).contiguous()
+        a = NearList(xt, cnt, dsp, self.X.reshape(-1).contiguous(), rad).arrays()
+        p = torch.repeat_interleave(torch.arange(self.np, device=xt.device), a["near_elem_cnt"])
+        return a["near_trg_idx"].contiguous(), p.to(torch.int64).contiguous()
+
     # ------------------------------------------------------------ far field
     def far_field(self, r_trg, sigma, kernel=1, mode="mixed", digits=10, out=None):
         xt = r_trg.reshape(-1)

@@ -105,3 +105,42 @@ def near_blocks(n_blocks=4096, kernel=1, seed=0, panel=False, diameter=0.1):
     return dict(r_trg=np.concatenate(xt), r_src=np.concatenate(xs),
                 n_src=np.concatenate(xn) if NORMAL_DIM[kernel] else np.zeros((0, 3)),
                 v_src=np.concatenate(f), blocks=blocks)
+
+
+def near_list_case(kind: str, seed: int = 0):
+    """Inputs of a near-list build (BuildNearList's Xtrg, Xsrc, src_radius, elem_nds_cnt/dsp):
+
+    * "clusters": 300 elements of 0..11 nodes scattered (sigma 0.02) around uniform centres in
+      the unit cube, node radii U(0.01, 0.06), 4000 uniform targets (some elements empty);
+    * "torus": the 64 x 32-panel torus (10 x 10 Chebyshev nodes per panel), node radius = its
+      panel's size, 1500 targets at 1e-4..1 panel sizes off the surface;
+    * "many": 70,000 single-node elements in the unit cube, radii U(0, 0.01), 20,000 targets
+      (element ids need three 8-bit radix passes)."""
+    rng = np.random.default_rng(seed)
+    if kind == "clusters":
+        ne = 300
+        cnt = rng.integers(0, 12, ne)
+        cnt[[5, 17, 299]] = 0
+        cen = rng.uniform(0, 1, (ne, 3))
+        xs = np.repeat(cen, cnt, 0) + rng.normal(0, 0.02, (int(cnt.sum()), 3))
+        rad = rng.uniform(0.01, 0.06, int(cnt.sum()))
+        xt = rng.uniform(0, 1, (4000, 3))
+    elif kind == "torus":
+        from .torus import Torus
+        T = Torus(seed=seed)
+        cnt = np.full(T.np, T.p * T.p)
+        xs = T.X.reshape(-1, 3)
+        rad = np.repeat(T.size, T.p * T.p)
+        xt = T.targets(1500, seed=seed + 1)["r_trg"]
+    elif kind == "many":
+        ne = 70000
+        cnt = np.ones(ne, np.int64)
+        xs = rng.uniform(0, 1, (ne, 3))
+        rad = rng.uniform(0, 0.01, ne)
+        xt = rng.uniform(0, 1, (20000, 3))
+    else:
+        raise ValueError(kind)
+    cnt = cnt.astype(np.int64)
+    dsp = np.concatenate([[0], np.cumsum(cnt)[:-1]]).astype(np.int64)
+    return dict(r_trg=np.ascontiguousarray(xt, np.float64), r_src=np.ascontiguousarray(xs, np.float64),
+                src_radius=np.ascontiguousarray(rad, np.float64), elem_nds_cnt=cnt, elem_nds_dsp=dsp)
