@@ -34,13 +34,28 @@ extern "C" {
 
 #define SCTLGPU_VERSION 1
 
-/* Kernel ids: the micro-kernels of kernel_functions.hpp (aliases at :677-678, :669-670). */
+/* Kernel ids: the micro-kernels of kernel_functions.hpp (aliases at :669-684).  Ids 0-3 are
+ * the hot path (every mode, near plans, the allocation-free entry); ids 4-15 run Eval and
+ * KernelMatrix in FP64 and FP32 (SCTLGPU_MIXED runs them on the FP64 path). */
 enum sctlgpu_kernel {
-  SCTLGPU_LAPLACE3D_FXU = 0, /* sctl::Laplace3D_FxU  kernel_functions.hpp:32-59   */
-  SCTLGPU_LAPLACE3D_DXU = 1, /* sctl::Laplace3D_DxU  kernel_functions.hpp:61-79   */
-  SCTLGPU_STOKES3D_FXU = 2,  /* sctl::Stokes3D_FxU   kernel_functions.hpp:125-178 */
-  SCTLGPU_STOKES3D_DXU = 3   /* sctl::Stokes3D_DxU   kernel_functions.hpp:180-218 */
+  SCTLGPU_LAPLACE3D_FXU = 0,        /* sctl::Laplace3D_FxU        kernel_functions.hpp:32-59   */
+  SCTLGPU_LAPLACE3D_DXU = 1,        /* sctl::Laplace3D_DxU        kernel_functions.hpp:61-79   */
+  SCTLGPU_STOKES3D_FXU = 2,         /* sctl::Stokes3D_FxU         kernel_functions.hpp:125-178 */
+  SCTLGPU_STOKES3D_DXU = 3,         /* sctl::Stokes3D_DxU         kernel_functions.hpp:180-218 */
+  SCTLGPU_LAPLACE3D_FXDU = 4,       /* sctl::Laplace3D_FxdU       kernel_functions.hpp:81-123  */
+  SCTLGPU_LAPLACE3D_FXD2U = 5,      /* sctl::Laplace3D_Fxd2U      kernel_functions.hpp:366-390 */
+  SCTLGPU_LAPLACE3D_DXDU = 6,       /* sctl::Laplace3D_DxdU       kernel_functions.hpp:392-414 */
+  SCTLGPU_BIOTSAVART3D_FXU = 7,     /* sctl::BiotSavart3D_FxU     kernel_functions.hpp:416-449 */
+  SCTLGPU_BIOTSAVART3D_FXDU = 8,    /* sctl::BiotSavart3D_FxdU    kernel_functions.hpp:451-483 */
+  SCTLGPU_HELMHOLTZ3D_FXU = 9,      /* sctl::Helmholtz3D_FxU      kernel_functions.hpp:491-527 (needs ctx) */
+  SCTLGPU_HELMHOLTZ3D_DXU = 10,     /* sctl::Helmholtz3D_DxU      kernel_functions.hpp:529-571 (needs ctx) */
+  SCTLGPU_HELMHOLTZ3D_FXDU = 11,    /* sctl::Helmholtz3D_FxdU     kernel_functions.hpp:573-620 (needs ctx) */
+  SCTLGPU_HELMHOLTZDIFF3D_FXDU = 12,/* sctl::HelmholtzDiff3D_FxdU kernel_functions.hpp:627-659 (needs ctx) */
+  SCTLGPU_STOKES3D_FXT = 13,        /* sctl::Stokes3D_FxT         kernel_functions.hpp:220-262 */
+  SCTLGPU_STOKES3D_FSXU = 14,       /* sctl::Stokes3D_FSxU        kernel_functions.hpp:264-323 */
+  SCTLGPU_STOKES3D_FXUP = 15        /* sctl::Stokes3D_FxUP        kernel_functions.hpp:325-364 */
 };
+#define SCTLGPU_NUM_KERNELS 16
 
 /* Arithmetic modes. */
 enum sctlgpu_mode {
@@ -74,7 +89,7 @@ enum sctlgpu_status {
  */
 int sctlgpu_kernel_dims(int kernel, int* coord_dim, int* normal_dim, int* src_dim, int* trg_dim);
 
-/* uKerScaleFactor<double>() of the kernel (kernel_functions.hpp:40,69,133,188). */
+/* uKerScaleFactor<double>() of the kernel (kernel_functions.hpp:40,69,88,133,188,...). */
 double sctlgpu_scale_factor(int kernel);
 
 /*
@@ -100,6 +115,23 @@ int sctlgpu_kernel_matrix(int kernel, int mode, int digits,
                           int64_t nt, const void* r_trg,
                           int64_t ns, const void* r_src, const void* n_src,
                           void* M, unsigned flags, void* stream);
+
+/*
+ * sctlgpu_eval / sctlgpu_kernel_matrix with the kernel's context, as the reference's
+ * GenericKernel::SetCtxPtr (generic-kernel.hpp:79) provides it to uKerMatrix /
+ * uKerApply: for the Helmholtz kernels (ids 9-12) `ctx` points to the wavenumber, a
+ * host value of the call's real type (double, or float for SCTLGPU_F32); other
+ * kernels ignore it.  The entries without ctx refuse the Helmholtz kernels
+ * (SCTLGPU_ERR_NULL_POINTER).
+ */
+int sctlgpu_eval_ctx(int kernel, int mode, int digits,
+                     int64_t nt, const void* r_trg,
+                     int64_t ns, const void* r_src, const void* n_src, const void* v_src,
+                     void* v_trg, unsigned flags, const void* ctx, void* stream);
+int sctlgpu_kernel_matrix_ctx(int kernel, int mode, int digits,
+                              int64_t nt, const void* r_trg,
+                              int64_t ns, const void* r_src, const void* n_src,
+                              void* M, unsigned flags, const void* ctx, void* stream);
 
 /*
  * Batched near-field direct sums: many independent blocks of uneven sizes in one

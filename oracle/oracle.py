@@ -21,9 +21,15 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "libsctl_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libsctlref.so")
 
-KERNELS = {"Laplace3D_FxU": 0, "Laplace3D_DxU": 1, "Stokes3D_FxU": 2, "Stokes3D_DxU": 3}
-# (NormalDim, SrcDim, TrgDim), generic-kernel.txx:48-62 with kernel_functions.hpp
-DIMS = {0: (0, 1, 1), 1: (3, 1, 1), 2: (0, 3, 3), 3: (3, 3, 3)}
+KERNELS = {"Laplace3D_FxU": 0, "Laplace3D_DxU": 1, "Stokes3D_FxU": 2, "Stokes3D_DxU": 3,
+           "Laplace3D_FxdU": 4, "Laplace3D_Fxd2U": 5, "Laplace3D_DxdU": 6, "BiotSavart3D_FxU": 7,
+           "BiotSavart3D_FxdU": 8, "Helmholtz3D_FxU": 9, "Helmholtz3D_DxU": 10, "Helmholtz3D_FxdU": 11,
+           "HelmholtzDiff3D_FxdU": 12, "Stokes3D_FxT": 13, "Stokes3D_FSxU": 14, "Stokes3D_FxUP": 15}
+# (NormalDim, SrcDim, TrgDim), generic-kernel.hpp:54-74 with kernel_functions.hpp
+DIMS = {0: (0, 1, 1), 1: (3, 1, 1), 2: (0, 3, 3), 3: (3, 3, 3), 4: (0, 1, 3), 5: (0, 1, 9), 6: (3, 1, 3),
+        7: (0, 3, 3), 8: (0, 3, 9), 9: (0, 2, 2), 10: (3, 2, 2), 11: (0, 2, 6), 12: (0, 2, 6), 13: (0, 3, 9),
+        14: (0, 4, 3), 15: (0, 3, 4)}
+HELMHOLTZ = (9, 10, 11, 12)
 
 _lib = None
 _ref = None
@@ -55,6 +61,12 @@ def lib():
         L.oracle_scale_factor.argtypes = [i32]
         L.oracle_scale_factor.restype = ctypes.c_double
         L.oracle_max_threads.restype = i32
+        L.oracle_xscale.argtypes = [i32]
+        L.oracle_xscale.restype = ctypes.c_double
+        L.oracle_xeval.argtypes = [i32, i32, i64, vp, i64, vp, vp, vp, ctypes.c_double, vp, i32]
+        L.oracle_xeval.restype = i32
+        L.oracle_xkmat.argtypes = [i32, i32, i64, vp, i64, vp, vp, ctypes.c_double, vp, i32]
+        L.oracle_xkmat.restype = i32
         L.oracle_near_pairs.argtypes = [i64, vp, i64, vp, vp, vp, vp, i64, vp, vp]
         L.oracle_near_pairs.restype = i64
         _lib = L
@@ -78,6 +90,8 @@ def ref():
         L.ref_kernel_matrix.restype = i32
         L.ref_vec_len.argtypes = [i32]
         L.ref_vec_len.restype = i32
+        L.ref_set_ctx.argtypes = [ctypes.c_double]
+        L.ref_set_ctx.restype = None
         L.ref_near_list.argtypes = [i64, vp, i64, vp, vp, i64, vp, vp]
         L.ref_near_list.restype = i64
         L.ref_near_list_get.argtypes = [vp, vp, vp, vp, vp, vp]
@@ -94,9 +108,12 @@ def _ptr(a):
     return None if a is None or a.size == 0 else a.ctypes.data
 
 
-def eval(kernel, r_trg, r_src, n_src, v_src, v_trg=None, precision="f64", nthreads=0):
-    """v_trg (+)= scale * sum_s K f (the reference's Eval); returns v_trg."""
+def eval(kernel, r_trg, r_src, n_src, v_src, v_trg=None, precision="f64", nthreads=0, mu=0.0):
+    """v_trg (+)= scale * sum_s K f (the reference's Eval); returns v_trg.  mu: the Helmholtz
+    wavenumber (kernel ids 9-12)."""
     k = _kid(kernel)
+    if k >= 4:
+        return _xeval(k, r_trg, r_src, n_src, v_src, v_trg, precision, nthreads, mu)
     nd, sd, td = DIMS[k]
     dt = np.float32 if precision == "f32" else np.float64
     r_trg = np.ascontiguousarray(r_trg, dt).reshape(-1)
@@ -113,8 +130,39 @@ def eval(kernel, r_trg, r_src, n_src, v_src, v_trg=None, precision="f64", nthrea
     return v_trg
 
 
-def kernel_matrix(kernel, r_trg, r_src, n_src, precision="f64", nthreads=0):
+def _xeval(k, r_trg, r_src, n_src, v_src, v_trg, precision, nthreads, mu):
+    nd, sd, td = DIMS[k]
+    dt = np.float32 if precision == "f32" else np.float64
+    r_trg = np.ascontiguousarray(r_trg, dt).reshape(-1)
+    r_src = np.ascontiguousarray(r_src, dt).reshape(-1)
+    v_src = np.ascontiguousarray(v_src, dt).reshape(-1)
+    n_src = np.ascontiguousarray(n_src, dt).reshape(-1) if nd else None
+    nt, ns = r_trg.size // 3, r_src.size // 3
+    if v_trg is None:
+        v_trg = np.zeros(nt * td, dt)
+    prec = {"f64": 0, "f32": 1, "ld": 2}[precision]
+    rc = lib().oracle_xeval(k, prec, nt, _ptr(r_trg), ns, _ptr(r_src), _ptr(n_src), _ptr(v_src), float(mu),
+                            _ptr(v_trg), nthreads)
+    if rc:
+        raise RuntimeError(f"oracle eval failed: {rc}")
+    return v_trg
+
+
+def kernel_matrix(kernel, r_trg, r_src, n_src, precision="f64", nthreads=0, mu=0.0):
     k = _kid(kernel)
+    if k >= 4:
+        nd, sd, td = DIMS[k]
+        dt = np.float32 if precision == "f32" else np.float64
+        r_trg = np.ascontiguousarray(r_trg, dt).reshape(-1)
+        r_src = np.ascontiguousarray(r_src, dt).reshape(-1)
+        n_src = np.ascontiguousarray(n_src, dt).reshape(-1) if nd else None
+        nt, ns = r_trg.size // 3, r_src.size // 3
+        M = np.zeros((ns * sd, nt * td), dt)
+        rc = lib().oracle_xkmat(k, int(precision == "f32"), nt, _ptr(r_trg), ns, _ptr(r_src), _ptr(n_src),
+                                float(mu), _ptr(M), nthreads)
+        if rc:
+            raise RuntimeError(f"oracle kernel_matrix failed: {rc}")
+        return M
     nd, sd, td = DIMS[k]
     dt = np.float32 if precision == "f32" else np.float64
     r_trg = np.ascontiguousarray(r_trg, dt).reshape(-1)
@@ -129,7 +177,7 @@ def kernel_matrix(kernel, r_trg, r_src, n_src, precision="f64", nthreads=0):
     return M
 
 
-def ref_eval(kernel, r_trg, r_src, n_src, v_src, digits=-1, precision="f64", omp=True, v_trg=None):
+def ref_eval(kernel, r_trg, r_src, n_src, v_src, digits=-1, precision="f64", omp=True, v_trg=None, mu=0.0):
     """The reference's own GenericKernel::Eval<Real,omp>(..., digits, self)."""
     k = _kid(kernel)
     nd, sd, td = DIMS[k]
@@ -141,6 +189,7 @@ def ref_eval(kernel, r_trg, r_src, n_src, v_src, digits=-1, precision="f64", omp
     nt, ns = r_trg.size // 3, r_src.size // 3
     if v_trg is None:
         v_trg = np.zeros(nt * td, dt)
+    ref().ref_set_ctx(float(mu))
     rc = ref().ref_eval(k, int(dt == np.float64), int(digits), nt, _ptr(r_trg), ns, _ptr(r_src), _ptr(n_src),
                         _ptr(v_src), _ptr(v_trg), int(omp))
     if rc:
@@ -148,7 +197,7 @@ def ref_eval(kernel, r_trg, r_src, n_src, v_src, digits=-1, precision="f64", omp
     return v_trg
 
 
-def ref_kernel_matrix(kernel, r_trg, r_src, n_src, precision="f64"):
+def ref_kernel_matrix(kernel, r_trg, r_src, n_src, precision="f64", mu=0.0):
     k = _kid(kernel)
     nd, sd, td = DIMS[k]
     dt = np.float32 if precision == "f32" else np.float64
@@ -157,6 +206,7 @@ def ref_kernel_matrix(kernel, r_trg, r_src, n_src, precision="f64"):
     n_src = np.ascontiguousarray(n_src, dt).reshape(-1) if nd else None
     nt, ns = r_trg.size // 3, r_src.size // 3
     M = np.zeros((ns * sd, nt * td), dt)
+    ref().ref_set_ctx(float(mu))
     rc = ref().ref_kernel_matrix(k, int(dt == np.float64), nt, _ptr(r_trg), ns, _ptr(r_src), _ptr(n_src), _ptr(M))
     if rc:
         raise RuntimeError(f"reference kernel_matrix failed: {rc}")
@@ -172,7 +222,8 @@ def rsqrt_newton(x, y0, steps):
 
 
 def scale_factor(kernel):
-    return lib().oracle_scale_factor(_kid(kernel))
+    k = _kid(kernel)
+    return lib().oracle_xscale(k) if k >= 4 else lib().oracle_scale_factor(k)
 
 
 def max_threads():

@@ -9,15 +9,28 @@
 //   (generic-kernel.hpp:124, called by boundary_integral.txx:1197,1211).
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 
 #include "sctl.hpp"
 
 namespace {
 
+// The Helmholtz kernels read their wavenumber through the kernel object's ctx
+// pointer (GenericKernel::SetCtxPtr, generic-kernel.hpp:79), as a value of the
+// evaluation's real type.
+double g_ctx_d = 0.0;
+float g_ctx_f = 0.0f;
+
+template <class Real>
+void* ctx_for() {
+  return std::is_same<Real, float>::value ? (void*)&g_ctx_f : (void*)&g_ctx_d;
+}
+
 template <class Kernel, class Real>
 int eval_impl(int digits, int64_t nt, const Real* r_trg, int64_t ns, const Real* r_src, const Real* n_src,
               const Real* v_src, Real* v_trg, int omp) {
   Kernel ker;
+  ker.SetCtxPtr(ctx_for<Real>());
   const sctl::Long nd = Kernel::NormalDim(), sd = Kernel::SrcDim(), td = Kernel::TrgDim();
   sctl::Vector<Real> Xt(nt * 3, sctl::Ptr2Itr<Real>((Real*)r_trg, nt * 3), false);
   sctl::Vector<Real> Xs(ns * 3, sctl::Ptr2Itr<Real>((Real*)r_src, ns * 3), false);
@@ -36,6 +49,7 @@ int eval_impl(int digits, int64_t nt, const Real* r_trg, int64_t ns, const Real*
 template <class Kernel, class Real>
 int kmat_impl(int64_t nt, const Real* r_trg, int64_t ns, const Real* r_src, const Real* n_src, Real* M) {
   Kernel ker;
+  ker.SetCtxPtr(ctx_for<Real>());
   const sctl::Long nd = Kernel::NormalDim(), sd = Kernel::SrcDim(), td = Kernel::TrgDim();
   sctl::Vector<Real> Xt(nt * 3, sctl::Ptr2Itr<Real>((Real*)r_trg, nt * 3), false);
   sctl::Vector<Real> Xs(ns * 3, sctl::Ptr2Itr<Real>((Real*)r_src, ns * 3), false);
@@ -54,6 +68,18 @@ int eval_dispatch(int kernel, int digits, int64_t nt, const Real* r_trg, int64_t
     case 1: return eval_impl<sctl::Laplace3D_DxU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
     case 2: return eval_impl<sctl::Stokes3D_FxU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
     case 3: return eval_impl<sctl::Stokes3D_DxU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    case 4: return eval_impl<sctl::Laplace3D_FxdU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    case 5: return eval_impl<sctl::Laplace3D_Fxd2U, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    case 6: return eval_impl<sctl::Laplace3D_DxdU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    case 7: return eval_impl<sctl::BiotSavart3D_FxU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    case 8: return eval_impl<sctl::BiotSavart3D_FxdU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    case 9: return eval_impl<sctl::Helmholtz3D_FxU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    case 10: return eval_impl<sctl::Helmholtz3D_DxU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    case 11: return eval_impl<sctl::Helmholtz3D_FxdU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    case 12: return eval_impl<sctl::HelmholtzDiff3D_FxdU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    case 13: return eval_impl<sctl::Stokes3D_FxT, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    case 14: return eval_impl<sctl::Stokes3D_FSxU, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
+    case 15: return eval_impl<sctl::Stokes3D_FxUP, Real>(digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, omp);
     default: return -1;
   }
 }
@@ -65,6 +91,18 @@ int kmat_dispatch(int kernel, int64_t nt, const Real* r_trg, int64_t ns, const R
     case 1: return kmat_impl<sctl::Laplace3D_DxU, Real>(nt, r_trg, ns, r_src, n_src, M);
     case 2: return kmat_impl<sctl::Stokes3D_FxU, Real>(nt, r_trg, ns, r_src, n_src, M);
     case 3: return kmat_impl<sctl::Stokes3D_DxU, Real>(nt, r_trg, ns, r_src, n_src, M);
+    case 4: return kmat_impl<sctl::Laplace3D_FxdU, Real>(nt, r_trg, ns, r_src, n_src, M);
+    case 5: return kmat_impl<sctl::Laplace3D_Fxd2U, Real>(nt, r_trg, ns, r_src, n_src, M);
+    case 6: return kmat_impl<sctl::Laplace3D_DxdU, Real>(nt, r_trg, ns, r_src, n_src, M);
+    case 7: return kmat_impl<sctl::BiotSavart3D_FxU, Real>(nt, r_trg, ns, r_src, n_src, M);
+    case 8: return kmat_impl<sctl::BiotSavart3D_FxdU, Real>(nt, r_trg, ns, r_src, n_src, M);
+    case 9: return kmat_impl<sctl::Helmholtz3D_FxU, Real>(nt, r_trg, ns, r_src, n_src, M);
+    case 10: return kmat_impl<sctl::Helmholtz3D_DxU, Real>(nt, r_trg, ns, r_src, n_src, M);
+    case 11: return kmat_impl<sctl::Helmholtz3D_FxdU, Real>(nt, r_trg, ns, r_src, n_src, M);
+    case 12: return kmat_impl<sctl::HelmholtzDiff3D_FxdU, Real>(nt, r_trg, ns, r_src, n_src, M);
+    case 13: return kmat_impl<sctl::Stokes3D_FxT, Real>(nt, r_trg, ns, r_src, n_src, M);
+    case 14: return kmat_impl<sctl::Stokes3D_FSxU, Real>(nt, r_trg, ns, r_src, n_src, M);
+    case 15: return kmat_impl<sctl::Stokes3D_FxUP, Real>(nt, r_trg, ns, r_src, n_src, M);
     default: return -1;
   }
 }
@@ -122,6 +160,12 @@ int ref_near_list_get(double* xtrg_near, int64_t* elem_cnt, int64_t* elem_dsp, i
   for (sctl::Long i = 0; i < g_trg_cnt.Dim(); ++i) trg_cnt[i] = g_trg_cnt[i];
   for (sctl::Long i = 0; i < g_trg_dsp.Dim(); ++i) trg_dsp[i] = g_trg_dsp[i];
   return 0;
+}
+
+// Wavenumber seen by the Helmholtz kernels (both real types).
+void ref_set_ctx(double mu) {
+  g_ctx_d = mu;
+  g_ctx_f = (float)mu;
 }
 
 // Which SIMD path the reference was compiled for (DefaultVecLen, vec.txx:27-42).

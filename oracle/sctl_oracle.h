@@ -81,6 +81,17 @@ int oracle_max_threads(void);
  * pairs, written element-major sorted by (element, target): pair_elem[k],
  * pair_trg[k].  With pair arrays NULL only counts.  Returns the number of
  * pairs, or -1 when more than `cap`. */
+/* The other twelve micro-kernels (ids 4-15, kernel_functions.hpp:81-659): Eval and
+ * KernelMatrix from each kernel's uKerMatrix, exact 1/sqrt, in float, double or long
+ * double; mu is the Helmholtz wavenumber (ids 9-12).  Same layouts as above. */
+int oracle_xdims(int kernel, int* nd, int* sd, int* td);
+double oracle_xscale(int kernel);
+int oracle_xeval(int kernel, int precision /* 0 double, 1 float, 2 long double */, int64_t nt, const void* r_trg,
+                 int64_t ns, const void* r_src, const void* n_src, const void* v_src, double mu, void* v_trg,
+                 int nthreads);
+int oracle_xkmat(int kernel, int precision /* 0 double, 1 float */, int64_t nt, const void* r_trg, int64_t ns,
+                 const void* r_src, const void* n_src, double mu, void* M, int nthreads);
+
 int64_t oracle_near_pairs(int64_t nt, const double* r_trg, int64_t n_elem, const int64_t* elem_nds_cnt,
                           const int64_t* elem_nds_dsp, const double* r_src, const double* src_radius, int64_t cap,
                           int64_t* pair_elem, int64_t* pair_trg);

@@ -1,8 +1,12 @@
 """sctl_gb300 -- GB300 (sm_103a) drop-in for SCTL's particle-kernel hot path.
 
 Python mirror of sctl::GenericKernel (include/sctl/generic-kernel.hpp) for the
-four kernels of include/sctl/kernel_functions.hpp that BoundaryIntegralOp and
-ParticleFMM evaluate: Laplace3D_FxU, Laplace3D_DxU, Stokes3D_FxU, Stokes3D_DxU.
+micro-kernels of include/sctl/kernel_functions.hpp: the four that
+BoundaryIntegralOp and ParticleFMM evaluate on the hot path (Laplace3D_FxU,
+Laplace3D_DxU, Stokes3D_FxU, Stokes3D_DxU; every precision mode) and the other
+twelve (Laplace gradient / Hessian, BiotSavart, Helmholtz, Stokes traction /
+source-sink / pressure; FP64 and FP32).  The Helmholtz kernels need their
+wavenumber, the reference's ctx_ptr: GenericKernel("Helmholtz3D_FxU", ctx=k).
 All compute runs in libsctlgpu.so through its C ABI (include/sctlgpu.h).
 
 Arguments follow the reference: flat array-of-structures coordinates
@@ -19,8 +23,10 @@ import numpy as np
 from . import capi
 from .capi import F32, F64, MIXED, SctlGpuError, kernel_dims, launch_count  # noqa: F401
 
-__all__ = ["GenericKernel", "Laplace3D_FxU", "Laplace3D_DxU", "Stokes3D_FxU", "Stokes3D_DxU",
-           "SctlGpuError", "F64", "F32", "MIXED", "eval_device", "kernel_matrix_device"]
+__all__ = ["GenericKernel", "Laplace3D_FxU", "Laplace3D_DxU", "Stokes3D_FxU", "Stokes3D_DxU", "Laplace3D_FxdU",
+           "Laplace3D_Fxd2U", "Laplace3D_DxdU", "BiotSavart3D_FxU", "BiotSavart3D_FxdU", "Stokes3D_FxT",
+           "Stokes3D_FSxU", "Stokes3D_FxUP", "SctlGpuError", "F64", "F32", "MIXED", "eval_device",
+           "kernel_matrix_device"]
 
 
 def _is_torch(x):
@@ -37,26 +43,43 @@ def _real(mode):
     return np.float32 if mode == F32 else np.float64
 
 
+def _ctx_arg(mode, ctx):
+    """Host value of the call's real type holding the kernel context (or None)."""
+    import ctypes
+    if ctx is None:
+        return None, None
+    v = ctypes.c_float(ctx) if mode == F32 else ctypes.c_double(ctx)
+    return v, ctypes.addressof(v)
+
+
 def eval_device(kernel: int, mode: int, digits: int, nt: int, r_trg: int, ns: int, r_src: int, n_src: int,
-                v_src: int, v_trg: int, accumulate: bool, stream: int = 0) -> None:
+                v_src: int, v_trg: int, accumulate: bool, stream: int = 0, ctx=None) -> None:
     """Raw device-pointer entry (asynchronous on `stream`)."""
     flags = capi.DEVICE_PTRS | (capi.ACCUMULATE if accumulate else 0)
-    capi.check(capi.load().sctlgpu_eval(kernel, mode, digits, nt, r_trg, ns, r_src, n_src or None, v_src, v_trg,
-                                        flags, stream or None), "sctlgpu_eval")
+    keep, cp = _ctx_arg(mode, ctx)
+    capi.check(capi.load().sctlgpu_eval_ctx(kernel, mode, digits, nt, r_trg, ns, r_src, n_src or None, v_src, v_trg,
+                                            flags, cp, stream or None), "sctlgpu_eval")
 
 
 def kernel_matrix_device(kernel: int, mode: int, digits: int, nt: int, r_trg: int, ns: int, r_src: int, n_src: int,
-                         M: int, stream: int = 0) -> None:
-    capi.check(capi.load().sctlgpu_kernel_matrix(kernel, mode, digits, nt, r_trg, ns, r_src, n_src or None, M,
-                                                 capi.DEVICE_PTRS, stream or None), "sctlgpu_kernel_matrix")
+                         M: int, stream: int = 0, ctx=None) -> None:
+    keep, cp = _ctx_arg(mode, ctx)
+    capi.check(capi.load().sctlgpu_kernel_matrix_ctx(kernel, mode, digits, nt, r_trg, ns, r_src, n_src or None, M,
+                                                     capi.DEVICE_PTRS, cp, stream or None), "sctlgpu_kernel_matrix")
 
 
 class GenericKernel:
     """One micro-kernel behind the GenericKernel API."""
 
-    def __init__(self, name: str):
+    def __init__(self, name: str, ctx=None):
         self.name = name
         self.kernel_id = capi.KERNEL_IDS[name]
+        self.ctx = ctx  # the reference's ctx_ptr target (Helmholtz wavenumber)
+
+    def SetCtx(self, ctx):
+        """GenericKernel::SetCtxPtr (generic-kernel.hpp:79), by value."""
+        self.ctx = ctx
+        return self
 
     # dims are constexpr in the reference (generic-kernel.hpp:54-74)
     def CoordDim(self) -> int:
@@ -102,8 +125,10 @@ class GenericKernel:
         else:
             out = np.zeros(nt * td, dt)
         ptr = lambda a: None if a is None or a.size == 0 else a.ctypes.data  # noqa: E731
-        rc = capi.load().sctlgpu_eval(self.kernel_id, m, int(digits), nt, ptr(r_trg), ns, ptr(r_src), ptr(n_src),
-                                      ptr(v_src), ptr(out), capi.ACCUMULATE if accumulate else 0, None)
+        keep, cp = _ctx_arg(m, self.ctx)
+        rc = capi.load().sctlgpu_eval_ctx(self.kernel_id, m, int(digits), nt, ptr(r_trg), ns, ptr(r_src),
+                                          ptr(n_src), ptr(v_src), ptr(out), capi.ACCUMULATE if accumulate else 0, cp,
+                                          None)
         capi.check(rc, f"{self.name}.Eval")
         if accumulate and out is not v_trg:
             np.copyto(np.asarray(v_trg).reshape(-1), out.reshape(np.asarray(v_trg).reshape(-1).shape))
@@ -130,7 +155,7 @@ class GenericKernel:
         stream = torch.cuda.current_stream(r_trg.device).cuda_stream
         eval_device(self.kernel_id, m, int(digits), nt, r_trg.data_ptr(), ns, r_src.data_ptr(),
                     n_src.data_ptr() if n_src is not None else 0, v_src.data_ptr(), out.data_ptr(), accumulate,
-                    stream)
+                    stream, self.ctx)
         return out
 
     def KernelMatrix(self, Xt, Xs, Xn, digits: int = -1, mode=None):
@@ -148,7 +173,7 @@ class GenericKernel:
             M = torch.empty((ns * sd, nt * td), dtype=tdt, device=Xt.device)
             kernel_matrix_device(self.kernel_id, m, int(digits), nt, Xt.data_ptr(), ns, Xs.data_ptr(),
                                  Xn.data_ptr() if Xn is not None else 0, M.data_ptr(),
-                                 torch.cuda.current_stream(Xt.device).cuda_stream)
+                                 torch.cuda.current_stream(Xt.device).cuda_stream, self.ctx)
             return M
         m = _mode_for(np.asarray(Xt).dtype, mode)
         dt = _real(m)
@@ -158,17 +183,28 @@ class GenericKernel:
         nt, ns = Xt.size // 3, Xs.size // 3
         M = np.zeros((ns * sd, nt * td), dt)
         ptr = lambda a: None if a is None or a.size == 0 else a.ctypes.data  # noqa: E731
-        rc = capi.load().sctlgpu_kernel_matrix(self.kernel_id, m, int(digits), nt, ptr(Xt), ns, ptr(Xs), ptr(Xn),
-                                               ptr(M), 0, None)
+        keep, cp = _ctx_arg(m, self.ctx)
+        rc = capi.load().sctlgpu_kernel_matrix_ctx(self.kernel_id, m, int(digits), nt, ptr(Xt), ns, ptr(Xs),
+                                                   ptr(Xn), ptr(M), 0, cp, None)
         capi.check(rc, f"{self.name}.KernelMatrix")
         return M
 
 
-# (NormalDim, SrcDim, TrgDim) of each kernel id -- generic-kernel.txx:48-62.
+# (NormalDim, SrcDim, TrgDim) of each kernel id -- generic-kernel.hpp:54-74 with kernel_functions.hpp.
 _DIMS = {capi.LAPLACE3D_FXU: (0, 1, 1), capi.LAPLACE3D_DXU: (3, 1, 1),
-         capi.STOKES3D_FXU: (0, 3, 3), capi.STOKES3D_DXU: (3, 3, 3)}
+         capi.STOKES3D_FXU: (0, 3, 3), capi.STOKES3D_DXU: (3, 3, 3),
+         4: (0, 1, 3), 5: (0, 1, 9), 6: (3, 1, 3), 7: (0, 3, 3), 8: (0, 3, 9), 9: (0, 2, 2), 10: (3, 2, 2),
+         11: (0, 2, 6), 12: (0, 2, 6), 13: (0, 3, 9), 14: (0, 4, 3), 15: (0, 3, 4)}
 
 Laplace3D_FxU = GenericKernel("Laplace3D_FxU")
 Laplace3D_DxU = GenericKernel("Laplace3D_DxU")
 Stokes3D_FxU = GenericKernel("Stokes3D_FxU")
 Stokes3D_DxU = GenericKernel("Stokes3D_DxU")
+Laplace3D_FxdU = GenericKernel("Laplace3D_FxdU")
+Laplace3D_Fxd2U = GenericKernel("Laplace3D_Fxd2U")
+Laplace3D_DxdU = GenericKernel("Laplace3D_DxdU")
+BiotSavart3D_FxU = GenericKernel("BiotSavart3D_FxU")
+BiotSavart3D_FxdU = GenericKernel("BiotSavart3D_FxdU")
+Stokes3D_FxT = GenericKernel("Stokes3D_FxT")
+Stokes3D_FSxU = GenericKernel("Stokes3D_FSxU")
+Stokes3D_FxUP = GenericKernel("Stokes3D_FxUP")

@@ -21,7 +21,11 @@ ERR_INVALID_KERNEL, ERR_INVALID_MODE, ERR_INVALID_SIZE, ERR_NULL_POINTER = -1, -
 ERR_CUDA, ERR_NO_DEVICE, ERR_DEVICE_TIMEOUT, ERR_INVALID_ARGUMENT, ERR_TOO_LARGE = -5, -6, -7, -8, -9
 
 KERNEL_IDS = {"Laplace3D_FxU": LAPLACE3D_FXU, "Laplace3D_DxU": LAPLACE3D_DXU,
-              "Stokes3D_FxU": STOKES3D_FXU, "Stokes3D_DxU": STOKES3D_DXU}
+              "Stokes3D_FxU": STOKES3D_FXU, "Stokes3D_DxU": STOKES3D_DXU,
+              "Laplace3D_FxdU": 4, "Laplace3D_Fxd2U": 5, "Laplace3D_DxdU": 6, "BiotSavart3D_FxU": 7,
+              "BiotSavart3D_FxdU": 8, "Helmholtz3D_FxU": 9, "Helmholtz3D_DxU": 10, "Helmholtz3D_FxdU": 11,
+              "HelmholtzDiff3D_FxdU": 12, "Stokes3D_FxT": 13, "Stokes3D_FSxU": 14, "Stokes3D_FxUP": 15}
+HELMHOLTZ_IDS = (9, 10, 11, 12)
 MODE_IDS = {"f64": F64, "f32": F32, "mixed": MIXED}
 
 # Every symbol include/*.h declares, with its ctypes signature.
@@ -32,6 +36,8 @@ SIGNATURES = {
     "sctlgpu_scale_factor": (_d, [_i]),
     "sctlgpu_eval": (_i, [_i, _i, _i, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _u, _vp]),
     "sctlgpu_kernel_matrix": (_i, [_i, _i, _i, _i64, _vp, _i64, _vp, _vp, _vp, _u, _vp]),
+    "sctlgpu_eval_ctx": (_i, [_i, _i, _i, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _u, _vp, _vp]),
+    "sctlgpu_kernel_matrix_ctx": (_i, [_i, _i, _i, _i64, _vp, _i64, _vp, _vp, _vp, _u, _vp, _vp]),
     "sctlgpu_strerror": (_cp, [_i]),
     "sctlgpu_last_cuda_error": (_cp, []),
     "sctlgpu_device_status": (_i, [_vp]),

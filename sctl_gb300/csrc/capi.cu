@@ -105,8 +105,31 @@ int dims(int kernel, int* nd, int* sd, int* td) {
     case SCTLGPU_LAPLACE3D_DXU: *nd = 3; *sd = 1; *td = 1; return SCTLGPU_OK;
     case SCTLGPU_STOKES3D_FXU: *nd = 0; *sd = 3; *td = 3; return SCTLGPU_OK;
     case SCTLGPU_STOKES3D_DXU: *nd = 3; *sd = 3; *td = 3; return SCTLGPU_OK;
+    case SCTLGPU_LAPLACE3D_FXDU: *nd = 0; *sd = 1; *td = 3; return SCTLGPU_OK;
+    case SCTLGPU_LAPLACE3D_FXD2U: *nd = 0; *sd = 1; *td = 9; return SCTLGPU_OK;
+    case SCTLGPU_LAPLACE3D_DXDU: *nd = 3; *sd = 1; *td = 3; return SCTLGPU_OK;
+    case SCTLGPU_BIOTSAVART3D_FXU: *nd = 0; *sd = 3; *td = 3; return SCTLGPU_OK;
+    case SCTLGPU_BIOTSAVART3D_FXDU: *nd = 0; *sd = 3; *td = 9; return SCTLGPU_OK;
+    case SCTLGPU_HELMHOLTZ3D_FXU: *nd = 0; *sd = 2; *td = 2; return SCTLGPU_OK;
+    case SCTLGPU_HELMHOLTZ3D_DXU: *nd = 3; *sd = 2; *td = 2; return SCTLGPU_OK;
+    case SCTLGPU_HELMHOLTZ3D_FXDU: *nd = 0; *sd = 2; *td = 6; return SCTLGPU_OK;
+    case SCTLGPU_HELMHOLTZDIFF3D_FXDU: *nd = 0; *sd = 2; *td = 6; return SCTLGPU_OK;
+    case SCTLGPU_STOKES3D_FXT: *nd = 0; *sd = 3; *td = 9; return SCTLGPU_OK;
+    case SCTLGPU_STOKES3D_FSXU: *nd = 0; *sd = 4; *td = 3; return SCTLGPU_OK;
+    case SCTLGPU_STOKES3D_FXUP: *nd = 0; *sd = 3; *td = 4; return SCTLGPU_OK;
     default: return SCTLGPU_ERR_INVALID_KERNEL;
   }
+}
+
+bool is_helmholtz(int kernel) { return kernel >= SCTLGPU_HELMHOLTZ3D_FXU && kernel <= SCTLGPU_HELMHOLTZDIFF3D_FXDU; }
+
+// The context value a kernel reads (ctx points to a value of the call's real type).
+int read_ctx(int kernel, int mode, const void* ctx, double* out) {
+  *out = 0.0;
+  if (!is_helmholtz(kernel)) return SCTLGPU_OK;
+  if (!ctx) return SCTLGPU_ERR_NULL_POINTER;
+  *out = mode == SCTLGPU_F32 ? (double)*(const float*)ctx : *(const double*)ctx;
+  return SCTLGPU_OK;
 }
 
 // digits as the reference reads it: -1 (and >= 16) -> floor(SigBits*log10 2) (vec.txx:376).
@@ -164,6 +187,10 @@ int steps_for(int mode, int d) {
 }
 
 cudaError_t run_eval(EvalCall& c, int mode, int d) {
+  if (c.kernel > SCTLGPU_STOKES3D_DXU) {  // FP64 arithmetic also for SCTLGPU_MIXED
+    if (mode == SCTLGPU_F32) return eval_ext_f32(c, steps_for(mode, d));
+    return eval_ext_f64(c, steps_for(SCTLGPU_F64, d));
+  }
   const int n = steps_for(mode, d);
   if (mode == SCTLGPU_F64) return eval_f64(c, n);
   if (mode == SCTLGPU_F32) return eval_f32(c, n);
@@ -173,6 +200,10 @@ cudaError_t run_eval(EvalCall& c, int mode, int d) {
 }
 
 cudaError_t run_kmat(KmatCall& c, int mode, int d) {
+  if (c.kernel > SCTLGPU_STOKES3D_DXU) {
+    if (mode == SCTLGPU_F32) return kmat_ext_f32(c, steps_for(mode, d));
+    return kmat_ext_f64(c, steps_for(SCTLGPU_F64, d));
+  }
   const int n = steps_for(mode, d);
   if (mode == SCTLGPU_F64) return kmat_f64(c, n);
   if (mode == SCTLGPU_F32) return kmat_f32(c, n);
@@ -213,6 +244,18 @@ double sctlgpu_scale_factor(int kernel) {
     case SCTLGPU_LAPLACE3D_DXU: return 1.0 / (4.0 * pi);
     case SCTLGPU_STOKES3D_FXU: return 1.0 / (8.0 * pi);
     case SCTLGPU_STOKES3D_DXU: return 3.0 / (4.0 * pi);
+    case SCTLGPU_LAPLACE3D_FXDU: return -1.0 / (4.0 * pi);        /* kernel_functions.hpp:88-90 */
+    case SCTLGPU_LAPLACE3D_FXD2U: return 1.0 / (4.0 * pi);        /* :374-376 */
+    case SCTLGPU_LAPLACE3D_DXDU: return 1.0 / (4.0 * pi);         /* :400-402 */
+    case SCTLGPU_BIOTSAVART3D_FXU: return 1.0 / (4.0 * pi);       /* :424-426 */
+    case SCTLGPU_BIOTSAVART3D_FXDU: return -1.0 / (4.0 * pi);     /* :459-461 */
+    case SCTLGPU_HELMHOLTZ3D_FXU: return 1.0 / (4.0 * pi);        /* :499-501 */
+    case SCTLGPU_HELMHOLTZ3D_DXU: return -1.0 / (4.0 * pi);       /* :537-539 */
+    case SCTLGPU_HELMHOLTZ3D_FXDU: return 1.0 / (4.0 * pi);       /* :581-583 */
+    case SCTLGPU_HELMHOLTZDIFF3D_FXDU: return 1.0 / (4.0 * pi);   /* :635-637 */
+    case SCTLGPU_STOKES3D_FXT: return -3.0 / (4.0 * pi);          /* :228-230 */
+    case SCTLGPU_STOKES3D_FSXU: return 1.0 / (8.0 * pi);          /* :272-274 */
+    case SCTLGPU_STOKES3D_FXUP: return 1.0 / (8.0 * pi);          /* :333-335 */
     default: return 0.0;
   }
 }
@@ -224,9 +267,17 @@ int sctlgpu_newton_steps(int mode, int digits) {
 
 int sctlgpu_eval(int kernel, int mode, int digits, int64_t nt, const void* r_trg, int64_t ns, const void* r_src,
                  const void* n_src, const void* v_src, void* v_trg, unsigned flags, void* stream) {
+  return sctlgpu_eval_ctx(kernel, mode, digits, nt, r_trg, ns, r_src, n_src, v_src, v_trg, flags, nullptr, stream);
+}
+
+int sctlgpu_eval_ctx(int kernel, int mode, int digits, int64_t nt, const void* r_trg, int64_t ns, const void* r_src,
+                     const void* n_src, const void* v_src, void* v_trg, unsigned flags, const void* ctx,
+                     void* stream) {
   int nd, sd, td;
   int rc = check_common(kernel, mode, nt, r_trg, ns, r_src, n_src, &nd, &sd, &td);
   if (rc) return rc;
+  double ctx_value;
+  if ((rc = read_ctx(kernel, mode, ctx, &ctx_value))) return rc;
   if ((ns > 0 && !v_src) || (nt > 0 && !v_trg)) return SCTLGPU_ERR_NULL_POINTER;
   if (nt == 0) return SCTLGPU_OK;
   const bool dev_ptrs = flags & SCTLGPU_DEVICE_PTRS;
@@ -250,6 +301,7 @@ int sctlgpu_eval(int kernel, int mode, int digits, int64_t nt, const void* r_trg
 
   EvalCall c;
   c.kernel = kernel;
+  c.ctx = ctx_value;
   c.nt = nt;
   c.ns = ns;
   c.accumulate = accumulate;
@@ -300,9 +352,17 @@ int sctlgpu_eval(int kernel, int mode, int digits, int64_t nt, const void* r_trg
 
 int sctlgpu_kernel_matrix(int kernel, int mode, int digits, int64_t nt, const void* r_trg, int64_t ns,
                           const void* r_src, const void* n_src, void* M, unsigned flags, void* stream) {
+  return sctlgpu_kernel_matrix_ctx(kernel, mode, digits, nt, r_trg, ns, r_src, n_src, M, flags, nullptr, stream);
+}
+
+int sctlgpu_kernel_matrix_ctx(int kernel, int mode, int digits, int64_t nt, const void* r_trg, int64_t ns,
+                              const void* r_src, const void* n_src, void* M, unsigned flags, const void* ctx,
+                              void* stream) {
   int nd, sd, td;
   int rc = check_common(kernel, mode, nt, r_trg, ns, r_src, n_src, &nd, &sd, &td);
   if (rc) return rc;
+  double ctx_value;
+  if ((rc = read_ctx(kernel, mode, ctx, &ctx_value))) return rc;
   if (nt == 0 || ns == 0) return SCTLGPU_OK;
   if (!M) return SCTLGPU_ERR_NULL_POINTER;
   if (overflows(nt * td, ns * sd)) return SCTLGPU_ERR_INVALID_SIZE;
@@ -317,6 +377,7 @@ int sctlgpu_kernel_matrix(int kernel, int mode, int digits, int64_t nt, const vo
 
   KmatCall c;
   c.kernel = kernel;
+  c.ctx = ctx_value;
   c.nt = nt;
   c.ns = ns;
   c.stream = st;

@@ -32,6 +32,7 @@ struct EvalCall {
   unsigned* status;  // device status word
   int sms;           // multiprocessors of the current device
   Timing* timing;    // may be null
+  double ctx = 0.0;  // kernel context (Helmholtz wavenumber)
 };
 
 struct KmatCall {
@@ -44,6 +45,7 @@ struct KmatCall {
   cudaStream_t stream;
   int sms;
   Timing* timing;
+  double ctx = 0.0;  // kernel context (Helmholtz wavenumber)
 };
 
 // Direct sums.  `newton` is the number of Newton steps after the hardware seed.
@@ -51,6 +53,12 @@ cudaError_t eval_f64(const EvalCall& c, int newton);
 cudaError_t eval_f32(const EvalCall& c, int newton);
 cudaError_t eval_mixed_lo(const EvalCall& c, int newton);  // FP32 arithmetic on split coordinates
 cudaError_t eval_mixed_df(const EvalCall& c);              // double-float arithmetic
+
+// Kernel ids 4-15 (ext.cuh): FP64 or FP32 arithmetic.
+cudaError_t eval_ext_f64(const EvalCall& c, int newton);
+cudaError_t eval_ext_f32(const EvalCall& c, int newton);
+cudaError_t kmat_ext_f64(const KmatCall& c, int newton);
+cudaError_t kmat_ext_f32(const KmatCall& c, int newton);
 
 // Kernel matrices.
 cudaError_t kmat_f64(const KmatCall& c, int newton);

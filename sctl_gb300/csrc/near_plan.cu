@@ -289,6 +289,7 @@ extern "C" {
 
 int sctlgpu_near_autotune(int kernel, int mode, int digits, int* splits) {
   int nd, sd, td;
+  if (kernel < 0 || kernel > SCTLGPU_STOKES3D_DXU) return SCTLGPU_ERR_INVALID_KERNEL;  // the four hot-path kernels
   if (sctlgpu_kernel_dims(kernel, nullptr, &nd, &sd, &td) != SCTLGPU_OK) return SCTLGPU_ERR_INVALID_KERNEL;
   if (mode != SCTLGPU_F64 && mode != SCTLGPU_F32 && mode != SCTLGPU_MIXED) return SCTLGPU_ERR_INVALID_MODE;
   int dev;
@@ -319,6 +320,7 @@ int sctlgpu_near_plan_create_indexed(sctlgpu_near_plan* out, int kernel, int mod
   if (!out) return SCTLGPU_ERR_NULL_POINTER;
   *out = nullptr;
   int nd, sd, td;
+  if (kernel < 0 || kernel > SCTLGPU_STOKES3D_DXU) return SCTLGPU_ERR_INVALID_KERNEL;  // the four hot-path kernels
   if (sctlgpu_kernel_dims(kernel, nullptr, &nd, &sd, &td) != SCTLGPU_OK) return SCTLGPU_ERR_INVALID_KERNEL;
   if (mode != SCTLGPU_F64 && mode != SCTLGPU_F32 && mode != SCTLGPU_MIXED) return SCTLGPU_ERR_INVALID_MODE;
   if (nblk < 0 || ns < 0 || nt < 0 || nblk > INT32_MAX) return SCTLGPU_ERR_INVALID_SIZE;

@@ -144,6 +144,7 @@ extern "C" int sctlgpu_eval_mixed_noalloc(int kernel, int digits, int64_t nt, co
                                           const double* r_src, const double* n_src, const double* v_src,
                                           double* v_trg, unsigned flags, void* stream) {
   int nd = 0, sd = 0, td = 0;
+  if (kernel < 0 || kernel > SCTLGPU_STOKES3D_DXU) return SCTLGPU_ERR_INVALID_KERNEL;  // the four hot-path kernels
   if (sctlgpu_kernel_dims(kernel, nullptr, &nd, &sd, &td) != SCTLGPU_OK) return SCTLGPU_ERR_INVALID_KERNEL;
   if (nt < 0 || ns < 0 || nt > ((int64_t)1 << 40) || ns > ((int64_t)1 << 40)) return SCTLGPU_ERR_INVALID_SIZE;
   if (flags & ~(unsigned)(SCTLGPU_ACCUMULATE | SCTLGPU_DEVICE_PTRS)) return SCTLGPU_ERR_INVALID_ARGUMENT;

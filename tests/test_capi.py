@@ -39,22 +39,31 @@ def test_kernel_dims_match_reference():
     assert capi.kernel_dims(2) == (3, 0, 3, 3)
     assert capi.kernel_dims(3) == (3, 3, 3, 3)
     with pytest.raises(S.SctlGpuError):
-        capi.kernel_dims(7)
+        capi.kernel_dims(16)
     for k, v in ((0, 1 / (4 * np.pi)), (1, 1 / (4 * np.pi)), (2, 1 / (8 * np.pi)), (3, 3 / (4 * np.pi))):
         assert abs(capi.load().sctlgpu_scale_factor(k) - v) < 1e-17
+    # the other twelve micro-kernels (kernel_functions.hpp:81-659): dims and uKerScaleFactor
+    from oracle import oracle as O
+    for k in range(4, 16):
+        assert capi.kernel_dims(k)[1:] == O.DIMS[k], k
+        assert abs(capi.load().sctlgpu_scale_factor(k) - O.scale_factor(k)) < 1e-17, k
 
 
 def test_argument_errors_without_gpu():
     lib = capi.load()
     x = np.zeros(6)
     p = x.ctypes.data
-    assert lib.sctlgpu_eval(9, 0, -1, 1, p, 1, p, None, p, p, 0, None) == capi.ERR_INVALID_KERNEL
+    assert lib.sctlgpu_eval(16, 0, -1, 1, p, 1, p, None, p, p, 0, None) == capi.ERR_INVALID_KERNEL
     assert lib.sctlgpu_eval(0, 7, -1, 1, p, 1, p, None, p, p, 0, None) == capi.ERR_INVALID_MODE
     assert lib.sctlgpu_eval(0, 0, -1, -1, p, 1, p, None, p, p, 0, None) == capi.ERR_INVALID_SIZE
     assert lib.sctlgpu_eval(0, 0, -1, 1, None, 1, p, None, p, p, 0, None) == capi.ERR_NULL_POINTER
     assert lib.sctlgpu_eval(1, 0, -1, 1, p, 1, p, None, p, p, 0, None) == capi.ERR_NULL_POINTER  # DxU needs normals
     assert lib.sctlgpu_eval(0, 0, -1, 1 << 62, p, 1, p, None, p, p, 0, None) == capi.ERR_INVALID_SIZE
     assert lib.sctlgpu_kernel_matrix(0, 0, -1, 1, p, 1, p, None, None, 0, None) == capi.ERR_NULL_POINTER
+    # the Helmholtz kernels need their wavenumber (ctx); the hot-path-only entries refuse ids >= 4
+    assert lib.sctlgpu_eval(9, 0, -1, 1, p, 1, p, None, p, p, 0, None) == capi.ERR_NULL_POINTER
+    assert lib.sctlgpu_kernel_matrix(11, 0, -1, 1, p, 1, p, None, p, 0, None) == capi.ERR_NULL_POINTER
+    assert lib.sctlgpu_eval_mixed_noalloc(4, 10, 1, p, 1, p, None, p, p, 2, None) == capi.ERR_INVALID_KERNEL
     # zero targets is a no-op that needs no device
     assert lib.sctlgpu_eval(0, 0, -1, 0, None, 5, p, None, p, None, 0, None) == capi.OK
     # near-matrix application: TrgDim must be 1, 2, 3, 4 or 9; pointers checked before any launch
