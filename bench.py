@@ -256,6 +256,39 @@ def cube_section(torch, stream):
             "rel_l2_vs_cpu": O.rel_l2(gpu, ref)}
 
 
+def ext_section(torch, stream, nt=1 << 16, ns=1 << 18):
+    """The twelve micro-kernels beyond the hot-path four: FP64 and FP32 direct sums of 2^16 targets x
+    2^18 sources (uniform in [-1,1]^3, N(0,1) densities, wavenumber 2.5), Ginteractions/s, and the
+    FP64 result against the oracle on 64 targets."""
+    import sctl_gb300 as S
+    from oracle import oracle as O
+    from sctl_gb300 import capi
+    rng = np.random.default_rng(0)
+    res = {"workload": f"{nt} targets x {ns} sources in [-1,1]^3, digits -1"}
+    names = {v: k for k, v in capi.KERNEL_IDS.items()}
+    for k in range(4, 16):
+        nd, sd, td = O.DIMS[k]
+        xs, xt = rng.uniform(-1, 1, (ns, 3)), rng.uniform(-1, 1, (nt, 3))
+        n = rng.normal(size=(ns, 3)) if nd else np.zeros((0, 3))
+        f = rng.normal(size=ns * sd)
+        K = S.GenericKernel(names[k], ctx=2.5 if k in capi.HELMHOLTZ_IDS else None)
+        row = {}
+        for mode, dt in (("f64", torch.float64), ("f32", torch.float32)):
+            d = [torch.from_numpy(np.ascontiguousarray(a)).to(dt).cuda() for a in (xt, xs, n, f)]
+            out = torch.zeros(nt * td, dtype=dt, device="cuda")
+            run = lambda: K.Eval(out, d[0], d[1], d[2], d[3], digits=-1, mode=mode)  # noqa: E731
+            run()
+            ms = _ev_ms(torch, run, reps=2)
+            row[f"{mode}_gint_s"] = nt * ns / (ms * 1e-3) / 1e9
+            if mode == "f64":
+                out.zero_()
+                run()
+                ref = O.eval(k, xt[:64], xs, n if nd else None, f, mu=2.5)
+                row["f64_rel_l2_vs_oracle_64_targets"] = O.rel_l2(out.cpu().numpy()[:64 * td], ref)
+        res[names[k]] = row
+    return res
+
+
 def mlp_section(torch, stream):
     """tcgen05 BF16 tensor-core path: one large GEMM (65536 x 256 x 4096) and the correction network
     (15 -> 256 -> 256 -> 256 -> 100, GELU) forward on 2^17 pairs and training steps on 2^14 pairs,
@@ -403,7 +436,7 @@ def main():
     ap.add_argument("--kernels", default="1,2,3", help="kernel ids of the step (default: the three sphere/ball kernels)")
     ap.add_argument("--quick", action="store_true", help="timed region only (for profiler runs)")
     ap.add_argument("--skip-torus", action="store_true", help="omit the near-singular torus section")
-    ap.add_argument("--section", choices=["near", "clusters", "cube", "torus", "torus_plain", "mlp"],
+    ap.add_argument("--section", choices=["near", "clusters", "cube", "torus", "torus_plain", "mlp", "ext"],
                     help="run only this secondary workload and print its JSON (profiling of one kernel family)")
     ap.add_argument("--torus-n", type=int, default=1 << 16, help="targets of the torus section")
     args = ap.parse_args()
@@ -417,6 +450,7 @@ def main():
         stream = torch.cuda.current_stream()
         fn = {"near": lambda: near_field_section(torch, stream), "clusters": lambda: cluster_section(torch, stream),
               "cube": lambda: cube_section(torch, stream), "mlp": lambda: mlp_section(torch, stream),
+              "ext": lambda: ext_section(torch, stream),
               "torus": lambda: torus_section(torch, n_eval=args.torus_n),
               "torus_plain": lambda: torus_section(torch, n_eval=args.torus_n, learned=False)}[args.section]
         print(json.dumps({"section": args.section, **fn()}), flush=True)
@@ -588,6 +622,7 @@ def main():
         extras["precision_stress_clusters"] = cluster_section(torch, stream)
         extras["cube8192_fp64_d14"] = cube_section(torch, stream)
         extras["tensor_core_mlp"] = mlp_section(torch, stream)
+        extras["other_micro_kernels"] = ext_section(torch, stream)
         if not args.skip_torus:
             extras["torus_near_singular"] = torus_section(torch)
 

@@ -52,7 +52,25 @@ inline void set_double_mode(int mode) { double_mode() = mode; }
 
 template <int KID>
 class GpuKernel {
-  static constexpr long kDims[4][3] = {{0, 1, 1}, {3, 1, 1}, {0, 3, 3}, {3, 3, 3}};  // NormalDim, SrcDim, TrgDim
+  // NormalDim, SrcDim, TrgDim of every kernel id (kernel_functions.hpp with generic-kernel.hpp:54-74).
+  static constexpr long kDims[SCTLGPU_NUM_KERNELS][3] = {
+      {0, 1, 1}, {3, 1, 1}, {0, 3, 3}, {3, 3, 3}, {0, 1, 3}, {0, 1, 9}, {3, 1, 3}, {0, 3, 3},
+      {0, 3, 9}, {0, 2, 2}, {3, 2, 2}, {0, 2, 6}, {0, 2, 6}, {0, 3, 9}, {0, 4, 3}, {0, 3, 4}};
+  static constexpr bool kNeedsCtx = KID >= SCTLGPU_HELMHOLTZ3D_FXU && KID <= SCTLGPU_HELMHOLTZDIFF3D_FXDU;
+
+  // The kernel object behind `self`: a GpuKernel pointer (member calls), or the
+  // kernel object's bytes as ParticleFMM passes them (fmm-wrapper.txx:618).
+  template <class SelfT>
+  static const void* ctx_of(const SelfT& self) {
+    if constexpr (!kNeedsCtx) {
+      return nullptr;
+    } else if constexpr (std::is_convertible<SelfT, const void*>::value) {
+      const void* p = self;
+      return p ? static_cast<const GpuKernel*>(p)->ctx_ptr : nullptr;
+    } else {
+      return reinterpret_cast<const GpuKernel*>(&self[0])->ctx_ptr;
+    }
+  }
 
   template <class V>
   static auto ptr(V& v) -> decltype(&v[0]) {
@@ -64,14 +82,18 @@ class GpuKernel {
   }
 
  public:
-  static_assert(KID >= 0 && KID < 4, "unknown sctlgpu kernel id");
+  static_assert(KID >= 0 && KID < SCTLGPU_NUM_KERNELS, "unknown sctlgpu kernel id");
 
   static constexpr long CoordDim() { return 3; }
   static constexpr long NormalDim() { return kDims[KID][0]; }
   static constexpr long SrcDim() { return kDims[KID][1]; }
   static constexpr long TrgDim() { return kDims[KID][2]; }
-  static const std::string& Name() {  // kernel_functions.hpp:33-36,62-65,126-129,181-184
-    static const std::string names[4] = {"Laplace3D-FxU", "Laplace3D-DxU", "Stokes3D-FxU", "Stokes3D-DxU"};
+  static const std::string& Name() {  // the Name() of each micro-kernel, kernel_functions.hpp
+    static const std::string names[SCTLGPU_NUM_KERNELS] = {
+        "Laplace3D-FxU",    "Laplace3D-DxU",     "Stokes3D-FxU",    "Stokes3D-DxU",
+        "Laplace3D-FxdU",   "Laplace3D-Fxd2U",   "Laplace3D-DxdU",  "BiotSavart3D-FxU",
+        "BiotSavart3D-FxdU", "Helmholtz3D-FxU",  "Helmholtz3D-DxU", "Helmholtz3D-FxdU",
+        "HelmholtzDiff3D-FxdU", "Stokes3D-FxT", "Stokes3D-FSxU",   "Stokes3D-FxUP"};
     return names[KID];
   }
 
@@ -80,9 +102,11 @@ class GpuKernel {
   const void* GetCtxPtr() const { return ctx_ptr; }
 
   // GenericKernel<uK>::Eval<Real,enable_openmp>(..., digits, self), generic-kernel.hpp:99.
+  // `self` is the kernel object; the Helmholtz kernels read their wavenumber through its ctx
+  // pointer (SetCtxPtr), a value of type Real.
   template <class Real, bool enable_openmp, class VecT, class SelfT>
   static void Eval(VecT& v_trg, const VecT& r_trg, const VecT& r_src, const VecT& n_src, const VecT& v_src,
-                   long digits, SelfT /*self*/) {
+                   long digits, SelfT self) {
     static_assert(std::is_same<Real, float>::value || std::is_same<Real, double>::value, "Real must be float or double");
     const long nt = (long)r_trg.Dim() / 3, ns = (long)r_src.Dim() / 3;
     if ((long)r_trg.Dim() != nt * 3 || (long)r_src.Dim() != ns * 3 || (long)v_src.Dim() != ns * SrcDim() ||
@@ -94,8 +118,9 @@ class GpuKernel {
       v_trg.SetZero();
       flags = 0;
     }
-    const int rc = sctlgpu_eval(KID, mode_for<Real>(), (int)digits, nt, ptr(r_trg), ns, ptr(r_src),
-                                NormalDim() ? ptr(n_src) : nullptr, ptr(v_src), ptr(v_trg), flags, nullptr);
+    const int rc = sctlgpu_eval_ctx(KID, mode_for<Real>(), (int)digits, nt, ptr(r_trg), ns, ptr(r_src),
+                                    NormalDim() ? ptr(n_src) : nullptr, ptr(v_src), ptr(v_trg), flags, ctx_of(self),
+                                    nullptr);
     if (rc != SCTLGPU_OK) SCTLGPU_ON_ERROR(rc, "GpuKernel::Eval");
   }
 
@@ -114,8 +139,8 @@ class GpuKernel {
       M.SetZero();
     }
     if (!ns || !nt) return;
-    const int rc = sctlgpu_kernel_matrix(KID, mode_for<Real>(), (int)digits, nt, ptr(Xt), ns, ptr(Xs),
-                                         NormalDim() ? ptr(Xn) : nullptr, &M[0][0], 0, nullptr);
+    const int rc = sctlgpu_kernel_matrix_ctx(KID, mode_for<Real>(), (int)digits, nt, ptr(Xt), ns, ptr(Xs),
+                                             NormalDim() ? ptr(Xn) : nullptr, &M[0][0], 0, ctx_ptr, nullptr);
     if (rc != SCTLGPU_OK) SCTLGPU_ON_ERROR(rc, "GpuKernel::KernelMatrix");
   }
 
@@ -124,13 +149,25 @@ class GpuKernel {
 };
 
 template <int KID>
-constexpr long GpuKernel<KID>::kDims[4][3];
+constexpr long GpuKernel<KID>::kDims[SCTLGPU_NUM_KERNELS][3];
 
-// The aliases of kernel_functions.hpp:669-678.
+// The aliases of kernel_functions.hpp:669-684.
 using Laplace3D_FxU = GpuKernel<SCTLGPU_LAPLACE3D_FXU>;
 using Laplace3D_DxU = GpuKernel<SCTLGPU_LAPLACE3D_DXU>;
+using Laplace3D_FxdU = GpuKernel<SCTLGPU_LAPLACE3D_FXDU>;
+using Laplace3D_Fxd2U = GpuKernel<SCTLGPU_LAPLACE3D_FXD2U>;
+using Laplace3D_DxdU = GpuKernel<SCTLGPU_LAPLACE3D_DXDU>;
+using BiotSavart3D_FxU = GpuKernel<SCTLGPU_BIOTSAVART3D_FXU>;
+using BiotSavart3D_FxdU = GpuKernel<SCTLGPU_BIOTSAVART3D_FXDU>;
+using Helmholtz3D_FxU = GpuKernel<SCTLGPU_HELMHOLTZ3D_FXU>;
+using Helmholtz3D_DxU = GpuKernel<SCTLGPU_HELMHOLTZ3D_DXU>;
+using Helmholtz3D_FxdU = GpuKernel<SCTLGPU_HELMHOLTZ3D_FXDU>;
+using HelmholtzDiff3D_FxdU = GpuKernel<SCTLGPU_HELMHOLTZDIFF3D_FXDU>;
 using Stokes3D_FxU = GpuKernel<SCTLGPU_STOKES3D_FXU>;
 using Stokes3D_DxU = GpuKernel<SCTLGPU_STOKES3D_DXU>;
+using Stokes3D_FxT = GpuKernel<SCTLGPU_STOKES3D_FXT>;
+using Stokes3D_FSxU = GpuKernel<SCTLGPU_STOKES3D_FSXU>;
+using Stokes3D_FxUP = GpuKernel<SCTLGPU_STOKES3D_FXUP>;
 
 }  // namespace sctlgpu
 

@@ -21,6 +21,9 @@ KerS2TEval<double> p0 = &sctlgpu::Laplace3D_FxU::Eval<double, true, sctl::Vector
 KerS2TEval<double> p1 = &sctlgpu::Laplace3D_DxU::Eval<double, true, sctl::Vector<double>, sctl::ConstIterator<char>>;
 KerS2TEval<float> p2 = &sctlgpu::Stokes3D_FxU::Eval<float, false, sctl::Vector<float>, sctl::ConstIterator<char>>;
 KerS2TEval<double> p3 = &sctlgpu::Stokes3D_DxU::Eval<double, true, sctl::Vector<double>, sctl::ConstIterator<char>>;
+// a kernel that reads its context through `self` (the Helmholtz wavenumber)
+KerS2TEval<double> p4 = &sctlgpu::Helmholtz3D_FxdU::Eval<double, true, sctl::Vector<double>, sctl::ConstIterator<char>>;
+KerS2TEval<float> p5 = &sctlgpu::Stokes3D_FxT::Eval<float, true, sctl::Vector<float>, sctl::ConstIterator<char>>;
 
 void instantiate_members() {
   sctlgpu::Stokes3D_DxU k;

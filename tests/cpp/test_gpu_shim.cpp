@@ -111,8 +111,9 @@ static void known_answers(R tol) {
 
 // Eval vs KernelMatrix on the 7 x 5 inputs of test-kernel_functions.cpp:487-526.
 template <class K, class R>
-static void eval_vs_matrix(R tol) {
+static void eval_vs_matrix(R tol, R* ctx = nullptr) {
   K ker;
+  ker.SetCtxPtr(ctx);
   const long Ns = 7, Nt = 5, K0 = K::SrcDim(), K1 = K::TrgDim(), ND = K::NormalDim();
   Vec<R> Xs(Ns * 3), Xn(Ns * ND), Vs(Ns * K0), Xt(Nt * 3), Vt;
   for (long i = 0; i < Xs.Dim(); i++) Xs[i] = R(0.1 * (i + 1) - 0.35);
@@ -157,6 +158,35 @@ int main() {
   }
   known_answers<float>(1e-5f);
   eval_vs_matrix<sctlgpu::Stokes3D_DxU, float>(1e-5f);
+  // the other micro-kernels (kernel_functions.hpp:81-659), the Helmholtz ones with ctx = wavenumber
+  sctlgpu::set_double_mode(SCTLGPU_F64);
+  double mu = 2.5;
+  float muf = 2.5f;
+  eval_vs_matrix<sctlgpu::Laplace3D_FxdU, double>(1e-12);
+  eval_vs_matrix<sctlgpu::Laplace3D_Fxd2U, double>(1e-12);
+  eval_vs_matrix<sctlgpu::Laplace3D_DxdU, double>(1e-12);
+  eval_vs_matrix<sctlgpu::BiotSavart3D_FxU, double>(1e-12);
+  eval_vs_matrix<sctlgpu::BiotSavart3D_FxdU, double>(1e-12);
+  eval_vs_matrix<sctlgpu::Helmholtz3D_FxU, double>(1e-12, &mu);
+  eval_vs_matrix<sctlgpu::Helmholtz3D_DxU, double>(1e-12, &mu);
+  eval_vs_matrix<sctlgpu::Helmholtz3D_FxdU, double>(1e-12, &mu);
+  eval_vs_matrix<sctlgpu::HelmholtzDiff3D_FxdU, double>(1e-12, &mu);
+  eval_vs_matrix<sctlgpu::Stokes3D_FxT, double>(1e-12);
+  eval_vs_matrix<sctlgpu::Stokes3D_FSxU, double>(1e-12);
+  eval_vs_matrix<sctlgpu::Stokes3D_FxUP, double>(1e-12);
+  eval_vs_matrix<sctlgpu::Helmholtz3D_FxdU, float>(1e-5f, &muf);
+  {
+    // ParticleFMM passes the kernel object's bytes as `self` (fmm-wrapper.txx:618): the
+    // static Eval finds the wavenumber through them.
+    sctlgpu::Helmholtz3D_FxU H;
+    H.SetCtxPtr(&mu);
+    S2TEval<double> hp = &sctlgpu::Helmholtz3D_FxU::Eval<double, true, Vec<double>, const char*>;
+    Vec<double> Xs({0, 0, 0}), Xt({2, 0, 0}), Xn, v_s({1.0, 0.0}), v_t;
+    hp(v_t, Xt, Xs, Xn, v_s, -1, reinterpret_cast<const char*>(&H));
+    const double pi = 3.14159265358979323846;
+    CHECK(v_t.Dim() == 2 && approx_eq(v_t[0], std::cos(2 * mu) / (4 * pi * 2), 1e-12) &&
+          approx_eq(v_t[1], std::sin(2 * mu) / (4 * pi * 2), 1e-12));
+  }
   std::printf("\n%s (%d check(s) failed)\n", failures == 0 ? "PASS" : "FAIL", failures);
   return failures == 0 ? 0 : 1;
 }
