@@ -3,22 +3,28 @@
 //
 //   C[M x N] = act(A[M x K] . Bt[N x K]^T + bias)     (A, Bt row-major, K contiguous)
 //
-// One CTA of 128 threads owns a 128-row tile of C and all N (<= 256) columns.
-// K is consumed in chunks of 64: every thread copies 16-byte pieces of the A
-// and Bt chunks (cp.async) into shared memory in the canonical no-swizzle
-// K-major layout of tcgen05 (8 x 16-byte core matrices; K-adjacent cores 128 B
-// apart, 8-row groups 1024 B apart), one elected thread issues four
-// tcgen05.mma (M=128, N, K=16) per chunk into the TMEM accumulator and commits
-// them to an mbarrier, which gates the reuse of that chunk's buffer (two
-// buffers: the copy of chunk k+1 overlaps the MMAs of chunk k).  The epilogue
-// warps read their 32 TMEM lanes (tcgen05.ld 32x32b), add the bias, apply GELU
-// and store FP32 and/or BF16.  Every mbarrier wait is bounded; TMEM is always
-// released before the CTA exits.
+// One CTA of 128 threads owns a 128-row tile of C and all N (<= 256) columns,
+// optionally a slice of K (split-K, partials reduced in a fixed order).  K is
+// consumed in chunks of 64 through a ring of 4-8 shared-memory stages:
+//   * one producer thread loads each chunk of A (128 x 64) and Bt (N x 64) with
+//     TMA tensor copies (cp.async.bulk.tensor.2d, 128-byte swizzle) completing
+//     on the stage's `full` mbarrier;
+//   * one MMA thread waits for `full`, issues four tcgen05.mma (M=128, N, K=16)
+//     from swizzled K-major shared-memory descriptors into the TMEM
+//     accumulator, and commits them to the stage's `empty` mbarrier, which
+//     hands the stage back to the producer;
+//   * after the last chunk the MMA thread commits to `done`; all four warps
+//     then read their 32 TMEM lanes (tcgen05.ld 32x32b), add the bias, apply
+//     GELU and store FP32 and/or BF16 rows with 16-byte stores.
+// Every mbarrier wait is bounded (a timeout sets the status word, skips the
+// epilogue and drains the copies in flight); TMEM is always released.
 #include <cmath>
 #include <cstdint>
+#include <mutex>
 #include <random>
 #include <vector>
 
+#include <cuda.h>  // CUtensorMap and its enums; the encoder is fetched from the driver at run time
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -30,16 +36,18 @@ namespace sctlgpu {
 namespace {
 
 constexpr int TC_M = 128, TC_KC = 64, TC_THREADS = 128;
-constexpr int TC_A_BYTES = TC_M * TC_KC * 2;   // 16 KB per chunk
-constexpr int TC_B_BYTES = 256 * TC_KC * 2;    // up to 32 KB per chunk
+constexpr int TC_A_BYTES = TC_M * TC_KC * 2;  // 16 KB per chunk
+constexpr int TC_SMEM_BUDGET = 200 * 1024;     // stage ring
 
-// tcgen05 shared-memory matrix descriptor, no swizzle, K-major:
-// start >> 4 in [0,14), leading-dimension byte offset >> 4 in [16,30) (between
-// K-adjacent core matrices), stride-dimension byte offset >> 4 in [32,46)
-// (between 8-row groups), bits [46,49) = 0b001, layout type 0 (no swizzle).
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
-         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+// tcgen05 shared-memory matrix descriptor for a K-major tile written by TMA
+// with 128-byte swizzle: start >> 4 in [0,14), leading byte offset (unused
+// for swizzled K-major, 16 B) in [16,30), stride byte offset >> 4 in [32,46)
+// (1024 B between 8-row groups of 128-byte rows), version 1 at bit 46, layout
+// SWIZZLE_128B (2) in [61,64).  Stepping K by 16 elements adds 32 bytes to the
+// start address inside the swizzle atom.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) | (1ull << 46) |
+         (2ull << 61);
 }
 
 // Instruction descriptor for kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
@@ -85,17 +93,13 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
-}
-
-// Offset of element (row r, k) inside a chunk stored as 8x16B core matrices:
-// core (r/8, k/8) at ((r/8)*8 + k/8) * 128 bytes, row r%8 at +16*(r%8).
-__device__ __forceinline__ uint32_t core_off(int r, int k) {
-  return (uint32_t)((((r >> 3) * (TC_KC / 8) + (k >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1));
+// 2-D TMA tile load (x = innermost coordinate, in elements) into shared memory.
+__device__ __forceinline__ void tma_load_2d(void* smem_dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(smem_dst)),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
 }
 
 __device__ __forceinline__ float gelu(float x) {  // tanh form
@@ -119,23 +123,39 @@ struct TcParams {
   int dot_cols;
   double* dot_out;
   unsigned* status;
+  // split-K (gridDim.y slices): raw FP32 partials [slice][M][N], reduced afterwards
+  float* partial;
+  int stages;
 };
 
-__global__ void __launch_bounds__(TC_THREADS) tc_gemm_kernel(TcParams p) {
-  extern __shared__ __align__(1024) unsigned char tsm[];
-  unsigned char* bufA[2] = {tsm, tsm + TC_A_BYTES};
-  unsigned char* bufB[2] = {tsm + 2 * TC_A_BYTES, tsm + 2 * TC_A_BYTES + TC_B_BYTES};
-  uint64_t* bars = reinterpret_cast<uint64_t*>(tsm + 2 * TC_A_BYTES + 2 * TC_B_BYTES);  // [2] chunk + [1] done
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 4);
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, TcParams p) {
+  extern __shared__ unsigned char tsm_raw[];
+  unsigned char* tsm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tsm_raw) + 1023) & ~(uintptr_t)1023);
+  const int nst = p.stages;
+  const uint32_t b_bytes = (uint32_t)p.N * TC_KC * 2;
+  const uint32_t stage_bytes = TC_A_BYTES + b_bytes;  // multiple of 1024 (N % 16 == 0)
+  uint64_t* full = reinterpret_cast<uint64_t*>(tsm + (size_t)nst * stage_bytes);
+  uint64_t* empty = full + nst;
+  uint64_t* done = empty + nst;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  int* s_err = reinterpret_cast<int*>(tmem_slot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.x * TC_M;
   const uint32_t ncols = p.N <= 32 ? 32 : p.N <= 64 ? 64 : p.N <= 128 ? 128 : 256;
+  const int nchunks = p.K / TC_KC;
+  const int per = (nchunks + (int)gridDim.y - 1) / (int)gridDim.y;
+  const int c0 = (int)blockIdx.y * per;
+  const int nk = max(0, min(nchunks, c0 + per) - c0);
 
   if (tid == 0) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
-    mbar_init(&bars[2], 1);
+    for (int s = 0; s < nst; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    *s_err = 0;
     fence_mbar_init();
   }
   if (warp == 0) tmem_alloc(tmem_slot, ncols);
@@ -144,87 +164,211 @@ __global__ void __launch_bounds__(TC_THREADS) tc_gemm_kernel(TcParams p) {
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  const uint32_t idesc = idesc_bf16(TC_M, p.N);
-  const int nchunks = p.K / TC_KC;
-  uint32_t use[2] = {0, 0};  // times each buffer was committed
-  bool ok = true;
-  for (int kc = 0; kc < nchunks; ++kc) {
-    const int b = kc & 1;
-    if (kc >= 2) {  // the MMAs that read this buffer two chunks ago must be complete
-      if (!mbar_wait_bounded(&bars[b], (use[b] - 1) & 1, p.status)) ok = false;
-    }
-    // copy the A chunk (128 x 64) and the Bt chunk (N x 64) into core-matrix layout
-    const int k0 = kc * TC_KC;
-    for (int i = tid; i < TC_M * (TC_KC / 8); i += TC_THREADS) {
-      const int r = i / (TC_KC / 8), kk = (i % (TC_KC / 8)) * 8;
-      cp_async16(bufA[b] + core_off(r, kk), p.A + (size_t)(m0 + r) * p.K + k0 + kk);
-    }
-    for (int i = tid; i < p.N * (TC_KC / 8); i += TC_THREADS) {
-      const int r = i / (TC_KC / 8), kk = (i % (TC_KC / 8)) * 8;
-      cp_async16(bufB[b] + core_off(r, kk), p.Bt + (size_t)r * p.K + k0 + kk);
-    }
-    cp_async_wait_all();
-    fence_proxy_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-      tc_fence_after();
-      const uint32_t a0 = smem_u32(bufA[b]), b0 = smem_u32(bufB[b]);
-#pragma unroll
-      for (int j = 0; j < TC_KC / 16; ++j) {
-        const uint64_t ad = smem_desc(a0 + j * 256, 128, 1024);
-        const uint64_t bd = smem_desc(b0 + j * 256, 128, 1024);
-        tc_mma(tmem, ad, bd, idesc, (kc > 0 || j > 0) ? 1 : 0);
+  if (warp == 0 && lane == 0) {  // producer
+    int issued = 0;
+    for (int i = 0; i < nk; ++i) {
+      const int s = i % nst;
+      const uint32_t use = (uint32_t)(i / nst);
+      if (i >= nst && !mbar_wait_bounded(&empty[s], (use - 1) & 1, p.status)) {
+        atomicExch(s_err, 1);
+        break;
       }
-      tc_commit(&bars[b]);
+      unsigned char* a = tsm + (size_t)s * stage_bytes;
+      mbar_arrive_expect_tx(&full[s], stage_bytes);
+      tma_load_2d(a, &mapA, (c0 + i) * TC_KC, m0, &full[s]);
+      tma_load_2d(a + TC_A_BYTES, &mapB, (c0 + i) * TC_KC, 0, &full[s]);
+      ++issued;
     }
-    ++use[b];
+    // Copies still in flight (only after a timeout): let them land before the CTA exits.
+    for (int i = max(0, issued - nst); i < issued; ++i)
+      mbar_wait_bounded(&full[i % nst], (uint32_t)((i / nst) & 1), nullptr);
+  } else if (warp == 1 && lane == 0) {  // MMA issuer
+    const uint32_t idesc = idesc_bf16(TC_M, p.N);
+    for (int i = 0; i < nk; ++i) {
+      const int s = i % nst;
+      if (!mbar_wait_bounded(&full[s], (uint32_t)((i / nst) & 1), p.status)) {
+        atomicExch(s_err, 1);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t a0 = smem_u32(tsm + (size_t)s * stage_bytes), b0 = a0 + TC_A_BYTES;
+#pragma unroll
+      for (int j = 0; j < TC_KC / 16; ++j)
+        tc_mma(tmem, smem_desc_sw128(a0 + j * 32), smem_desc_sw128(b0 + j * 32), idesc, (i > 0 || j > 0) ? 1 : 0);
+      tc_commit(&empty[s]);
+    }
+    tc_commit(done);  // tracks every MMA issued above (arrives at once if none)
   }
-  if (tid == 0) tc_commit(&bars[2]);
-  if (!mbar_wait_bounded(&bars[2], 0, p.status)) ok = false;
-  // Drain the chunk barriers' last phases as well (their MMAs are complete once bars[2] fired).
+  if (!mbar_wait_bounded(done, 0, p.status)) atomicExch(s_err, 1);
+  if (tid == 32) {  // the MMA thread's last commits to the stage barriers have landed too
+    for (int i = max(0, nk - nst); i < nk; ++i)
+      mbar_wait_bounded(&empty[i % nst], (uint32_t)((i / nst) & 1), nullptr);
+  }
+  __syncthreads();
   tc_fence_after();
+  const bool ok = *s_err == 0 && nk > 0;
 
   if (ok) {
     const int row = m0 + warp * 32 + lane;
-    double dot = 0.0;
-    const double* dv = (p.dot_out && p.dot_index[row] >= 0) ? p.dot_dens + p.dot_index[row] * p.dot_cols : nullptr;
-    for (int c0 = 0; c0 < p.N; c0 += 16) {
-      float v[16];
-      tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+    if (p.partial) {  // split-K slice: raw sums
+      float* dst = p.partial + ((size_t)blockIdx.y * p.M + row) * p.N;
+      for (int cb = 0; cb < p.N; cb += 16) {
+        float v[16];
+        tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb, v);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int col = c0 + i;
-        float x = v[i] + (p.bias ? p.bias[col] : 0.f);
-        if (p.pre32) p.pre32[(size_t)row * p.N + col] = x;
-        if (p.act == 1) x = gelu(x);
-        if (p.C32) {
-          float* o = &p.C32[(size_t)row * p.N + col];
-          *o = p.accumulate32 ? *o + x : x;
-        }
-        if (p.C16) p.C16[(size_t)row * p.N + col] = __float2bfloat16_rn(x);
-        if (dv && col < p.dot_cols) dot = fma((double)x, dv[col], dot);
+        for (int q = 0; q < 4; ++q)
+          reinterpret_cast<float4*>(dst + cb)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
       }
+    } else {
+      double dot = 0.0;
+      const double* dv =
+          (p.dot_out && p.dot_index[row] >= 0) ? p.dot_dens + p.dot_index[row] * p.dot_cols : nullptr;
+      for (int cb = 0; cb < p.N; cb += 16) {
+        float v[16], x[16];
+        tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb, v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          v[i] += p.bias ? p.bias[cb + i] : 0.f;
+          x[i] = p.act == 1 ? gelu(v[i]) : v[i];
+        }
+        const size_t o = (size_t)row * p.N + cb;
+        if (p.pre32)
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            reinterpret_cast<float4*>(p.pre32 + o)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        if (p.C32) {
+          float4* c = reinterpret_cast<float4*>(p.C32 + o);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            float4 w = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
+            if (p.accumulate32) {
+              const float4 old = c[q];
+              w.x += old.x;
+              w.y += old.y;
+              w.z += old.z;
+              w.w += old.w;
+            }
+            c[q] = w;
+          }
+        }
+        if (p.C16) {
+          __nv_bfloat162 h[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) h[q] = __floats2bfloat162_rn(x[2 * q], x[2 * q + 1]);
+          uint4* d16 = reinterpret_cast<uint4*>(p.C16 + o);
+          d16[0] = *reinterpret_cast<const uint4*>(&h[0]);
+          d16[1] = *reinterpret_cast<const uint4*>(&h[4]);
+        }
+        if (dv)
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+            if (cb + i < p.dot_cols) dot = fma((double)x[i], dv[cb + i], dot);
+      }
+      if (dv) p.dot_out[row] += dot;
     }
-    if (dv) p.dot_out[row] += dot;
   }
-  if (!ok && tid == 0) mbar_wait_bounded(&bars[2], 0, nullptr);  // let in-flight MMAs land before TMEM is freed
   tc_fence_before();
   __syncthreads();
   if (warp == 0) tmem_dealloc(tmem, ncols);
 }
 
-cudaError_t tc_gemm_launch(const TcParams& p, cudaStream_t st) {
-  const size_t smem = 2 * TC_A_BYTES + 2 * TC_B_BYTES + 64;
+// C (+)= sum over slices of the split-K partials, in slice order.
+__global__ void tc_splitk_reduce_kernel(int64_t n, int slices, const float* __restrict__ partial, int accumulate,
+                                        float* __restrict__ C) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float acc = accumulate ? C[i] : 0.f;
+    for (int s = 0; s < slices; ++s) acc += partial[(int64_t)s * n + i];
+    C[i] = acc;
+  }
+}
+
+// cuTensorMapEncodeTiled from the driver (no link-time dependency on libcuda).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return (EncodeTiledFn) nullptr;
+    return (EncodeTiledFn)f;
+  }();
+  return fn;
+}
+
+// Row-major BF16 matrix [rows][K] as a 2-D tensor map with box (64, box_rows), 128-byte swizzle.
+cudaError_t make_map(CUtensorMap* map, const void* base, int rows, int K, int box_rows) {
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc) return cudaErrorNotSupported;
+  const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)TC_KC, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+int stages_for(int N) {
+  const int stage = TC_A_BYTES + N * TC_KC * 2;
+  return std::max(2, std::min(8, TC_SMEM_BUDGET / stage));
+}
+
+size_t smem_for(int N, int stages) { return 1024 + (size_t)stages * (TC_A_BYTES + N * TC_KC * 2) + 256; }
+
+cudaError_t tc_gemm_launch(const TcParams& p0, cudaStream_t st) {
+  TcParams p = p0;
+  int dev = 0, sms = 0;
+  unsigned* status = nullptr;
+  if (runtime_device(&dev, &status, &sms) != SCTLGPU_OK) return cudaErrorNoDevice;
+  CUtensorMap ma, mb;
+  cudaError_t e = make_map(&ma, p.A, p.M, p.K, TC_M);
+  if (e == cudaSuccess) e = make_map(&mb, p.Bt, p.N, p.K, p.N);
+  if (e != cudaSuccess) return e;
+  p.stages = stages_for(p.N);
+  const size_t smem = smem_for(p.N, p.stages);
   static bool attr[64] = {};
-  int dev = 0;
-  cudaGetDevice(&dev);
   if (dev >= 0 && dev < 64 && !attr[dev]) {
-    cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int n = 16;  // the largest ring over all N
+    for (int N = 32; N <= 256; N += 16)
+      if (smem_for(N, stages_for(N)) > smem_for(n, stages_for(n))) n = N;
+    cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_for(n, stages_for(n)));
     attr[dev] = true;
   }
-  tc_gemm_kernel<<<p.M / TC_M, TC_THREADS, smem, st>>>(p);
+  // Split K when the row tiles cannot fill the GPU and the epilogue is a plain FP32 store;
+  // every slice gets at least one chunk.
+  const int tiles = p.M / TC_M, chunks = p.K / TC_KC;
+  const bool plain = p.C32 && !p.pre32 && !p.C16 && !p.bias && p.act == 0 && !p.dot_out;
+  int slices = 1;
+  if (plain && tiles < sms && chunks >= 8) {
+    slices = std::min(std::max(1, sms / tiles), chunks / 4);
+    const int per = (chunks + slices - 1) / slices;
+    slices = (chunks + per - 1) / per;
+  }
+  p.partial = nullptr;
+  float* part = nullptr;
+  if (slices > 1) {
+    if ((e = cudaMallocAsync((void**)&part, (size_t)slices * p.M * p.N * sizeof(float), st))) return e;
+    p.partial = part;
+  }
+  tc_gemm_kernel<<<dim3((unsigned)tiles, (unsigned)slices), TC_THREADS, smem, st>>>(ma, mb, p);
   g_launches.fetch_add(1, std::memory_order_relaxed);
-  return cudaGetLastError();
+  e = cudaGetLastError();
+  if (slices > 1) {
+    if (e == cudaSuccess) {
+      const int64_t n = (int64_t)p.M * p.N;
+      tc_splitk_reduce_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)sms * 8), 256, 0, st>>>(
+          n, slices, part, p.accumulate32, p.C32);
+      g_launches.fetch_add(1, std::memory_order_relaxed);
+      e = cudaGetLastError();
+    }
+    cudaError_t e2 = cudaFreeAsync(part, st);
+    if (e == cudaSuccess) e = e2;
+  }
+  return e;
 }
 
 TcParams gemm_params(int M, int N, int K, const __nv_bfloat16* A, const __nv_bfloat16* Bt, unsigned* status) {
@@ -620,18 +764,14 @@ extern "C" int sctlgpu_tc_gemm_bf16(int M, int N, int K, const void* A, const vo
   if (M <= 0 || N <= 0 || K <= 0 || M % TC_M || N % 16 || N > 256 || K % TC_KC) return SCTLGPU_ERR_INVALID_SIZE;
   if (!A || !Bt || (!C32 && !C16 && !pre32)) return SCTLGPU_ERR_NULL_POINTER;
   if (act != 0 && act != 1) return SCTLGPU_ERR_INVALID_ARGUMENT;
-  if (((uintptr_t)A | (uintptr_t)Bt) & 15) return SCTLGPU_ERR_INVALID_ARGUMENT;  // 16-byte copies
+  // TMA sources and 16-byte epilogue stores need 16-byte aligned bases
+  if (((uintptr_t)A | (uintptr_t)Bt | (uintptr_t)C32 | (uintptr_t)pre32 | (uintptr_t)C16) & 15)
+    return SCTLGPU_ERR_INVALID_ARGUMENT;
   int dev;
   unsigned* status;
   int sms;
   int rc = runtime_device(&dev, &status, &sms);
   if (rc) return rc;
-  const size_t smem = 2 * TC_A_BYTES + 2 * TC_B_BYTES + 64;
-  static bool attr[64] = {};
-  if (!attr[dev]) {
-    cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr[dev] = true;
-  }
   TcParams p{};
   p.M = M;
   p.N = N;

@@ -64,3 +64,35 @@ def test_tc_gemm_rejects_bad_shapes(cuda):
     A = torch.zeros(100, 64, dtype=torch.bfloat16, device="cuda")
     assert capi.load().sctlgpu_tc_gemm_bf16(100, 16, 64, A.data_ptr(), A.data_ptr(), None, 0, A.data_ptr(), None,
                                             None, 0, None) == capi.ERR_INVALID_SIZE
+
+
+@pytest.mark.parametrize("M,N,K,acc", [(512, 256, 4096, 0), (256, 64, 16384, 0), (128, 128, 8192, 1),
+                                       (1024, 16, 640, 0)])
+def test_tc_gemm_ring_wraparound_and_split_k(cuda, M, N, K, acc):
+    """Many more K chunks than ring stages (the producer waits for stages the MMAs released),
+    and small-M plain FP32 outputs that take the split-K path (partials reduced in slice order),
+    with and without accumulation into C."""
+    torch = cuda
+    g = torch.Generator(device="cuda").manual_seed(M * 7 + N + K)
+    A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
+    Bt = (torch.randn(N, K, device="cuda", generator=g) / math.sqrt(K)).to(torch.bfloat16)
+    C0 = torch.randn(M, N, device="cuda", generator=g)
+    C = C0.clone()
+    rc = capi.load().sctlgpu_tc_gemm_bf16(M, N, K, A.data_ptr(), Bt.data_ptr(), None, 0, C.data_ptr(), None, None,
+                                          acc, torch.cuda.current_stream().cuda_stream)
+    assert rc == capi.OK, capi.load().sctlgpu_strerror(rc)
+    torch.cuda.synchronize()
+    want = A.float() @ Bt.float().T + (C0 if acc else 0)
+    err = ((C - want).abs().max() / want.abs().max()).item()
+    assert err < 1e-5, err
+    assert capi.load().sctlgpu_device_status(None) == capi.OK
+
+
+def test_tc_gemm_rejects_misaligned_outputs(cuda):
+    torch = cuda
+    A = torch.zeros(128, 64, dtype=torch.bfloat16, device="cuda")
+    Bt = torch.zeros(16, 64, dtype=torch.bfloat16, device="cuda")
+    C = torch.zeros(128 * 16 + 4, device="cuda")
+    rc = capi.load().sctlgpu_tc_gemm_bf16(128, 16, 64, A.data_ptr(), Bt.data_ptr(), None, 0, C.data_ptr() + 4, None,
+                                          None, 0, None)
+    assert rc == capi.ERR_INVALID_ARGUMENT
