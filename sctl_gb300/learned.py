@@ -6,10 +6,12 @@ features; the pair's correction is then sum_ab (W_ab - W^smooth_ab) sigma_ab.
 * Labels come from the adaptive quadrature (`sctlgpu_panel_near_weights`).
 * Training and inference run on the tcgen05 kernels of libsctlgpu
   (`sctlgpu_mlp_*`): BF16 weights and activations, FP32 accumulation.
-* Two networks trained from different seeds form the a-posteriori check: where
-  their predicted corrections differ by more than the tolerance, or the pair is
-  outside the trained range, the plain adaptive path (the judge of the error)
-  is used instead.
+* Two networks trained from different seeds and a calibrated error model form
+  the a-posteriori check: a pair is accepted only when it is inside the trained
+  range, the networks' predicted corrections agree to the tolerance, and the
+  calibrated bound on its error -- the largest weight error seen on held-out
+  labels at its distance, times 2, times the panel's density l1 norm -- is
+  below the tolerance; every other pair takes the plain adaptive path.
 """
 from __future__ import annotations
 
@@ -148,20 +150,32 @@ class Standardizer:
 
 
 class LearnedCorrection:
-    """Ensemble of correction networks with range gating and a disagreement check."""
+    """Ensemble of correction networks with range gating, a disagreement check and an error model
+    calibrated on held-out labels."""
+
+    CALIB_BINS = 16  # bins of |signed log distance feature| in [0, 1]
+    CALIB_SAFETY = 2.0
 
     def __init__(self, n_models=2, max_batch=1 << 14, seeds=(1, 2)):
         self.models = [MLP(max_batch=max_batch, seed=s) for s in seeds[:n_models]]
         self.fx = self.fy = None
         self.range = None
+        self.calib = None
 
-    def fit(self, feats: torch.Tensor, w: torch.Tensor, steps=2000, batch=1 << 14, lr=2e-3, seed=0, log=None):
-        """Train every model on (features, accurate weights); returns the final losses."""
+    def fit(self, feats: torch.Tensor, w: torch.Tensor, steps=2000, batch=1 << 14, lr=2e-3, seed=0, log=None,
+            val_frac=0.1):
+        """Train every model on (features, accurate weights), holding out `val_frac` of the pairs to
+        calibrate the error model; returns the final losses."""
+        g = torch.Generator(device=feats.device).manual_seed(seed)
+        perm = torch.randperm(feats.shape[0], device=feats.device, generator=g)
+        n_val = int(feats.shape[0] * val_frac)
+        val, trn = perm[:n_val], perm[n_val:]
+        fv, wv = feats[val], w[val]
+        feats, w = feats[trn], w[trn]
         self.fx, self.fy = Standardizer(feats), Standardizer(w)
         self.range = (feats.min(0).values, feats.max(0).values)
         X, Y = self.fx.fwd(feats).contiguous(), self.fy.fwd(w).contiguous()
         n = X.shape[0]
-        g = torch.Generator(device=X.device).manual_seed(seed)
         losses = []
         for mi, m in enumerate(self.models):
             last = None
@@ -175,7 +189,29 @@ class LearnedCorrection:
                     if log:
                         log(f"model {mi} step {it} loss {loss:.4e}")
             losses.append(last)
+        self._calibrate(fv, wv)
         return losses
+
+    def _bin(self, feats):
+        return (feats[:, 2].abs().clamp(0, 1) * self.CALIB_BINS).long().clamp(max=self.CALIB_BINS - 1)
+
+    def _calibrate(self, fv, wv):
+        """Largest max-norm weight error of the ensemble mean on held-out pairs, per distance bin
+        (bins without held-out pairs get the overall largest)."""
+        pred = self.predict(fv).mean(0)
+        err = (pred - wv).abs().max(1).values
+        b = self._bin(fv)
+        top = err.max() if err.numel() else torch.tensor(float("inf"), device=fv.device, dtype=torch.float64)
+        calib = torch.full((self.CALIB_BINS,), float(top), dtype=torch.float64, device=fv.device)
+        for i in range(self.CALIB_BINS):
+            m = b == i
+            if m.any():
+                calib[i] = err[m].max()
+        self.calib = calib * self.CALIB_SAFETY
+
+    def error_bound(self, feats, sig_l1):
+        """Calibrated bound on |predicted - accurate correction| of pairs (features, panel density l1)."""
+        return self.calib[self._bin(feats)] * sig_l1
 
     def in_range(self, feats):
         lo, hi = self.range
@@ -221,7 +257,8 @@ def learned_near_field(S, T, L: LearnedCorrection, r_trg: torch.Tensor, sigma: t
         o = torch.zeros(idx.numel(), dtype=torch.float64, device=xt.device)
         m.forward_dot(x, dens, pp[idx].contiguous(), o)
         preds.append(o + const[pp[idx]])
-    agree = (preds[0] - preds[1]).abs() <= tol
+    bound = L.error_bound(f[idx], sig.abs().sum(1)[pp[idx]])
+    agree = ((preds[0] - preds[1]).abs() <= tol) & (bound <= tol)
     acc_idx = idx[agree]
     out.index_add_(0, pt[acc_idx], 0.5 * (preds[0][agree] + preds[1][agree]))
     rej = torch.ones(pt.numel(), dtype=torch.bool, device=xt.device)
@@ -231,5 +268,6 @@ def learned_near_field(S, T, L: LearnedCorrection, r_trg: torch.Tensor, sigma: t
         S.near_correction(xt, sigma, (rt, rp), kernel, alpha, out=out, subtract_smooth=False)
     if stats is not None:
         stats.update(pairs=int(pt.numel()), candidates=int(ok.sum()), accepted=int(acc_idx.numel()),
-                     fallback=int(rt.numel()))
+                     fallback=int(rt.numel()),
+                     accepted_per_target=torch.bincount(pt[acc_idx], minlength=nt))
     return out

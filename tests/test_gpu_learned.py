@@ -60,3 +60,26 @@ def test_tight_tolerance_falls_back_to_plain_path(trained):
     out = learned_near_field(S, T, L, xt, sig, tol=1e-12, stats=st).cpu().numpy()
     assert st["fallback"] >= 0.99 * st["pairs"]
     assert np.abs(out - plain).max() / np.abs(plain).max() < 1e-8
+
+
+def test_calibrated_gate_bounds_the_error(trained):
+    """At a moderate tolerance the accepted pairs' calibrated bounds hold: each target's deviation
+    from the plain path stays below tol times its number of accepted pairs."""
+    torch, T, S, L, _ = trained
+    from sctl_gb300.learned import learned_near_field
+    from sctl_gb300.torus import pair_features
+    tg = T.targets(2000, seed=400)
+    xt = torch.from_numpy(tg["r_trg"]).cuda()
+    sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()
+    plain = S.evaluate(xt, sig).cpu().numpy()
+    assert L.calib is not None and bool((L.calib > 0).all())
+    accepted = {}
+    for tol in (1.0, 1e-1, 1e-3):
+        st = {}
+        out = learned_near_field(S, T, L, xt, sig, tol=tol, stats=st).cpu().numpy()
+        dev = np.abs(out - plain)
+        n_acc = st["accepted_per_target"].cpu().numpy()
+        assert st["accepted"] <= st["candidates"]
+        assert np.all(dev <= tol * n_acc + 1e-12 * np.abs(plain).max()), (tol, (dev - tol * n_acc).max())
+        accepted[tol] = st["accepted"]
+    assert accepted[1.0] > 0 and accepted[1.0] >= accepted[1e-1] >= accepted[1e-3], accepted
