@@ -273,6 +273,14 @@ int sctlgpu_near_matrix_apply(int k0, int k1, int64_t n_trg, const int64_t* trg_
                               const double* F, double* U, void* stream);
 
 /*
+ * Arithmetic of sctlgpu_panel_near_correction / sctlgpu_panel_near_weights for the whole
+ * process: SCTLGPU_MIXED (default; double-float error-free transformations on the FP32
+ * pipe, within ~1e-13 of the FP64 form) or SCTLGPU_F64.  Returns the previous mode, or
+ * SCTLGPU_ERR_INVALID_MODE.
+ */
+int sctlgpu_panel_arithmetic(int mode);
+
+/*
  * C[M x N] = act(A[M x K] . Bt[N x K]^T + bias) on the tcgen05 tensor cores: A and Bt
  * row-major BF16 (K contiguous, 16-byte aligned), FP32 accumulation in tensor memory,
  * act 0 = none, 1 = GELU (tanh form).  Outputs (any may be NULL, not all): C32 (FP32,

@@ -1,0 +1,409 @@
+// Double-float form of the near-singular panel quadrature (included by
+// panel_quad.cu inside its namespace; same algorithm and parameters as the
+// FP64 panel_near_kernel).  GB300's FP64 pipe is a small fraction of its FP32
+// pipe and the FP64 kernel is bound by it, so the quadrature runs here on
+// error-free transformations in FP32 (hi + lo pairs, ~2^-46 relative):
+//
+//  * the panel's node coordinates are stored relative to the target
+//    (x_s - x_t, formed in FP64 once per pair), so interpolated positions
+//    carry no cancellation and r = -(interpolated offset);
+//  * the box-acceptance test runs in FP32 (it is a threshold, not a result);
+//  * every accepted box: basis values at its Gauss points in double-float
+//    (barycentric formula, Newton-refined reciprocals), tensor-product
+//    interpolation of the 7 fields as 10-term double-float dot products, and
+//    per Gauss node the kernel times the area element from the unnormalised
+//    normal Xs x Xt: Laplace DxU (r . (Xs x Xt)) / r^3, Laplace FxU |Xs x Xt| / r
+//    -- no normalisation of n is needed;
+//  * per-lane double-float sums, combined in FP64 per pair.
+#pragma once
+
+namespace dfq {
+
+using sctlgpu::f2;
+using sctlgpu::two_prod;
+using sctlgpu::two_sum;
+
+__device__ __forceinline__ f2 norm(f2 x) {
+  const float s = x.h + x.l;
+  return {s, x.l - (s - x.h)};
+}
+__device__ __forceinline__ f2 neg(f2 x) { return {-x.h, -x.l}; }
+// Products keep the cross terms; sums are TwoSum on the high parts.
+__device__ __forceinline__ f2 mul(f2 a, f2 b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return {p, e};
+}
+__device__ __forceinline__ f2 mulf(f2 a, float b) {
+  const float p = a.h * b;
+  return {p, fmaf(a.l, b, fmaf(a.h, b, -p))};
+}
+__device__ __forceinline__ f2 add(f2 a, f2 b) {
+  const f2 s = two_sum(a.h, b.h);
+  return norm({s.h, s.l + a.l + b.l});
+}
+__device__ __forceinline__ f2 sub(f2 a, f2 b) { return add(a, neg(b)); }
+// acc += a * b, accumulator left unnormalised (normalise after a short sum).
+__device__ __forceinline__ void fma_acc(f2& acc, f2 a, f2 b) {
+  const f2 p = mul(a, b);
+  const f2 s = two_sum(acc.h, p.h);
+  acc = {s.h, acc.l + (s.l + p.l)};
+}
+// 1 / d: FP32 reciprocal refined by one Newton step on the double-float residual.
+__device__ __forceinline__ f2 rcp(f2 d) {
+  const float y = 1.0f / d.h;
+  float t = fmaf(-d.h, y, 1.0f);
+  t = fmaf(-d.l, y, t);
+  return norm({y, y * t});
+}
+__device__ __forceinline__ f2 from_double(double v) {
+  const float h = (float)v;
+  return {h, (float)(v - (double)h)};
+}
+__device__ __forceinline__ double to_double(f2 x) { return (double)x.h + (double)x.l; }
+// 1/sqrt(R) and its powers from the hardware estimate and one Newton step on
+// the exact residual rho = 1 - y0^2 R (|rho| ~ 2^-22): y = y0 (1 + rho/2).
+__device__ __forceinline__ f2 rsqrt(f2 R, float* rho_out, float* y0_out) {
+  float y0 = sctlgpu::rsqrt_seed(R.h);
+  y0 = R.h > 0.f ? y0 : 0.f;
+  const f2 q = two_prod(y0, y0);
+  float rho = fmaf(-q.h, R.h, 1.f);
+  rho = fmaf(-q.l, R.h, rho);
+  rho = fmaf(-q.h, R.l, rho);
+  *rho_out = rho;
+  *y0_out = y0;
+  return {y0, (0.5f * y0) * rho};
+}
+
+}  // namespace dfq
+
+// Per-warp shared state of the double-float kernel (same footprint as PanelWarpSmem).
+struct PanelWarpSmemDF {
+  f2 F[4][PQ_NODES];          // x_s - x_t (3 components) and sigma at the panel nodes
+  f2 Ls[PQ_GL][PQ_P], Lds[PQ_GL][PQ_P], Lt[PQ_GL][PQ_P], Ldt[PQ_GL][PQ_P];
+  f2 A[7][PQ_GL][PQ_P];
+  f2 Kd[PQ_GL][PQ_GL];
+  f2 T[PQ_GL][PQ_P];
+  f2 W[PQ_NODES];
+  float box[2][PQ_QUEUE][3];
+  float leaf[PQ_QUEUE][3];
+};
+
+__constant__ float c_ch_xf[PQ_P], c_ch_wf[PQ_P];          // FP32 copies for the box test
+__constant__ float c_gl_xh[PQ_GL], c_gl_xl[PQ_GL];        // Gauss-Legendre nodes, double-float
+__constant__ float c_gl_wh[PQ_GL], c_gl_wl[PQ_GL];        // and weights
+__constant__ float c_ch_xh[PQ_P], c_ch_xl[PQ_P];          // Chebyshev nodes, double-float
+__constant__ float c_ch_wh[PQ_P], c_ch_wl[PQ_P];          // barycentric weights, double-float
+
+// FP32 barycentric basis and derivative (box test only).
+__device__ __forceinline__ void basis_f32(float s, float (&l)[PQ_P], float (&d)[PQ_P]) {
+  int hit = -1;
+#pragma unroll
+  for (int a = 0; a < PQ_P; ++a)
+    if (s == c_ch_xf[a]) hit = a;
+  if (hit >= 0) {
+#pragma unroll
+    for (int a = 0; a < PQ_P; ++a) {
+      l[a] = (a == hit) ? 1.f : 0.f;
+      d[a] = 0.f;
+    }
+    float diag = 0.f;
+    const float xh = c_ch_xf[hit], iwh = 1.f / c_ch_wf[hit];
+#pragma unroll
+    for (int a = 0; a < PQ_P; ++a)
+      if (a != hit) {
+        d[a] = (c_ch_wf[a] * iwh) / (xh - c_ch_xf[a]);
+        diag -= d[a];
+      }
+#pragma unroll
+    for (int a = 0; a < PQ_P; ++a)
+      if (a == hit) d[a] = diag;
+    return;
+  }
+  float T = 0.f, U = 0.f, r[PQ_P], t[PQ_P];
+#pragma unroll
+  for (int a = 0; a < PQ_P; ++a) {
+    r[a] = 1.f / (s - c_ch_xf[a]);
+    t[a] = c_ch_wf[a] * r[a];
+    T += t[a];
+    U += t[a] * r[a];
+  }
+  const float iT = 1.f / T, UT = U * iT;
+#pragma unroll
+  for (int a = 0; a < PQ_P; ++a) {
+    l[a] = t[a] * iT;
+    d[a] = l[a] * (UT - r[a]);
+  }
+}
+
+// Double-float basis and derivative at s (s = bs + bz * g, g a Gauss node).
+__device__ __forceinline__ void basis_df(f2 s, f2 (&l)[PQ_P], f2 (&d)[PQ_P]) {
+  int hit = -1;
+#pragma unroll
+  for (int a = 0; a < PQ_P; ++a)
+    if (s.h == c_ch_xh[a] && s.l == c_ch_xl[a]) hit = a;
+  if (hit >= 0) {  // at a node: l is a unit vector, l' the differentiation-matrix row
+    f2 diag = {0.f, 0.f};
+    const f2 xh = {c_ch_xh[hit], c_ch_xl[hit]}, iwh = dfq::rcp({c_ch_wh[hit], c_ch_wl[hit]});
+#pragma unroll
+    for (int a = 0; a < PQ_P; ++a) {
+      l[a] = {(a == hit) ? 1.f : 0.f, 0.f};
+      d[a] = {0.f, 0.f};
+      if (a != hit) {
+        const f2 w = dfq::mul({c_ch_wh[a], c_ch_wl[a]}, iwh);
+        d[a] = dfq::mul(w, dfq::rcp(dfq::sub(xh, {c_ch_xh[a], c_ch_xl[a]})));
+        diag = dfq::sub(diag, d[a]);
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < PQ_P; ++a)
+      if (a == hit) d[a] = diag;
+    return;
+  }
+  f2 T = {0.f, 0.f}, U = {0.f, 0.f}, r[PQ_P];
+#pragma unroll
+  for (int a = 0; a < PQ_P; ++a) {
+    r[a] = dfq::rcp(dfq::sub(s, {c_ch_xh[a], c_ch_xl[a]}));
+    const f2 t = dfq::mul({c_ch_wh[a], c_ch_wl[a]}, r[a]);
+    l[a] = t;
+    T = dfq::add(T, t);
+    U = dfq::add(U, dfq::mul(t, r[a]));
+  }
+  const f2 iT = dfq::rcp(T), UT = dfq::mul(U, iT);
+#pragma unroll
+  for (int a = 0; a < PQ_P; ++a) {
+    l[a] = dfq::mul(l[a], iT);
+    d[a] = dfq::mul(l[a], dfq::sub(UT, r[a]));
+  }
+}
+
+template <int KER, bool WEIGHTS>
+__global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParams p) {
+  extern __shared__ __align__(16) unsigned char pq_smem_df[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  PanelWarpSmemDF& sm = reinterpret_cast<PanelWarpSmemDF*>(pq_smem_df)[warp];
+  for (int64_t pr = (int64_t)blockIdx.x * PQ_WARPS + warp; pr < p.n_pairs; pr += (int64_t)gridDim.x * PQ_WARPS) {
+    const int64_t tix = p.pair_trg[pr], pix = p.pair_panel[pr];
+    const int64_t oix = p.trg_map ? (tix >= 0 && tix < p.nt ? p.trg_map[tix] : -1) : tix;
+    if (tix < 0 || tix >= p.nt || pix < 0 || pix >= p.n_panels || oix < 0 || oix >= p.n_out) {
+      if (lane == 0 && p.status) atomicOr(p.status, 4u);
+      continue;
+    }
+    const double xt[3] = {p.r_trg[tix * 3], p.r_trg[tix * 3 + 1], p.r_trg[tix * 3 + 2]};
+    __syncwarp();
+    double acc_smooth = 0.0;
+    for (int q = lane; q < PQ_NODES; q += 32) {
+      const double* xq = p.X + (pix * PQ_NODES + q) * 3;
+      const double rx = xq[0] - xt[0], ry = xq[1] - xt[1], rz = xq[2] - xt[2];
+      sm.F[0][q] = dfq::from_double(rx);
+      sm.F[1][q] = dfq::from_double(ry);
+      sm.F[2][q] = dfq::from_double(rz);
+      if (!WEIGHTS) {
+        const double sg = p.sigma[pix * PQ_NODES + q];
+        sm.F[3][q] = dfq::from_double(sg);
+        if (p.subtract_smooth) {  // the panel's own smooth-rule part (FP64, once per pair)
+          const double r[3] = {-rx, -ry, -rz};
+          const double n[3] = {p.N[(pix * PQ_NODES + q) * 3], p.N[(pix * PQ_NODES + q) * 3 + 1],
+                               p.N[(pix * PQ_NODES + q) * 3 + 2]};
+          acc_smooth -= kernel_val<KER>(r, n) * sg * p.Q[pix * PQ_NODES + q];
+        }
+      } else {
+        sm.W[q] = {0.f, 0.f};
+      }
+    }
+    __syncwarp();
+    f2 acc = {0.f, 0.f};
+    int cur = 0, ncur = 1, nleaf = 0;
+    if (lane == 0) {
+      sm.box[0][0][0] = 0.0f;
+      sm.box[0][0][1] = 0.0f;
+      sm.box[0][0][2] = 1.0f;
+    }
+    __syncwarp();
+    for (int depth = 0; depth <= p.max_depth && ncur > 0; ++depth) {
+      int nnext = 0;
+      nleaf = 0;
+      for (int base = 0; base < ncur; base += 32) {
+        const int i = base + lane;
+        bool accept = false, valid = i < ncur;
+        float bs = 0, bt = 0, bz = 0;
+        if (valid) {
+          bs = sm.box[cur][i][0];
+          bt = sm.box[cur][i][1];
+          bz = sm.box[cur][i][2];
+          // FP32 interpolation of the offset and tangents at the box centre
+          float ls[PQ_P], ds[PQ_P], lt[PQ_P], dt[PQ_P];
+          basis_f32(bs + 0.5f * bz, ls, ds);
+          basis_f32(bt + 0.5f * bz, lt, dt);
+          float X[3], Xs[3], Xt[3];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            float v = 0.f, vs = 0.f, vt = 0.f;
+#pragma unroll
+            for (int a = 0; a < PQ_P; ++a) {
+              float r0 = 0.f, rt = 0.f;
+#pragma unroll
+              for (int b = 0; b < PQ_P; ++b) {
+                const float f = sm.F[c][a * PQ_P + b].h;
+                r0 = fmaf(lt[b], f, r0);
+                rt = fmaf(dt[b], f, rt);
+              }
+              v = fmaf(ls[a], r0, v);
+              vs = fmaf(ds[a], r0, vs);
+              vt = fmaf(ls[a], rt, vt);
+            }
+            X[c] = v;
+            Xs[c] = vs;
+            Xt[c] = vt;
+          }
+          const float sl = Xs[0] * Xs[0] + Xs[1] * Xs[1] + Xs[2] * Xs[2];
+          const float tl = Xt[0] * Xt[0] + Xt[1] * Xt[1] + Xt[2] * Xt[2];
+          const float diam = bz * sqrtf(sl + tl);
+          const float d = sqrtf(X[0] * X[0] + X[1] * X[1] + X[2] * X[2]);
+          accept = d >= (float)p.alpha * diam || depth == p.max_depth;
+        }
+        const unsigned acc_mask = __ballot_sync(0xffffffffu, valid && accept);
+        const unsigned ref_mask = __ballot_sync(0xffffffffu, valid && !accept);
+        const unsigned lt_mask = (1u << lane) - 1u;
+        if (valid && accept) {
+          const int slot = nleaf + __popc(acc_mask & lt_mask);
+          if (slot < PQ_QUEUE) {
+            sm.leaf[slot][0] = bs;
+            sm.leaf[slot][1] = bt;
+            sm.leaf[slot][2] = bz;
+          }
+        }
+        if (valid && !accept) {
+          const int slot = nnext + 4 * __popc(ref_mask & lt_mask);
+          const float h = 0.5f * bz;
+          for (int c = 0; c < 4; ++c)
+            if (slot + c < PQ_QUEUE) {
+              sm.box[cur ^ 1][slot + c][0] = bs + (c & 1) * h;
+              sm.box[cur ^ 1][slot + c][1] = bt + (c >> 1) * h;
+              sm.box[cur ^ 1][slot + c][2] = h;
+            }
+        }
+        nleaf = min(PQ_QUEUE, nleaf + __popc(acc_mask));
+        nnext = min(PQ_QUEUE, nnext + 4 * __popc(ref_mask));
+        if (nleaf >= PQ_QUEUE || nnext >= PQ_QUEUE) {
+          if (lane == 0 && p.status) atomicOr(p.status, 2u);
+        }
+      }
+      __syncwarp();
+      for (int lf = 0; lf < nleaf; ++lf) {
+        const float bs = sm.leaf[lf][0], bt = sm.leaf[lf][1], bz = sm.leaf[lf][2];
+        if (lane < 2 * PQ_GL) {
+          const int i = lane % PQ_GL;
+          // s = b0 + bz * g_i (b0, bz dyadic: exact floats)
+          const f2 g = {c_gl_xh[i], c_gl_xl[i]};
+          const f2 s = dfq::add({lane < PQ_GL ? bs : bt, 0.f}, dfq::mulf(g, bz));
+          f2 l[PQ_P], d[PQ_P];
+          basis_df(s, l, d);
+#pragma unroll
+          for (int a = 0; a < PQ_P; ++a) {
+            if (lane < PQ_GL) {
+              sm.Ls[i][a] = l[a];
+              sm.Lds[i][a] = d[a];
+            } else {
+              sm.Lt[i][a] = l[a];
+              sm.Ldt[i][a] = d[a];
+            }
+          }
+        }
+        __syncwarp();
+        for (int e = lane; e < 7 * PQ_GL * PQ_P; e += 32) {
+          const int m = e / (PQ_GL * PQ_P), i = (e / PQ_P) % PQ_GL, b = e % PQ_P;
+          if (WEIGHTS && m == 3) continue;  // no density in weights mode
+          const int c = m < 4 ? m : m - 4;
+          const f2* L = m < 4 ? sm.Ls[i] : sm.Lds[i];
+          f2 v = {0.f, 0.f};
+#pragma unroll
+          for (int a = 0; a < PQ_P; ++a) dfq::fma_acc(v, L[a], sm.F[c][a * PQ_P + b]);
+          sm.A[m][i][b] = dfq::norm(v);
+        }
+        __syncwarp();
+        const float bz2 = bz * bz;
+        for (int gq = lane; gq < PQ_GL * PQ_GL; gq += 32) {
+          const int i = gq / PQ_GL, j = gq % PQ_GL;
+          f2 X[3] = {}, Xs[3] = {}, Xt[3] = {}, sg = {0.f, 0.f};
+#pragma unroll
+          for (int b = 0; b < PQ_P; ++b) {
+            const f2 lt = sm.Lt[j][b], ldt = sm.Ldt[j][b];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              dfq::fma_acc(X[c], sm.A[c][i][b], lt);
+              dfq::fma_acc(Xt[c], sm.A[c][i][b], ldt);
+              dfq::fma_acc(Xs[c], sm.A[4 + c][i][b], lt);
+            }
+            if (!WEIGHTS) dfq::fma_acc(sg, sm.A[3][i][b], lt);
+          }
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            X[c] = dfq::norm(X[c]);  // X = x_s - x_t = -r
+            Xs[c] = dfq::norm(Xs[c]);
+            Xt[c] = dfq::norm(Xt[c]);
+          }
+          // unnormalised normal n = Xs x Xt (|n| = area element of the parameter square)
+          const f2 n0 = dfq::sub(dfq::mul(Xs[1], Xt[2]), dfq::mul(Xs[2], Xt[1]));
+          const f2 n1 = dfq::sub(dfq::mul(Xs[2], Xt[0]), dfq::mul(Xs[0], Xt[2]));
+          const f2 n2 = dfq::sub(dfq::mul(Xs[0], Xt[1]), dfq::mul(Xs[1], Xt[0]));
+          f2 R = dfq::add(dfq::add(dfq::mul(X[0], X[0]), dfq::mul(X[1], X[1])), dfq::mul(X[2], X[2]));
+          float rho, y0;
+          const f2 y = dfq::rsqrt(R, &rho, &y0);
+          const f2 w = dfq::mulf(dfq::mul({c_gl_wh[i], c_gl_wl[i]}, {c_gl_wh[j], c_gl_wl[j]}), bz2);
+          f2 kda;
+          if (KER == 0) {  // single layer: |n| / r
+            const f2 J2 = dfq::add(dfq::add(dfq::mul(n0, n0), dfq::mul(n1, n1)), dfq::mul(n2, n2));
+            const float jh = sqrtf(J2.h);
+            const f2 jp = two_prod(jh, jh);
+            const f2 J = dfq::norm({jh, jh > 0.f ? ((J2.h - jp.h - jp.l) + J2.l) / (2.f * jh) : 0.f});
+            kda = dfq::mul(dfq::mul(J, y), w);
+          } else {  // double layer: (r . n) / r^3 with r = -X
+            const f2 rn = dfq::neg(
+                dfq::add(dfq::add(dfq::mul(X[0], n0), dfq::mul(X[1], n1)), dfq::mul(X[2], n2)));
+            f2 y3 = dfq::mulf(two_prod(y0, y0), y0);  // y0^3 (1 + 3 rho / 2)
+            y3.l = fmaf(y3.h, 1.5f * rho, y3.l);
+            kda = dfq::mul(dfq::mul(rn, y3), w);
+          }
+          if (WEIGHTS)
+            sm.Kd[i][j] = dfq::norm(kda);
+          else
+            dfq::fma_acc(acc, kda, dfq::norm(sg));
+        }
+        __syncwarp();
+        if (WEIGHTS) {
+          for (int e = lane; e < PQ_GL * PQ_P; e += 32) {
+            const int i = e / PQ_P, b = e % PQ_P;
+            f2 v = {0.f, 0.f};
+#pragma unroll
+            for (int j = 0; j < PQ_GL; ++j) dfq::fma_acc(v, sm.Kd[i][j], sm.Lt[j][b]);
+            sm.T[i][b] = dfq::norm(v);
+          }
+          __syncwarp();
+          for (int e = lane; e < PQ_NODES; e += 32) {
+            const int a = e / PQ_P, b = e % PQ_P;
+            f2 v = sm.W[e];
+#pragma unroll
+            for (int i = 0; i < PQ_GL; ++i) dfq::fma_acc(v, sm.Ls[i][a], sm.T[i][b]);
+            sm.W[e] = dfq::norm(v);
+          }
+          __syncwarp();
+        }
+        acc = dfq::norm(acc);
+      }
+      cur ^= 1;
+      ncur = nnext;
+    }
+    if (WEIGHTS) {
+      __syncwarp();
+      for (int q = lane; q < PQ_NODES; q += 32) p.out[pr * PQ_NODES + q] = dfq::to_double(sm.W[q]) * p.scale;
+    } else {
+      double v = dfq::to_double(acc) + acc_smooth;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) atomicAdd(&p.out[oix], v * p.scale);
+    }
+  }
+}

@@ -20,7 +20,10 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "../../include/sctlgpu.h"
+#include "common.cuh"
 #include "launch.h"
 
 namespace sctlgpu {
@@ -343,6 +346,11 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel(PanelParams p
   }
 }
 
+#include "panel_df.cuh"
+
+// Arithmetic of the panel entries: SCTLGPU_MIXED (double-float, default) or SCTLGPU_F64.
+std::atomic<int> g_panel_mode{SCTLGPU_MIXED};
+
 // Gauss-Legendre nodes and weights on [0,1] (Newton iteration on P_n).
 void gauss_legendre01(int n, double* x, double* w) {
   const double pi = 3.14159265358979323846264338327950288;
@@ -380,11 +388,37 @@ int ensure_gl(int dev) {
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gl_w, gw, sizeof(gw));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_ch_x, cx, sizeof(cx));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_ch_w, cw, sizeof(cw));
+    // double-float (hi + lo) and FP32 copies for the double-float kernel
+    float gxh[PQ_GL], gxl[PQ_GL], gwh[PQ_GL], gwl[PQ_GL], cxh[PQ_P], cxl[PQ_P], cwh[PQ_P], cwl[PQ_P];
+    auto split = [](double v, float* h, float* l) {
+      *h = (float)v;
+      *l = (float)(v - (double)*h);
+    };
+    for (int i = 0; i < PQ_GL; ++i) {
+      split(gx[i], &gxh[i], &gxl[i]);
+      split(gw[i], &gwh[i], &gwl[i]);
+    }
+    for (int a = 0; a < PQ_P; ++a) {
+      split(cx[a], &cxh[a], &cxl[a]);
+      split(cw[a], &cwh[a], &cwl[a]);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gl_xh, gxh, sizeof(gxh));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gl_xl, gxl, sizeof(gxl));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gl_wh, gwh, sizeof(gwh));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gl_wl, gwl, sizeof(gwl));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_ch_xh, cxh, sizeof(cxh));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_ch_xl, cxl, sizeof(cxl));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_ch_wh, cwh, sizeof(cwh));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_ch_wl, cwl, sizeof(cwl));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_ch_xf, cxh, sizeof(cxh));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_ch_wf, cwh, sizeof(cwh));
     if (e != cudaSuccess) return runtime_record(e);
     have_gl[dev] = true;
   }
   return SCTLGPU_OK;
 }
+
+static_assert(sizeof(PanelWarpSmemDF) == sizeof(PanelWarpSmem), "same shared-memory footprint");
 
 int launch_panel(int kernel, bool weights, const PanelParams& p, unsigned grid, int dev, cudaStream_t st) {
   const size_t smem = PQ_WARPS * sizeof(PanelWarpSmem);
@@ -394,7 +428,26 @@ int launch_panel(int kernel, bool weights, const PanelParams& p, unsigned grid, 
     cudaFuncSetAttribute(panel_near_kernel<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(panel_near_kernel<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(panel_near_kernel<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(panel_near_kernel_df<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(panel_near_kernel_df<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(panel_near_kernel_df<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(panel_near_kernel_df<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr[dev] = true;
+  }
+  if (g_panel_mode.load() == SCTLGPU_MIXED) {
+    if (kernel == SCTLGPU_LAPLACE3D_FXU) {
+      if (weights)
+        panel_near_kernel_df<0, true><<<grid, 32 * PQ_WARPS, smem, st>>>(p);
+      else
+        panel_near_kernel_df<0, false><<<grid, 32 * PQ_WARPS, smem, st>>>(p);
+    } else {
+      if (weights)
+        panel_near_kernel_df<1, true><<<grid, 32 * PQ_WARPS, smem, st>>>(p);
+      else
+        panel_near_kernel_df<1, false><<<grid, 32 * PQ_WARPS, smem, st>>>(p);
+    }
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return runtime_record(cudaGetLastError());
   }
   if (kernel == SCTLGPU_LAPLACE3D_FXU) {
     if (weights)
@@ -491,4 +544,9 @@ extern "C" int sctlgpu_panel_near_weights(int kernel, int64_t n_pairs, const int
   const int64_t ctas = (n_pairs + PQ_WARPS - 1) / PQ_WARPS;
   const unsigned grid = (unsigned)(ctas < (int64_t)sms * 16 ? ctas : (int64_t)sms * 16);
   return launch_panel(kernel, true, p, grid, dev, (cudaStream_t)stream);
+}
+
+extern "C" int sctlgpu_panel_arithmetic(int mode) {
+  if (mode != SCTLGPU_F64 && mode != SCTLGPU_MIXED) return SCTLGPU_ERR_INVALID_MODE;
+  return g_panel_mode.exchange(mode);
 }

@@ -136,3 +136,30 @@ def test_near_matrix_apply_general_layout(cuda, k0, k1):
     np.testing.assert_allclose(got, want, rtol=1e-13, atol=1e-13)
     np.testing.assert_array_equal(got[(nt - 5) * k1:], U0[(nt - 5) * k1:])
     assert capi.load().sctlgpu_device_status(None) == capi.OK
+
+
+@pytest.mark.parametrize("kernel", [0, 1])
+def test_double_float_panel_quadrature_matches_fp64(setup, kernel):
+    """The default double-float panel kernel against the FP64 one: corrections (with the smooth
+    part subtracted in-kernel) and weights agree far below the quadrature's own error."""
+    torch, T, S = setup
+    from sctl_gb300 import capi
+    from sctl_gb300.learned import panel_weights
+    lib = capi.load()
+    tg = T.targets(1500, seed=18, hmin=1e-4, hmax=1.0)
+    xt = torch.from_numpy(tg["r_trg"]).cuda().reshape(-1).contiguous()
+    pairs = S.near_pairs(xt, 1.0)
+    sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()
+    res = {}
+    for mode in (capi.F64, capi.MIXED):
+        prev = lib.sctlgpu_panel_arithmetic(mode)
+        try:
+            c = S.near_correction(xt, sig, pairs, kernel=kernel).cpu().numpy()
+            w = panel_weights(kernel, pairs[0][:3000].contiguous(), pairs[1][:3000].contiguous(), xt, S.X)
+            res[mode] = (c, w.cpu().numpy())
+        finally:
+            lib.sctlgpu_panel_arithmetic(prev)
+    (c64, w64), (cdf, wdf) = res[capi.F64], res[capi.MIXED]
+    assert np.abs(cdf - c64).max() <= 1e-11 * np.abs(c64).max(), np.abs(cdf - c64).max() / np.abs(c64).max()
+    assert np.abs(wdf - w64).max() <= 1e-11 * np.abs(w64).max()
+    assert lib.sctlgpu_device_status(None) == capi.OK
