@@ -17,6 +17,8 @@
 //  * per-lane double-float sums, combined in FP64 per pair.
 #pragma once
 
+#include <type_traits>
+
 namespace dfq {
 
 using sctlgpu::f2;
@@ -79,17 +81,24 @@ __device__ __forceinline__ f2 rsqrt(f2 R, float* rho_out, float* y0_out) {
 
 }  // namespace dfq
 
-// Per-warp shared state of the double-float kernel (same footprint as PanelWarpSmem).
+// Per-warp shared state of the double-float kernel.  All boxes of one round
+// have the same size (2^-depth), so only their corners are queued; the
+// weights-mode arrays exist only in the weights-mode layout (smaller footprint
+// = more resident warps for the potential mode).
 struct PanelWarpSmemDF {
   f2 F[4][PQ_NODES];          // x_s - x_t (3 components) and sigma at the panel nodes
   f2 Ls[PQ_GL][PQ_P], Lds[PQ_GL][PQ_P], Lt[PQ_GL][PQ_P], Ldt[PQ_GL][PQ_P];
   f2 A[7][PQ_GL][PQ_P];
+  float box[2][PQ_QUEUE][2];  // (s0, t0) of the boxes of this and the next round (dyadic: exact)
+  float leaf[PQ_QUEUE][2];
+};
+struct PanelWarpSmemDFW : PanelWarpSmemDF {
   f2 Kd[PQ_GL][PQ_GL];
   f2 T[PQ_GL][PQ_P];
   f2 W[PQ_NODES];
-  float box[2][PQ_QUEUE][3];
-  float leaf[PQ_QUEUE][3];
 };
+template <bool WEIGHTS>
+using DFSmem = typename std::conditional<WEIGHTS, PanelWarpSmemDFW, PanelWarpSmemDF>::type;
 
 __constant__ float c_ch_xf[PQ_P], c_ch_wf[PQ_P];          // FP32 copies for the box test
 __constant__ float c_gl_xh[PQ_GL], c_gl_xl[PQ_GL];        // Gauss-Legendre nodes, double-float
@@ -183,7 +192,7 @@ template <int KER, bool WEIGHTS>
 __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParams p) {
   extern __shared__ __align__(16) unsigned char pq_smem_df[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  PanelWarpSmemDF& sm = reinterpret_cast<PanelWarpSmemDF*>(pq_smem_df)[warp];
+  DFSmem<WEIGHTS>& sm = reinterpret_cast<DFSmem<WEIGHTS>*>(pq_smem_df)[warp];
   for (int64_t pr = (int64_t)blockIdx.x * PQ_WARPS + warp; pr < p.n_pairs; pr += (int64_t)gridDim.x * PQ_WARPS) {
     const int64_t tix = p.pair_trg[pr], pix = p.pair_panel[pr];
     const int64_t oix = p.trg_map ? (tix >= 0 && tix < p.nt ? p.trg_map[tix] : -1) : tix;
@@ -210,7 +219,7 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
           acc_smooth -= kernel_val<KER>(r, n) * sg * p.Q[pix * PQ_NODES + q];
         }
       } else {
-        sm.W[q] = {0.f, 0.f};
+        if constexpr (WEIGHTS) sm.W[q] = {0.f, 0.f};
       }
     }
     __syncwarp();
@@ -219,20 +228,19 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
     if (lane == 0) {
       sm.box[0][0][0] = 0.0f;
       sm.box[0][0][1] = 0.0f;
-      sm.box[0][0][2] = 1.0f;
     }
     __syncwarp();
     for (int depth = 0; depth <= p.max_depth && ncur > 0; ++depth) {
       int nnext = 0;
       nleaf = 0;
+      const float bz = ldexpf(1.0f, -depth);  // every box of this round has this size
       for (int base = 0; base < ncur; base += 32) {
         const int i = base + lane;
         bool accept = false, valid = i < ncur;
-        float bs = 0, bt = 0, bz = 0;
+        float bs = 0, bt = 0;
         if (valid) {
           bs = sm.box[cur][i][0];
           bt = sm.box[cur][i][1];
-          bz = sm.box[cur][i][2];
           // FP32 interpolation of the offset and tangents at the box centre
           float ls[PQ_P], ds[PQ_P], lt[PQ_P], dt[PQ_P];
           basis_f32(bs + 0.5f * bz, ls, ds);
@@ -272,7 +280,6 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
           if (slot < PQ_QUEUE) {
             sm.leaf[slot][0] = bs;
             sm.leaf[slot][1] = bt;
-            sm.leaf[slot][2] = bz;
           }
         }
         if (valid && !accept) {
@@ -282,7 +289,6 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
             if (slot + c < PQ_QUEUE) {
               sm.box[cur ^ 1][slot + c][0] = bs + (c & 1) * h;
               sm.box[cur ^ 1][slot + c][1] = bt + (c >> 1) * h;
-              sm.box[cur ^ 1][slot + c][2] = h;
             }
         }
         nleaf = min(PQ_QUEUE, nleaf + __popc(acc_mask));
@@ -293,7 +299,7 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
       }
       __syncwarp();
       for (int lf = 0; lf < nleaf; ++lf) {
-        const float bs = sm.leaf[lf][0], bt = sm.leaf[lf][1], bz = sm.leaf[lf][2];
+        const float bs = sm.leaf[lf][0], bt = sm.leaf[lf][1];
         if (lane < 2 * PQ_GL) {
           const int i = lane % PQ_GL;
           // s = b0 + bz * g_i (b0, bz dyadic: exact floats)
@@ -367,13 +373,13 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
             y3.l = fmaf(y3.h, 1.5f * rho, y3.l);
             kda = dfq::mul(dfq::mul(rn, y3), w);
           }
-          if (WEIGHTS)
+          if constexpr (WEIGHTS)
             sm.Kd[i][j] = dfq::norm(kda);
           else
             dfq::fma_acc(acc, kda, dfq::norm(sg));
         }
         __syncwarp();
-        if (WEIGHTS) {
+        if constexpr (WEIGHTS) {
           for (int e = lane; e < PQ_GL * PQ_P; e += 32) {
             const int i = e / PQ_P, b = e % PQ_P;
             f2 v = {0.f, 0.f};
@@ -396,7 +402,7 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
       cur ^= 1;
       ncur = nnext;
     }
-    if (WEIGHTS) {
+    if constexpr (WEIGHTS) {
       __syncwarp();
       for (int q = lane; q < PQ_NODES; q += 32) p.out[pr * PQ_NODES + q] = dfq::to_double(sm.W[q]) * p.scale;
     } else {

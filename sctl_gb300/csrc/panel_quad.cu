@@ -418,33 +418,32 @@ int ensure_gl(int dev) {
   return SCTLGPU_OK;
 }
 
-static_assert(sizeof(PanelWarpSmemDF) == sizeof(PanelWarpSmem), "same shared-memory footprint");
-
 int launch_panel(int kernel, bool weights, const PanelParams& p, unsigned grid, int dev, cudaStream_t st) {
   const size_t smem = PQ_WARPS * sizeof(PanelWarpSmem);
+  const size_t smem_p = PQ_WARPS * sizeof(PanelWarpSmemDF), smem_w = PQ_WARPS * sizeof(PanelWarpSmemDFW);
   static bool attr[64] = {};
   if (!attr[dev]) {
     cudaFuncSetAttribute(panel_near_kernel<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(panel_near_kernel<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(panel_near_kernel<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(panel_near_kernel<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(panel_near_kernel_df<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(panel_near_kernel_df<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(panel_near_kernel_df<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(panel_near_kernel_df<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(panel_near_kernel_df<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p);
+    cudaFuncSetAttribute(panel_near_kernel_df<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p);
+    cudaFuncSetAttribute(panel_near_kernel_df<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_w);
+    cudaFuncSetAttribute(panel_near_kernel_df<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_w);
     attr[dev] = true;
   }
   if (g_panel_mode.load() == SCTLGPU_MIXED) {
     if (kernel == SCTLGPU_LAPLACE3D_FXU) {
       if (weights)
-        panel_near_kernel_df<0, true><<<grid, 32 * PQ_WARPS, smem, st>>>(p);
+        panel_near_kernel_df<0, true><<<grid, 32 * PQ_WARPS, smem_w, st>>>(p);
       else
-        panel_near_kernel_df<0, false><<<grid, 32 * PQ_WARPS, smem, st>>>(p);
+        panel_near_kernel_df<0, false><<<grid, 32 * PQ_WARPS, smem_p, st>>>(p);
     } else {
       if (weights)
-        panel_near_kernel_df<1, true><<<grid, 32 * PQ_WARPS, smem, st>>>(p);
+        panel_near_kernel_df<1, true><<<grid, 32 * PQ_WARPS, smem_w, st>>>(p);
       else
-        panel_near_kernel_df<1, false><<<grid, 32 * PQ_WARPS, smem, st>>>(p);
+        panel_near_kernel_df<1, false><<<grid, 32 * PQ_WARPS, smem_p, st>>>(p);
     }
     g_launches.fetch_add(1, std::memory_order_relaxed);
     return runtime_record(cudaGetLastError());
