@@ -2,11 +2,12 @@
  * CPU oracle for the particle-kernel direct sums -- TEST INFRASTRUCTURE ONLY.
  *
  * A plain-C restatement of SCTL's GenericKernel::Eval / KernelMatrix for the
- * Laplace3D_FxU, Laplace3D_DxU, Stokes3D_FxU and Stokes3D_DxU micro-kernels
- * (reference: include/sctl/generic-kernel.txx:102-211 and :213-329,
- * include/sctl/kernel_functions.hpp:32-218).  It is the checker for the CUDA
- * path and the timed CPU baseline ("port"); nothing in the product library
- * links or calls it.  It is pinned against outputs of the reference itself
+ * micro-kernels of include/sctl/kernel_functions.hpp (the four hot-path ones,
+ * include/sctl/generic-kernel.txx:102-211 and :213-329, kernel_functions.hpp:
+ * 32-218, and the other twelve, :81-659) and of BuildNearList's near test.
+ * The CUDA path's results are compared against it in the tests, and it is the
+ * timed CPU baseline ("port"); nothing in the product library links or calls
+ * it.  It is pinned against outputs of the reference itself
  * (fixtures under tests/golden/, generated by tests/golden/make_golden.py from
  * the reference headers) and against the reference's known-answer tests
  * (src/test-kernel_functions.cpp:36-132, src/test-generic-kernel.cpp:55-103).
