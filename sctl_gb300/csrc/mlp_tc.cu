@@ -164,7 +164,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 0 && lane == 0) {  // producer
+  // Role lanes run alone; the rest of their warp waits at __syncwarp (not on an mbarrier
+  // try_wait, which would suspend the warp the role lane runs in).
+  if (warp == 0) {
+    if (lane == 0) {  // producer
     int issued = 0;
     for (int i = 0; i < nk; ++i) {
       const int s = i % nst;
@@ -182,7 +185,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // Copies still in flight (only after a timeout): let them land before the CTA exits.
     for (int i = max(0, issued - nst); i < issued; ++i)
       mbar_wait_bounded(&full[i % nst], (uint32_t)((i / nst) & 1), nullptr);
-  } else if (warp == 1 && lane == 0) {  // MMA issuer
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
     const uint32_t idesc = idesc_bf16(TC_M, p.N);
     for (int i = 0; i < nk; ++i) {
       const int s = i % nst;
@@ -198,6 +204,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       tc_commit(&empty[s]);
     }
     tc_commit(done);  // tracks every MMA issued above (arrives at once if none)
+    }
+    __syncwarp();
   }
   if (!mbar_wait_bounded(done, 0, p.status)) atomicExch(s_err, 1);
   if (tid == 32) {  // the MMA thread's last commits to the stage barriers have landed too
