@@ -37,7 +37,7 @@ namespace {
 
 constexpr int TC_M = 128, TC_KC = 64, TC_THREADS = 128;
 constexpr int TC_A_BYTES = TC_M * TC_KC * 2;  // 16 KB per chunk
-constexpr int TC_SMEM_BUDGET = 200 * 1024;     // stage ring
+constexpr int TC_SMEM_BUDGET = 100 * 1024;     // stage ring (two CTAs per SM: one drains its tile while the other computes)
 
 // tcgen05 shared-memory matrix descriptor for a K-major tile written by TMA
 // with 128-byte swizzle: start >> 4 in [0,14), leading byte offset (unused
@@ -128,7 +128,7 @@ struct TcParams {
   int stages;
 };
 
-__global__ void __launch_bounds__(TC_THREADS, 1)
+__global__ void __launch_bounds__(TC_THREADS, 2)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, TcParams p) {
   extern __shared__ unsigned char tsm_raw[];
   unsigned char* tsm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tsm_raw) + 1023) & ~(uintptr_t)1023);
