@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
   extern __shared__ __align__(16) unsigned char pq_smem_df[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   DFSmem<WEIGHTS>& sm = reinterpret_cast<DFSmem<WEIGHTS>*>(pq_smem_df)[warp];
-  for (int64_t pr = (int64_t)blockIdx.x * PQ_WARPS + warp; pr < p.n_pairs; pr += (int64_t)gridDim.x * PQ_WARPS) {
+  for (int64_t pr = next_pair(p, lane); pr < p.n_pairs; pr = next_pair(p, lane)) {
     const int64_t tix = p.pair_trg[pr], pix = p.pair_panel[pr];
     const int64_t oix = p.trg_map ? (tix >= 0 && tix < p.nt ? p.trg_map[tix] : -1) : tix;
     if (tix < 0 || tix >= p.nt || pix < 0 || pix >= p.n_panels || oix < 0 || oix >= p.n_out) {

@@ -158,7 +158,16 @@ struct PanelParams {
   double scale;
   double* out;
   unsigned* status;
+  unsigned long long* next;  // work queue head: the next pair a warp takes
 };
+
+// The next (target, panel) pair for this warp: pairs are taken from a device
+// counter as warps finish (their costs differ by orders of magnitude).
+__device__ __forceinline__ int64_t next_pair(const PanelParams& p, int lane) {
+  unsigned long long v = 0;
+  if (lane == 0) v = atomicAdd(p.next, 1ull);
+  return (int64_t)__shfl_sync(0xffffffffu, v, 0);
+}
 
 // WEIGHTS = false: potential correction added into out[target].  WEIGHTS =
 // true: the accurate weights W_ab = int_P K(x_t - y) l_a(s) l_b(t) dA(y) of the
@@ -169,7 +178,7 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel(PanelParams p
   extern __shared__ __align__(16) unsigned char pq_smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   PanelWarpSmem& sm = reinterpret_cast<PanelWarpSmem*>(pq_smem)[warp];
-  for (int64_t pr = (int64_t)blockIdx.x * PQ_WARPS + warp; pr < p.n_pairs; pr += (int64_t)gridDim.x * PQ_WARPS) {
+  for (int64_t pr = next_pair(p, lane); pr < p.n_pairs; pr = next_pair(p, lane)) {
     const int64_t tix = p.pair_trg[pr], pix = p.pair_panel[pr];
     const int64_t oix = p.trg_map ? (tix >= 0 && tix < p.nt ? p.trg_map[tix] : -1) : tix;
     if (tix < 0 || tix >= p.nt || pix < 0 || pix >= p.n_panels || oix < 0 || oix >= p.n_out) {
@@ -418,7 +427,19 @@ int ensure_gl(int dev) {
   return SCTLGPU_OK;
 }
 
-int launch_panel(int kernel, bool weights, const PanelParams& p, unsigned grid, int dev, cudaStream_t st) {
+int launch_panel_kernels(int kernel, bool weights, const PanelParams& p, unsigned grid, int dev, cudaStream_t st);
+
+int launch_panel(int kernel, bool weights, const PanelParams& p0, unsigned grid, int dev, cudaStream_t st) {
+  PanelParams p = p0;
+  cudaError_t qe = cudaMallocAsync((void**)&p.next, sizeof(unsigned long long), st);
+  if (qe == cudaSuccess) qe = cudaMemsetAsync(p.next, 0, sizeof(unsigned long long), st);
+  if (qe != cudaSuccess) return runtime_record(qe);
+  const int rc = launch_panel_kernels(kernel, weights, p, grid, dev, st);
+  const cudaError_t fe = cudaFreeAsync(p.next, st);
+  return rc != SCTLGPU_OK ? rc : runtime_record(fe);
+}
+
+int launch_panel_kernels(int kernel, bool weights, const PanelParams& p, unsigned grid, int dev, cudaStream_t st) {
   const size_t smem = PQ_WARPS * sizeof(PanelWarpSmem);
   const size_t smem_p = PQ_WARPS * sizeof(PanelWarpSmemDF), smem_w = PQ_WARPS * sizeof(PanelWarpSmemDFW);
   static bool attr[64] = {};
