@@ -202,6 +202,26 @@ def test_large_sources_subset_of_targets(cuda, k):
         assert O.rel_l2(run(k, d, mode, digits), ref) < tol
 
 
+def test_packed_records_beyond_2gib(cuda):
+    """2^25 Stokes3D_DxU sources: the packed double-float records (80 B each, 2.7 GB) and the FP64
+    records are addressed past 2^31 bytes; 64-bit offsets in the pack, tile and slice arithmetic."""
+    torch = cuda
+    k, ns, nt = 3, 1 << 25, 96
+    rng = np.random.default_rng(21)
+    xs = rng.normal(size=(ns, 3))
+    xs /= np.linalg.norm(xs, axis=1, keepdims=True)
+    xt = rng.uniform(-1.5, 1.5, (nt, 3))
+    f = rng.normal(size=ns * 3)
+    dev = [torch.from_numpy(np.ascontiguousarray(a).reshape(-1)).cuda() for a in (xt, xs, xs, f)]
+    ref = O.eval(k, xt[:16], xs, xs, f)
+    for mode, digits, tol in (("mixed", 10, 1e-10), ("f64", -1, 1e-12)):
+        out = S.Stokes3D_DxU.Eval(None, dev[0], dev[1], dev[2], dev[3], digits=digits, mode=mode)
+        torch.cuda.synchronize()
+        assert O.rel_l2(out.cpu().numpy()[:16 * 3], ref) < tol, mode
+    del dev
+    torch.cuda.empty_cache()
+
+
 @pytest.mark.parametrize("k", [0, 2])
 def test_clusters_precision_stress(cuda, k):
     d = W.clusters(1 << 14, 512, k, 0)
