@@ -256,6 +256,37 @@ def cube_section(torch, stream):
             "rel_l2_vs_cpu": O.rel_l2(gpu, ref)}
 
 
+def kmat_section(torch, stream):
+    """KernelMatrix (SetupNear's per-block matrices) for a large near block: 2048 targets x 6400
+    sources, Stokes3D_FxU and Laplace3D_DxU, FP64 / mixed (double-float entries) / FP32; written
+    bytes per second against the measured HBM bandwidth, and the mixed entries against FP64."""
+    import sctl_gb300 as S
+    from sctl_gb300 import workloads as W
+    hbm = peaks().get("hbm_gbs", 6800.0)
+    res = {"workload": "2048 targets x 6400 sources (sphere/ball points), matrices written to HBM"}
+    for k, kern in ((2, S.Stokes3D_FxU), (1, S.Laplace3D_DxU)):
+        d = W.sphere_ball(6400, 2048, k, seed=11)
+        row = {}
+        ref = None
+        for mode in ("f64", "mixed", "f32"):
+            dt = torch.float32 if mode == "f32" else torch.float64
+            dd = [torch.from_numpy(np.ascontiguousarray(d[a])).to(dt).cuda() for a in ("r_trg", "r_src", "n_src")]
+            run = lambda: kern.KernelMatrix(dd[0], dd[1], dd[2], digits=-1 if mode != "mixed" else 10,  # noqa: E731
+                                            mode=mode)
+            M = run()
+            ms = _ev_ms(torch, run, reps=3)
+            nbytes = M.numel() * M.element_size()
+            row[mode] = {"ms": ms, "gb_s": nbytes / (ms * 1e-3) / 1e9,
+                         "frac_of_measured_hbm": nbytes / (ms * 1e-3) / 1e9 / hbm}
+            if mode == "f64":
+                ref = M
+            elif mode == "mixed":
+                row[mode]["max_rel_vs_f64"] = ((M - ref).abs().max() / ref.abs().max()).item()
+            del M
+        res[NAMES[k]] = row
+    return res
+
+
 def ext_section(torch, stream, nt=1 << 16, ns=1 << 18):
     """The twelve micro-kernels beyond the hot-path four: FP64 and FP32 direct sums of 2^16 targets x
     2^18 sources (uniform in [-1,1]^3, N(0,1) densities, wavenumber 2.5), Ginteractions/s, and the
@@ -437,7 +468,7 @@ def main():
     ap.add_argument("--kernels", default="1,2,3", help="kernel ids of the step (default: the three sphere/ball kernels)")
     ap.add_argument("--quick", action="store_true", help="timed region only (for profiler runs)")
     ap.add_argument("--skip-torus", action="store_true", help="omit the near-singular torus section")
-    ap.add_argument("--section", choices=["near", "clusters", "cube", "torus", "torus_plain", "mlp", "ext"],
+    ap.add_argument("--section", choices=["near", "clusters", "cube", "torus", "torus_plain", "mlp", "ext", "kmat"],
                     help="run only this secondary workload and print its JSON (profiling of one kernel family)")
     ap.add_argument("--torus-n", type=int, default=1 << 16, help="targets of the torus section")
     args = ap.parse_args()
@@ -451,7 +482,7 @@ def main():
         stream = torch.cuda.current_stream()
         fn = {"near": lambda: near_field_section(torch, stream), "clusters": lambda: cluster_section(torch, stream),
               "cube": lambda: cube_section(torch, stream), "mlp": lambda: mlp_section(torch, stream),
-              "ext": lambda: ext_section(torch, stream),
+              "ext": lambda: ext_section(torch, stream), "kmat": lambda: kmat_section(torch, stream),
               "torus": lambda: torus_section(torch, n_eval=args.torus_n),
               "torus_plain": lambda: torus_section(torch, n_eval=args.torus_n, learned=False)}[args.section]
         print(json.dumps({"section": args.section, **fn()}), flush=True)
@@ -624,6 +655,7 @@ def main():
         extras["cube8192_fp64_d14"] = cube_section(torch, stream)
         extras["tensor_core_mlp"] = mlp_section(torch, stream)
         extras["other_micro_kernels"] = ext_section(torch, stream)
+        extras["kernel_matrix"] = kmat_section(torch, stream)
         if not args.skip_torus:
             extras["torus_near_singular"] = torus_section(torch)
 

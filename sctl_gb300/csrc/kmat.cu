@@ -47,13 +47,5 @@ cudaError_t kmat_f32(const KmatCall& c, int newton) {
   }
 }
 
-cudaError_t kmat_mixed_df(const KmatCall& c) {
-  BBox* bb = nullptr;
-  SCTLGPU_TRY(cudaMallocAsync((void**)&bb, 256, c.stream));
-  cudaError_t err = compute_bbox(c.stream, c.nt, (const double*)c.r_trg, c.ns, (const double*)c.r_src, bb);
-  if (err == cudaSuccess) err = kmat_dispatch<MODE_MXDF, double, 1>(c, bb);
-  cudaError_t e2 = cudaFreeAsync(bb, c.stream);
-  return err != cudaSuccess ? err : e2;
-}
 
 }  // namespace sctlgpu
