@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
         for (int gq = lane; gq < PQ_GL * PQ_GL; gq += 32) {
           const int i = gq / PQ_GL, j = gq % PQ_GL;
           f2 X[3] = {}, Xs[3] = {}, Xt[3] = {}, sg = {0.f, 0.f};
-#pragma unroll
+#pragma unroll 2
           for (int b = 0; b < PQ_P; ++b) {
             const f2 lt = sm.Lt[j][b], ldt = sm.Ldt[j][b];
 #pragma unroll
