@@ -370,14 +370,14 @@ def mlp_section(torch, stream):
     return res
 
 
-def torus_section(torch, n_eval=1 << 16, n_train=48000, steps=2000, learned=True):
+def torus_section(torch, n_eval=1 << 20, n_train=440000, steps=4000, learned=True):
     """Near-singular Laplace double layer on the 64 x 32-panel torus (204,800 nodes): plain path
     (far field + smooth subtraction + adaptive panel corrections) vs the learned path (two
-    tcgen05 networks, gated, plain-path fallback).  n_eval targets stand in for the 2^20 of the
-    workload (cost is linear in targets); labels from n_train targets' near pairs."""
+    tcgen05 networks, gated, plain-path fallback) at n_eval targets; labels from the near pairs
+    of n_train other targets (440,000 targets give about 2^22 weight sets)."""
     from sctl_gb300.learned import LearnedCorrection, learned_near_field, panel_weights
     from sctl_gb300.nearquad import PanelSurface
-    from sctl_gb300.torus import Torus, pair_features
+    from sctl_gb300.torus import Torus, pair_features_device
     T = Torus(seed=0)
     S = PanelSurface(T.X, T.N, T.Q, T.size)
     res = {"workload": f"torus R=1 r=0.3, 64x32 panels x 10x10 Chebyshev nodes, {n_eval} targets at h in "
@@ -438,12 +438,17 @@ def torus_section(torch, n_eval=1 << 16, n_train=48000, steps=2000, learned=True
     torch.cuda.synchronize()
     res["labels"] = int(pt.numel())
     res["label_s"] = time.perf_counter() - t0
-    f = torch.from_numpy(pair_features(T, tt["r_trg"], pt.cpu().numpy(), pp.cpu().numpy())).cuda()
-    L = LearnedCorrection(max_batch=1 << 14)
+    f = pair_features_device(T, xtr, pt, pp)
+    L = LearnedCorrection(max_batch=1 << 14, singular=T)
     t0 = time.perf_counter()
     res["train_losses"] = L.fit(f, W, steps=steps, batch=1 << 14, lr=3e-3)
     torch.cuda.synchronize()
     res["train_s"] = time.perf_counter() - t0
+    del f, W
+    # held-out calibration (ensemble mean, max over nodes and pairs, x2) per |log distance| bin;
+    # bins are 1/16 of [1e-6, 1] panel sizes in log10, the labels cover bins 5-15
+    res["held_out_max_weight_err_by_bin"] = [float(f"{x:.3g}") for x in L.calib.tolist()]
+    res["held_out_max_weight_sum_err_by_bin"] = [float(f"{x:.3g}") for x in L.calib_sum.tolist()]
     for tol in (1e-8, 1e-3, 1e-1):
         st = {}
         out = learned_near_field(S, T, L, xt, sig, tol, pairs=pairs, plan=plan, stats=st)
@@ -470,7 +475,7 @@ def main():
     ap.add_argument("--skip-torus", action="store_true", help="omit the near-singular torus section")
     ap.add_argument("--section", choices=["near", "clusters", "cube", "torus", "torus_plain", "mlp", "ext", "kmat"],
                     help="run only this secondary workload and print its JSON (profiling of one kernel family)")
-    ap.add_argument("--torus-n", type=int, default=1 << 16, help="targets of the torus section")
+    ap.add_argument("--torus-n", type=int, default=1 << 20, help="targets of the torus section")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

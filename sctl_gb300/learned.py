@@ -6,12 +6,14 @@ features; the pair's correction is then sum_ab (W_ab - W^smooth_ab) sigma_ab.
 * Labels come from the adaptive quadrature (`sctlgpu_panel_near_weights`).
 * Training and inference run on the tcgen05 kernels of libsctlgpu
   (`sctlgpu_mlp_*`): BF16 weights and activations, FP32 accumulation.
+* The networks may learn the weights minus a known near-singular part (solid
+  angle x density frozen at the foot point, `torus.singular_part`).
 * Two networks trained from different seeds and a calibrated error model form
   the a-posteriori check: a pair is accepted only when it is inside the trained
   range, the networks' predicted corrections agree to the tolerance, and the
-  calibrated bound on its error -- the largest weight error seen on held-out
-  labels at its distance, times 2, times the panel's density l1 norm -- is
-  below the tolerance; every other pair takes the plain adaptive path.
+  calibrated bound on its error (held-out weight errors at its distance times
+  the panel density, see `LearnedCorrection.error_bound`) is below the
+  tolerance; every other pair takes the plain adaptive path.
 """
 from __future__ import annotations
 
@@ -151,16 +153,22 @@ class Standardizer:
 
 class LearnedCorrection:
     """Ensemble of correction networks with range gating, a disagreement check and an error model
-    calibrated on held-out labels."""
+    calibrated on held-out labels.
+
+    With `singular` (a surface with `singular_weights(f)` and `singular_dot(f, sig, pp)`, e.g. the
+    torus) the networks learn only the weights minus their known near-singular part (the jump and
+    the solid angle of the flat panel), a smoother function of the features; predictions add the
+    part back."""
 
     CALIB_BINS = 16  # bins of |signed log distance feature| in [0, 1]
     CALIB_SAFETY = 2.0
 
-    def __init__(self, n_models=2, max_batch=1 << 14, seeds=(1, 2)):
+    def __init__(self, n_models=2, max_batch=1 << 14, seeds=(1, 2), singular=None):
         self.models = [MLP(max_batch=max_batch, seed=s) for s in seeds[:n_models]]
+        self.singular = singular
         self.fx = self.fy = None
         self.range = None
-        self.calib = None
+        self.calib = self.calib_sum = None
 
     def fit(self, feats: torch.Tensor, w: torch.Tensor, steps=2000, batch=1 << 14, lr=2e-3, seed=0, log=None,
             val_frac=0.1):
@@ -172,9 +180,12 @@ class LearnedCorrection:
         val, trn = perm[:n_val], perm[n_val:]
         fv, wv = feats[val], w[val]
         feats, w = feats[trn], w[trn]
+        if self.singular is not None:
+            w = w - self.singular.singular_weights(feats)
         self.fx, self.fy = Standardizer(feats), Standardizer(w)
         self.range = (feats.min(0).values, feats.max(0).values)
         X, Y = self.fx.fwd(feats).contiguous(), self.fy.fwd(w).contiguous()
+        del w
         n = X.shape[0]
         losses = []
         for mi, m in enumerate(self.models):
@@ -196,31 +207,47 @@ class LearnedCorrection:
         return (feats[:, 2].abs().clamp(0, 1) * self.CALIB_BINS).long().clamp(max=self.CALIB_BINS - 1)
 
     def _calibrate(self, fv, wv):
-        """Largest max-norm weight error of the ensemble mean on held-out pairs, per distance bin
-        (bins without held-out pairs get the overall largest)."""
-        pred = self.predict(fv).mean(0)
-        err = (pred - wv).abs().max(1).values
+        """Per distance bin, on held-out pairs: the largest weight error of the ensemble mean
+        (max over nodes) and the largest error of its weight sum (bins without held-out pairs get
+        the overall largest), times the safety factor."""
+        pred = self.predict_weights(fv).mean(0)
+        e = pred - wv
         b = self._bin(fv)
-        top = err.max() if err.numel() else torch.tensor(float("inf"), device=fv.device, dtype=torch.float64)
-        calib = torch.full((self.CALIB_BINS,), float(top), dtype=torch.float64, device=fv.device)
-        for i in range(self.CALIB_BINS):
-            m = b == i
-            if m.any():
-                calib[i] = err[m].max()
-        self.calib = calib * self.CALIB_SAFETY
+        out = []
+        for err in (e.abs().max(1).values, e.sum(1).abs()):
+            top = err.max() if err.numel() else torch.tensor(float("inf"), device=fv.device, dtype=torch.float64)
+            c = torch.full((self.CALIB_BINS,), float(top), dtype=torch.float64, device=fv.device)
+            for i in range(self.CALIB_BINS):
+                m = b == i
+                if m.any():
+                    c[i] = err[m].max()
+            out.append(c * self.CALIB_SAFETY)
+        self.calib, self.calib_sum = out
 
-    def error_bound(self, feats, sig_l1):
-        """Calibrated bound on |predicted - accurate correction| of pairs (features, panel density l1)."""
-        return self.calib[self._bin(feats)] * sig_l1
+    def error_bound(self, feats, sig):
+        """Calibrated bound on |predicted - accurate correction| of pairs with features `feats` and
+        panel densities `sig` (n, 100): with e the weight errors and m the panel's mean density,
+        |e . sig| <= |sum e| |m| + max|e| sum|sig - m|, each factor from the calibration."""
+        b = self._bin(feats)
+        m = sig.mean(1)
+        return self.calib_sum[b] * m.abs() + self.calib[b] * (sig - m[:, None]).abs().sum(1)
 
     def in_range(self, feats):
         lo, hi = self.range
         return ((feats >= lo) & (feats <= hi)).all(1)
 
     def predict(self, feats: torch.Tensor):
-        """Per-model predicted accurate weights, (n_models, n, 100) FP64."""
+        """Per-model network outputs in weight units, (n_models, n, 100) FP64: the accurate weights,
+        or with `singular` the accurate weights minus their singular part."""
         x = self.fx.fwd(feats).contiguous()
         return torch.stack([self.fy.inv(m.forward(x)) for m in self.models])
+
+    def predict_weights(self, feats: torch.Tensor):
+        """Per-model predicted accurate weights, (n_models, n, 100) FP64."""
+        p = self.predict(feats)
+        if self.singular is not None:
+            p = p + self.singular.singular_weights(feats)[None]
+        return p
 
 
 def learned_near_field(S, T, L: LearnedCorrection, r_trg: torch.Tensor, sigma: torch.Tensor, tol: float,
@@ -230,7 +257,7 @@ def learned_near_field(S, T, L: LearnedCorrection, r_trg: torch.Tensor, sigma: t
     inside the panel and its distance below h_cut panel sizes -- elsewhere the smooth rule is already
     accurate and the network would only add its own error), inside the trained feature range, and the
     two networks agree to `tol`; the plain adaptive path for every other near pair."""
-    from .torus import pair_features
+    from .torus import pair_features_device
     xt = r_trg.reshape(-1).contiguous()
     nt = xt.numel() // 3
     out = S.far_field(xt, sigma, kernel, mode, digits)
@@ -242,11 +269,10 @@ def learned_near_field(S, T, L: LearnedCorrection, r_trg: torch.Tensor, sigma: t
     plan.execute(xt, S.X.reshape(-1), S.N.reshape(-1), sigma.reshape(-1).contiguous(), out, w_src=negq,
                  accumulate=True)
     pt, pp = pairs
-    f = torch.from_numpy(pair_features(T, xt.reshape(-1, 3).cpu().numpy(), pt.cpu().numpy(),
-                                       pp.cpu().numpy())).to(xt.device)
+    f = pair_features_device(T, xt, pt, pp)
     hfeat_cut = (np.log10(h_cut) + 6.0) / 6.0
-    singular = (f[:, 0] >= 0) & (f[:, 0] <= 1) & (f[:, 1] >= 0) & (f[:, 1] <= 1) & (f[:, 2].abs() < hfeat_cut)
-    ok = L.in_range(f) & singular
+    in_panel = (f[:, 0] >= 0) & (f[:, 0] <= 1) & (f[:, 1] >= 0) & (f[:, 1] <= 1) & (f[:, 2].abs() < hfeat_cut)
+    ok = L.in_range(f) & in_panel
     sig = sigma.reshape(S.np, S.nn)
     dens = (sig * L.fy.sd[None]).contiguous()
     const = (sig * L.fy.mu[None]).sum(1)
@@ -257,7 +283,10 @@ def learned_near_field(S, T, L: LearnedCorrection, r_trg: torch.Tensor, sigma: t
         o = torch.zeros(idx.numel(), dtype=torch.float64, device=xt.device)
         m.forward_dot(x, dens, pp[idx].contiguous(), o)
         preds.append(o + const[pp[idx]])
-    bound = L.error_bound(f[idx], sig.abs().sum(1)[pp[idx]])
+    if L.singular is not None:
+        base = L.singular.singular_dot(f[idx], sig, pp[idx])
+        preds = [p + base for p in preds]
+    bound = L.error_bound(f[idx], sig[pp[idx]])
     agree = ((preds[0] - preds[1]).abs() <= tol) & (bound <= tol)
     acc_idx = idx[agree]
     out.index_add_(0, pt[acc_idx], 0.5 * (preds[0][agree] + preds[1][agree]))

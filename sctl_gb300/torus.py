@@ -118,6 +118,12 @@ class Torus:
             pairs_p.append(pp)
         return np.concatenate(pairs_t).astype(np.int64), np.concatenate(pairs_p).astype(np.int64)
 
+    def singular_weights(self, f):
+        return singular_weights(self, f)
+
+    def singular_dot(self, f, sig, pp):
+        return singular_dot(self, f, sig, pp)
+
     def upsample_matrix(self, k: int):
         """Interpolation matrix (k*k*p*p, p*p) from a panel's nodes to k x k sub-panels with
         p x p Chebyshev nodes each, the sub-panel weights (fraction of the panel rule), and the
@@ -160,3 +166,87 @@ def pair_features(T: "Torus", xt, pt, pp):
     geo = np.stack([np.cos(phc), np.sin(phc), rho, lth, lph, k1, k2, size * 10.0, T.area[pp] / size ** 2,
                     lth / lph, k1 * k2, 0.5 * (k1 + k2)], 1)
     return np.concatenate([np.stack([s, t, hf], 1), geo], 1)
+
+
+def pair_features_device(T: "Torus", xt, pt, pp):
+    """`pair_features` on torch tensors (any device, FP64): xt (n, 3) or flat target coordinates,
+    pt / pp int64 pair indices.  Same formulas, evaluated where the pairs live."""
+    import torch
+    dev = xt.device
+    key = ("_feat_tables", str(dev))
+    tab = T.__dict__.get(key)
+    if tab is None:
+        phc = T.phi0 + 0.5 * T.dph
+        rho = R_MAJOR + R_MINOR * np.cos(phc)
+        lth, lph = rho * T.dth / T.size, R_MINOR * T.dph / T.size
+        k1, k2 = np.cos(phc) / rho * T.size, T.size / R_MINOR
+        geo = np.stack([np.cos(phc), np.sin(phc), rho, lth, lph, k1, k2, T.size * 10.0, T.area / T.size ** 2,
+                        lth / lph, k1 * k2, 0.5 * (k1 + k2)], 1)
+        t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)  # noqa: E731
+        tab = (t(T.theta0), t(T.phi0), t(T.size), t(geo))
+        T.__dict__[key] = tab
+    th0, ph0, size, geo = tab
+    x = xt.reshape(-1, 3)[pt]
+    th = torch.atan2(x[:, 1], x[:, 0])
+    rho = torch.hypot(x[:, 0], x[:, 1])
+    ph = torch.atan2(x[:, 2], rho - R_MAJOR)
+    d = torch.hypot(rho - R_MAJOR, x[:, 2]) - R_MINOR
+    s = (torch.remainder(th - th0[pp] + np.pi, 2 * np.pi) - np.pi) / T.dth
+    t = (torch.remainder(ph - ph0[pp] + np.pi, 2 * np.pi) - np.pi) / T.dph
+    hr = d.abs() / size[pp]
+    hf = torch.sign(d) * (torch.log10(hr.clamp_min(1e-6)) + 6.0) / 6.0
+    return torch.cat([torch.stack([s, t, hf], 1), geo[pp]], 1).contiguous()
+
+
+def _basis_device(T: "Torus", x):
+    """Barycentric Lagrange basis of the panel's 1-D Chebyshev nodes at points x (n,), clamped to
+    [0, 1]: (n, p), exact (one-hot) at the nodes."""
+    import torch
+    nodes = torch.as_tensor(T.x1d, dtype=torch.float64, device=x.device)
+    bw = torch.as_tensor(T.bw, dtype=torch.float64, device=x.device)
+    d = x.clamp(0.0, 1.0)[:, None] - nodes[None]
+    hit = d == 0
+    q = bw[None] / torch.where(hit, torch.ones_like(d), d)
+    L = q / q.sum(1, keepdim=True)
+    rows = hit.any(1)
+    return torch.where(rows[:, None], hit.to(L.dtype), L)
+
+
+SINGULAR_H0 = 0.05  # distance (panel sizes) over which the singular part is switched off
+
+
+def singular_part(T: "Torus", f, h0=SINGULAR_H0):
+    """Leading near-singular behaviour of the Laplace double-layer weights of (target, panel) pairs
+    from their features: the density frozen at the (clamped) foot point times the solid angle of
+    the panel's flat parameter rectangle, sign(d) * Omega / (4 pi), faded out as 1 / (1 + (h/h0)^2)
+    with the distance h in panel sizes (farther away the weights are smooth and the frozen-density
+    term would only add structure).  Returns the factor (n,) and the 1-D bases (n, p) along s and t;
+    the weight of node (a, b) is factor * Ls[a] * Lt[b].  As d -> 0 inside the panel the factor
+    tends to +-1/2, the double layer's jump."""
+    import torch
+    s, t, hf = f[:, 0], f[:, 1], f[:, 2]
+    lth, lph = f[:, 6], f[:, 7]
+    z = torch.pow(10.0, 6.0 * hf.abs() - 6.0)
+    x1, x2 = -s * lth, (1.0 - s) * lth
+    y1, y2 = -t * lph, (1.0 - t) * lph
+
+    def corner(x, y):
+        return torch.atan(x * y / (z * torch.sqrt(x * x + y * y + z * z)))
+
+    omega = corner(x2, y2) - corner(x1, y2) - corner(x2, y1) + corner(x1, y1)
+    fac = torch.sign(hf) * omega / (4.0 * np.pi) / (1.0 + (z / h0) ** 2)
+    return fac, _basis_device(T, s), _basis_device(T, t)
+
+
+def singular_weights(T: "Torus", f):
+    """`singular_part` as (n, p*p) node weights, node q = a * p + b."""
+    fac, Ls, Lt = singular_part(T, f)
+    return (fac[:, None, None] * Ls[:, :, None] * Lt[:, None, :]).reshape(f.shape[0], -1)
+
+
+def singular_dot(T: "Torus", f, sig, pp):
+    """sum_q singular_weights[n, q] * sig[pp[n], q] without forming the weights; sig (np, p*p)."""
+    import torch
+    fac, Ls, Lt = singular_part(T, f)
+    S = sig.reshape(sig.shape[0], T.p, T.p)[pp]
+    return fac * torch.einsum("na,nab,nb->n", Ls, S, Lt)

@@ -14,27 +14,39 @@ def trained(cuda):
     torch = cuda
     from sctl_gb300.learned import LearnedCorrection, panel_weights
     from sctl_gb300.nearquad import PanelSurface
-    from sctl_gb300.torus import Torus, pair_features
+    from sctl_gb300.torus import Torus, pair_features_device
     T = Torus(seed=0)
     S = PanelSurface(T.X, T.N, T.Q, T.size)
     tg = T.targets(24000, seed=100)
     xt = torch.from_numpy(tg["r_trg"]).cuda().reshape(-1).contiguous()
     pt, pp = S.near_pairs(xt, 1.0)
     W = panel_weights(1, pt, pp, xt, S.X)
-    f = torch.from_numpy(pair_features(T, tg["r_trg"], pt.cpu().numpy(), pp.cpu().numpy())).cuda()
-    L = LearnedCorrection(max_batch=8192)
-    losses = L.fit(f, W, steps=2000, batch=8192, lr=3e-3)
-    return torch, T, S, L, losses
+    f = pair_features_device(T, xt, pt, pp)
+    L = LearnedCorrection(max_batch=8192, singular=T)
+    losses = L.fit(f, W, steps=4000, batch=8192, lr=3e-3)
+    return torch, T, S, L, losses, (f, W)
 
 
 def test_training_converged(trained):
-    _, _, _, _, losses = trained
-    # standardized MSE starts near 1.1; the network explains most of the variance of the weights
-    assert all(l < 0.45 for l in losses), losses
+    _, _, _, _, losses, _ = trained
+    # the standardized MSE of the weights minus their singular part starts near 1.1; training
+    # at least halves it
+    assert all(l < 0.55 for l in losses), losses
+
+
+def test_singular_part_sharpens_the_network_near_the_surface(trained):
+    """Networks that learn the weights minus their singular part (solid angle x frozen density)
+    are far more accurate below 1e-3 panel sizes than networks that learn the weights outright."""
+    torch, T, S, L, _, (f, W) = trained
+    from sctl_gb300.learned import LearnedCorrection
+    L0 = LearnedCorrection(max_batch=8192)
+    L0.fit(f, W, steps=4000, batch=8192, lr=3e-3)
+    for b in (5, 6, 7):  # |log10 h| bins covering h in [1e-4, 1e-3] panel sizes
+        assert L.calib[b] < 0.25 * L0.calib[b], (b, L.calib[b].item(), L0.calib[b].item())
 
 
 def test_learned_correction_gain_over_smooth_rule(trained):
-    torch, T, S, L, _ = trained
+    torch, T, S, L, _, _ = trained
     from sctl_gb300.learned import learned_near_field
     tg = T.targets(2000, seed=200)
     xt = torch.from_numpy(tg["r_trg"]).cuda()
@@ -50,7 +62,7 @@ def test_learned_correction_gain_over_smooth_rule(trained):
 
 
 def test_tight_tolerance_falls_back_to_plain_path(trained):
-    torch, T, S, L, _ = trained
+    torch, T, S, L, _, _ = trained
     from sctl_gb300.learned import learned_near_field
     tg = T.targets(1000, seed=300)
     xt = torch.from_numpy(tg["r_trg"]).cuda()
@@ -65,9 +77,8 @@ def test_tight_tolerance_falls_back_to_plain_path(trained):
 def test_calibrated_gate_bounds_the_error(trained):
     """At a moderate tolerance the accepted pairs' calibrated bounds hold: each target's deviation
     from the plain path stays below tol times its number of accepted pairs."""
-    torch, T, S, L, _ = trained
+    torch, T, S, L, _, _ = trained
     from sctl_gb300.learned import learned_near_field
-    from sctl_gb300.torus import pair_features
     tg = T.targets(2000, seed=400)
     xt = torch.from_numpy(tg["r_trg"]).cuda()
     sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()

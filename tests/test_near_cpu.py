@@ -34,3 +34,18 @@ def test_near_blocks_generator_shapes():
     assert np.all(b[1:, 0] == np.cumsum(b[:, 1])[:-1])
     p = W.near_blocks(16, 0, seed=1, panel=True)
     assert set(np.unique(p["blocks"][:, 1])) <= {100 * k * k for k in range(1, 9)}
+
+
+def test_torus_pair_features_device_form_matches_numpy():
+    """The torch form of the learned path's pair features (run where the pairs live) equals the
+    numpy form used to define them."""
+    import torch
+    from sctl_gb300.torus import Torus, pair_features, pair_features_device
+    T = Torus(seed=0)
+    tg = T.targets(1500, seed=5)
+    pt, pp = T.near_pairs(tg["r_trg"], 1.0)
+    a = pair_features(T, tg["r_trg"], pt, pp)
+    b = pair_features_device(T, torch.from_numpy(tg["r_trg"]).reshape(-1), torch.from_numpy(pt),
+                             torch.from_numpy(pp)).numpy()
+    assert a.shape == b.shape == (pt.size, 15)
+    assert np.abs(a - b).max() < 1e-12
