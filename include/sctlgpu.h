@@ -193,7 +193,7 @@ int sctlgpu_near_plan_destroy(sctlgpu_near_plan plan);
  * for a surface given only by its panel nodes.  For every (target, panel) pair
  * the panel's geometry and density are interpolated from its nodes and
  * integrated with adaptive dyadic refinement (boxes accepted at distance >=
- * alpha x diameter, 10 x 10 Gauss-Legendre per box, at most max_depth levels),
+ * alpha x diameter, 8 x 8 Gauss-Legendre per box, at most max_depth levels),
  * the panel's smooth-rule part (nodes X, normals N, weights Q) is subtracted
  * when subtract_smooth != 0 (KNearSubtract, boundary_integral.txx:1165-1240; pass
  * 0 and subtract with a near plan in the far field's arithmetic when the far field

@@ -100,52 +100,10 @@ struct PanelWarpSmemDFW : PanelWarpSmemDF {
 template <bool WEIGHTS>
 using DFSmem = typename std::conditional<WEIGHTS, PanelWarpSmemDFW, PanelWarpSmemDF>::type;
 
-__constant__ float c_ch_xf[PQ_P], c_ch_wf[PQ_P];          // FP32 copies for the box test
 __constant__ float c_gl_xh[PQ_GL], c_gl_xl[PQ_GL];        // Gauss-Legendre nodes, double-float
 __constant__ float c_gl_wh[PQ_GL], c_gl_wl[PQ_GL];        // and weights
 __constant__ float c_ch_xh[PQ_P], c_ch_xl[PQ_P];          // Chebyshev nodes, double-float
 __constant__ float c_ch_wh[PQ_P], c_ch_wl[PQ_P];          // barycentric weights, double-float
-
-// FP32 barycentric basis and derivative (box test only).
-__device__ __forceinline__ void basis_f32(float s, float (&l)[PQ_P], float (&d)[PQ_P]) {
-  int hit = -1;
-#pragma unroll
-  for (int a = 0; a < PQ_P; ++a)
-    if (s == c_ch_xf[a]) hit = a;
-  if (hit >= 0) {
-#pragma unroll
-    for (int a = 0; a < PQ_P; ++a) {
-      l[a] = (a == hit) ? 1.f : 0.f;
-      d[a] = 0.f;
-    }
-    float diag = 0.f;
-    const float xh = c_ch_xf[hit], iwh = 1.f / c_ch_wf[hit];
-#pragma unroll
-    for (int a = 0; a < PQ_P; ++a)
-      if (a != hit) {
-        d[a] = (c_ch_wf[a] * iwh) / (xh - c_ch_xf[a]);
-        diag -= d[a];
-      }
-#pragma unroll
-    for (int a = 0; a < PQ_P; ++a)
-      if (a == hit) d[a] = diag;
-    return;
-  }
-  float T = 0.f, U = 0.f, r[PQ_P], t[PQ_P];
-#pragma unroll
-  for (int a = 0; a < PQ_P; ++a) {
-    r[a] = 1.f / (s - c_ch_xf[a]);
-    t[a] = c_ch_wf[a] * r[a];
-    T += t[a];
-    U += t[a] * r[a];
-  }
-  const float iT = 1.f / T, UT = U * iT;
-#pragma unroll
-  for (int a = 0; a < PQ_P; ++a) {
-    l[a] = t[a] * iT;
-    d[a] = l[a] * (UT - r[a]);
-  }
-}
 
 // Double-float basis and derivative at s (s = bs + bz * g, g a Gauss node).
 __device__ __forceinline__ void basis_df(f2 s, f2 (&l)[PQ_P], f2 (&d)[PQ_P]) {
@@ -241,36 +199,8 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
         if (valid) {
           bs = sm.box[cur][i][0];
           bt = sm.box[cur][i][1];
-          // FP32 interpolation of the offset and tangents at the box centre
-          float ls[PQ_P], ds[PQ_P], lt[PQ_P], dt[PQ_P];
-          basis_f32(bs + 0.5f * bz, ls, ds);
-          basis_f32(bt + 0.5f * bz, lt, dt);
-          float X[3], Xs[3], Xt[3];
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            float v = 0.f, vs = 0.f, vt = 0.f;
-#pragma unroll
-            for (int a = 0; a < PQ_P; ++a) {
-              float r0 = 0.f, rt = 0.f;
-#pragma unroll
-              for (int b = 0; b < PQ_P; ++b) {
-                const float f = sm.F[c][a * PQ_P + b].h;
-                r0 = fmaf(lt[b], f, r0);
-                rt = fmaf(dt[b], f, rt);
-              }
-              v = fmaf(ls[a], r0, v);
-              vs = fmaf(ds[a], r0, vs);
-              vt = fmaf(ls[a], rt, vt);
-            }
-            X[c] = v;
-            Xs[c] = vs;
-            Xt[c] = vt;
-          }
-          const float sl = Xs[0] * Xs[0] + Xs[1] * Xs[1] + Xs[2] * Xs[2];
-          const float tl = Xt[0] * Xt[0] + Xt[1] * Xt[1] + Xt[2] * Xt[2];
-          const float diam = bz * sqrtf(sl + tl);
-          const float d = sqrtf(X[0] * X[0] + X[1] * X[1] + X[2] * X[2]);
-          accept = d >= (float)p.alpha * diam || depth == p.max_depth;
+          accept = box_far_enough([&](int c, int q) { return sm.F[c][q].h; }, bs, bt, bz, (float)p.alpha) ||
+                   depth == p.max_depth;
         }
         const unsigned acc_mask = __ballot_sync(0xffffffffu, valid && accept);
         const unsigned ref_mask = __ballot_sync(0xffffffffu, valid && !accept);

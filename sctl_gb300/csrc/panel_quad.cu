@@ -7,7 +7,7 @@
 // [0,1]^2 level by level (a box is accepted once its distance to the target is
 // at least `alpha` times its physical diameter; the legacy quadrature's dyadic
 // refinement toward the target, boundary_quadrature.hpp:364-478, is the model),
-// integrates every accepted box with a 10 x 10 Gauss-Legendre rule on geometry
+// integrates every accepted box with an 8 x 8 Gauss-Legendre rule on geometry
 // and density interpolated from the panel's nodes (barycentric Lagrange,
 // as LagrangeInterp does on the CPU), and subtracts the panel's own smooth-rule
 // contribution (the KNearSubtract convention, boundary_integral.txx:1165-1240).
@@ -31,7 +31,12 @@ namespace {
 
 constexpr int PQ_P = 10;          // panel order
 constexpr int PQ_NODES = PQ_P * PQ_P;
-constexpr int PQ_GL = 10;         // Gauss-Legendre points per box side
+// Gauss-Legendre points per box side.  With alpha = 1 the nearest singularity
+// of an accepted box's integrand lies >= 2.8 half-sides from its centre; 8
+// points keep the torus near field within 1e-10 (max, relative) of a rule
+// refined twice as far (10 points: 2e-12 at 1.4x the time), and 64 nodes fill
+// two full warp rounds.
+constexpr int PQ_GL = 8;
 constexpr int PQ_WARPS = 4;       // warps per CTA
 constexpr int PQ_QUEUE = 256;     // boxes per round (per warp)
 constexpr int PQ_MAX_DEPTH = 22;  // box corners k * 2^-depth stay exact in FP32
@@ -39,6 +44,7 @@ constexpr int PQ_MAX_DEPTH = 22;  // box corners k * 2^-depth stay exact in FP32
 // Per-warp shared state (dynamic shared memory).
 struct PanelWarpSmem {
   double F[4][PQ_NODES];          // x, y, z, sigma at the panel nodes (a-major: F[c][a*P+b])
+  float Fo[3][PQ_NODES];          // (float)(x_q - x_t): the box test's node offsets
   double Ls[PQ_GL][PQ_P], Lds[PQ_GL][PQ_P], Lt[PQ_GL][PQ_P], Ldt[PQ_GL][PQ_P];  // basis at a box's Gauss points
   double A[7][PQ_GL][PQ_P];       // L_s F (x,y,z,sigma) and L_s' F (x,y,z)
   double Kd[PQ_GL][PQ_GL];        // weights mode: K * dA at a box's Gauss nodes
@@ -52,6 +58,88 @@ __constant__ double c_gl_x[PQ_GL], c_gl_w[PQ_GL];
 // First-kind Chebyshev points of [0,1] (ChebQuadRule's nodes) and their
 // barycentric weights (-1)^a sin((2a+1) pi / 2P), computed once on the host.
 __constant__ double c_ch_x[PQ_P], c_ch_w[PQ_P];
+
+__constant__ float c_ch_xf[PQ_P], c_ch_wf[PQ_P];  // FP32 copies for the box test
+
+// FP32 barycentric basis and derivative (box test only).
+__device__ __forceinline__ void basis_f32(float s, float (&l)[PQ_P], float (&d)[PQ_P]) {
+  int hit = -1;
+#pragma unroll
+  for (int a = 0; a < PQ_P; ++a)
+    if (s == c_ch_xf[a]) hit = a;
+  if (hit >= 0) {
+#pragma unroll
+    for (int a = 0; a < PQ_P; ++a) {
+      l[a] = (a == hit) ? 1.f : 0.f;
+      d[a] = 0.f;
+    }
+    float diag = 0.f;
+    const float xh = c_ch_xf[hit], iwh = 1.f / c_ch_wf[hit];
+#pragma unroll
+    for (int a = 0; a < PQ_P; ++a)
+      if (a != hit) {
+        d[a] = (c_ch_wf[a] * iwh) / (xh - c_ch_xf[a]);
+        diag -= d[a];
+      }
+#pragma unroll
+    for (int a = 0; a < PQ_P; ++a)
+      if (a == hit) d[a] = diag;
+    return;
+  }
+  float T = 0.f, U = 0.f, r[PQ_P], t[PQ_P];
+#pragma unroll
+  for (int a = 0; a < PQ_P; ++a) {
+    r[a] = 1.f / (s - c_ch_xf[a]);
+    t[a] = c_ch_wf[a] * r[a];
+    T += t[a];
+    U += t[a] * r[a];
+  }
+  const float iT = 1.f / T, UT = U * iT;
+#pragma unroll
+  for (int a = 0; a < PQ_P; ++a) {
+    l[a] = t[a] * iT;
+    d[a] = l[a] * (UT - r[a]);
+  }
+}
+
+// The box test of both arithmetic forms (a threshold, so FP32 suffices, and the
+// FP64 and double-float kernels refine identically): offset and tangents
+// interpolated at the box centre from the FP32 node offsets off(c, q) =
+// x_q - x_t; the box is far enough when that offset is at least alpha times
+// the box's physical diameter.
+template <class Off>
+__device__ __forceinline__ bool box_far_enough(Off off, float bs, float bt, float bz, float alpha) {
+  float ls[PQ_P], ds[PQ_P], lt[PQ_P], dt[PQ_P];
+  basis_f32(bs + 0.5f * bz, ls, ds);
+  basis_f32(bt + 0.5f * bz, lt, dt);
+  float X[3], Xs[3], Xt[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    float v = 0.f, vs = 0.f, vt = 0.f;
+#pragma unroll
+    for (int a = 0; a < PQ_P; ++a) {
+      float r0 = 0.f, rt = 0.f;
+#pragma unroll
+      for (int b = 0; b < PQ_P; ++b) {
+        const float f = off(c, a * PQ_P + b);
+        r0 = fmaf(lt[b], f, r0);
+        rt = fmaf(dt[b], f, rt);
+      }
+      v = fmaf(ls[a], r0, v);
+      vs = fmaf(ds[a], r0, vs);
+      vt = fmaf(ls[a], rt, vt);
+    }
+    X[c] = v;
+    Xs[c] = vs;
+    Xt[c] = vt;
+  }
+  const float sl = Xs[0] * Xs[0] + Xs[1] * Xs[1] + Xs[2] * Xs[2];
+  const float tl = Xt[0] * Xt[0] + Xt[1] * Xt[1] + Xt[2] * Xt[2];
+  const float diam = bz * sqrtf(sl + tl);
+  const float d = sqrtf(X[0] * X[0] + X[1] * X[1] + X[2] * X[2]);
+  return d >= alpha * diam;
+}
+
 
 struct Basis {
   double l[PQ_P], d[PQ_P];
@@ -97,39 +185,6 @@ __device__ __forceinline__ void basis(double s, Basis& B) {
   for (int a = 0; a < PQ_P; ++a) {
     B.l[a] = t[a] * iT;
     B.d[a] = B.l[a] * (UT - r[a]);  // d/ds of t_a/T = (-t_a r T + t_a U) / T^2
-  }
-}
-
-// Geometry and density at (s, t): position, tangents (per unit s, t) and sigma.
-__device__ __forceinline__ void interp(const double (*F)[PQ_NODES], double s, double t, double X[3], double Xs[3], double Xt[3],
-                       double& sig, bool need_sig) {
-  Basis A, B;
-  basis(s, A);
-  basis(t, B);
-#pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    if (c == 3 && !need_sig) break;
-    double v = 0, vs = 0, vt = 0;
-#pragma unroll
-    for (int a = 0; a < PQ_P; ++a) {
-      double r = 0, rt = 0;
-#pragma unroll
-      for (int b = 0; b < PQ_P; ++b) {
-        const double f = F[c][a * PQ_P + b];
-        r = fma(B.l[b], f, r);
-        rt = fma(B.d[b], f, rt);
-      }
-      v = fma(A.l[a], r, v);
-      vs = fma(A.d[a], r, vs);
-      vt = fma(A.l[a], rt, vt);
-    }
-    if (c < 3) {
-      X[c] = v;
-      Xs[c] = vs;
-      Xt[c] = vt;
-    } else {
-      sig = v;
-    }
   }
 }
 
@@ -188,9 +243,11 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel(PanelParams p
     const double xt[3] = {p.r_trg[tix * 3], p.r_trg[tix * 3 + 1], p.r_trg[tix * 3 + 2]};
     __syncwarp();
     for (int q = lane; q < PQ_NODES; q += 32) {
-      sm.F[0][q] = p.X[(pix * PQ_NODES + q) * 3 + 0];
-      sm.F[1][q] = p.X[(pix * PQ_NODES + q) * 3 + 1];
-      sm.F[2][q] = p.X[(pix * PQ_NODES + q) * 3 + 2];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        sm.F[c][q] = p.X[(pix * PQ_NODES + q) * 3 + c];
+        sm.Fo[c][q] = (float)(sm.F[c][q] - xt[c]);
+      }
       sm.F[3][q] = p.sigma[pix * PQ_NODES + q];
     }
     __syncwarp();
@@ -225,14 +282,9 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel(PanelParams p
           bs = sm.box[cur][i][0];
           bt = sm.box[cur][i][1];
           bz = sm.box[cur][i][2];
-          double X[3], Xs[3], Xt[3], sg;
-          interp(sm.F, bs + 0.5 * bz, bt + 0.5 * bz, X, Xs, Xt, sg, false);
-          const double ls = sqrt(Xs[0] * Xs[0] + Xs[1] * Xs[1] + Xs[2] * Xs[2]);
-          const double lt = sqrt(Xt[0] * Xt[0] + Xt[1] * Xt[1] + Xt[2] * Xt[2]);
-          const double diam = bz * sqrt(ls * ls + lt * lt);
-          const double d = sqrt((xt[0] - X[0]) * (xt[0] - X[0]) + (xt[1] - X[1]) * (xt[1] - X[1]) +
-                                (xt[2] - X[2]) * (xt[2] - X[2]));
-          accept = d >= p.alpha * diam || depth == p.max_depth;
+          accept = box_far_enough([&](int c, int q) { return sm.Fo[c][q]; }, (float)bs, (float)bt, (float)bz,
+                                  (float)p.alpha) ||
+                   depth == p.max_depth;
         }
         const unsigned acc_mask = __ballot_sync(0xffffffffu, valid && accept);
         const unsigned ref_mask = __ballot_sync(0xffffffffu, valid && !accept);

@@ -140,8 +140,9 @@ def test_near_matrix_apply_general_layout(cuda, k0, k1):
 
 @pytest.mark.parametrize("kernel", [0, 1])
 def test_double_float_panel_quadrature_matches_fp64(setup, kernel):
-    """The default double-float panel kernel against the FP64 one: corrections (with the smooth
-    part subtracted in-kernel) and weights agree far below the quadrature's own error."""
+    """The default double-float panel kernel against the FP64 one (both refine with the same FP32
+    box test): corrections (with the smooth part subtracted in-kernel) and weights agree far below
+    the quadrature's own error (1e-10 relative)."""
     torch, T, S = setup
     from sctl_gb300 import capi
     from sctl_gb300.learned import panel_weights
@@ -161,5 +162,5 @@ def test_double_float_panel_quadrature_matches_fp64(setup, kernel):
             lib.sctlgpu_panel_arithmetic(prev)
     (c64, w64), (cdf, wdf) = res[capi.F64], res[capi.MIXED]
     assert np.abs(cdf - c64).max() <= 1e-11 * np.abs(c64).max(), np.abs(cdf - c64).max() / np.abs(c64).max()
-    assert np.abs(wdf - w64).max() <= 1e-11 * np.abs(w64).max()
+    assert np.abs(wdf - w64).max() <= 2e-11 * np.abs(w64).max()
     assert lib.sctlgpu_device_status(None) == capi.OK
