@@ -174,21 +174,23 @@ def _ev_ms(torch, fn, reps=3):
     return best
 
 
-def near_field_section(torch, stream):
+def near_field_section(torch, stream, panel=False):
     """4096 uneven Laplace3D_DxU near blocks (100..6400 sources, 16..2048 targets), one persistent
-    launch per plan execution (CUDA-graph replay), FP64 vs mixed digits 10."""
+    launch per plan execution (CUDA-graph replay), FP64 vs mixed digits 10.  With panel=True the
+    sources per block are 10 x 10 panels upsampled k x per side (Ns = 100 k^2, k = 1..8)."""
     from oracle import oracle as O
     from sctl_gb300 import workloads as W
     from sctl_gb300.near import NearPlan
     k = 1
-    d = W.near_blocks(4096, k, seed=0)
+    d = W.near_blocks(4096, k, seed=0, panel=panel)
     blocks = d["blocks"]
     ns, nt = d["r_src"].shape[0], d["r_trg"].shape[0]
     pairs = int((blocks[:, 1] * blocks[:, 3]).sum())
     dd = {a: torch.from_numpy(np.ascontiguousarray(v)).cuda() for a, v in d.items() if a != "blocks"}
     # algorithmic bytes of one execution (FP64 inputs): sources x, n, f; targets x in, potential out
     alg_bytes = ns * (3 + 3 + 1) * 8 + nt * (3 * 8 + 8)
-    res = {"workload": "4096 blocks, Ns=round(100*64^u), Nt=round(16*128^v), Laplace3D_DxU, seed 0",
+    res = {"workload": "4096 blocks, Ns=" + ("100*k^2, k=1..8" if panel else "round(100*64^u)") +
+                       ", Nt=round(16*128^v), Laplace3D_DxU, seed 0",
            "interactions": pairs, "algorithmic_bytes": alg_bytes}
     outs = {}
     for mode, dg in (("mixed", 10), ("f64", -1)):
@@ -473,7 +475,8 @@ def main():
     ap.add_argument("--kernels", default="1,2,3", help="kernel ids of the step (default: the three sphere/ball kernels)")
     ap.add_argument("--quick", action="store_true", help="timed region only (for profiler runs)")
     ap.add_argument("--skip-torus", action="store_true", help="omit the near-singular torus section")
-    ap.add_argument("--section", choices=["near", "clusters", "cube", "torus", "torus_plain", "mlp", "ext", "kmat"],
+    ap.add_argument("--section", choices=["near", "near_panel", "clusters", "cube", "torus", "torus_plain", "mlp",
+                                          "ext", "kmat"],
                     help="run only this secondary workload and print its JSON (profiling of one kernel family)")
     ap.add_argument("--torus-n", type=int, default=1 << 20, help="targets of the torus section")
     args = ap.parse_args()
@@ -485,7 +488,9 @@ def main():
         from sctl_gb300 import capi
         capi.load()
         stream = torch.cuda.current_stream()
-        fn = {"near": lambda: near_field_section(torch, stream), "clusters": lambda: cluster_section(torch, stream),
+        fn = {"near": lambda: near_field_section(torch, stream),
+              "near_panel": lambda: near_field_section(torch, stream, panel=True),
+              "clusters": lambda: cluster_section(torch, stream),
               "cube": lambda: cube_section(torch, stream), "mlp": lambda: mlp_section(torch, stream),
               "ext": lambda: ext_section(torch, stream), "kmat": lambda: kmat_section(torch, stream),
               "torus": lambda: torus_section(torch, n_eval=args.torus_n),
@@ -656,6 +661,7 @@ def main():
     extras = {}
     if rank == 0:
         extras["near_field_blocks"] = near_field_section(torch, stream)
+        extras["near_field_blocks_panel_variant"] = near_field_section(torch, stream, panel=True)
         extras["precision_stress_clusters"] = cluster_section(torch, stream)
         extras["cube8192_fp64_d14"] = cube_section(torch, stream)
         extras["tensor_core_mlp"] = mlp_section(torch, stream)

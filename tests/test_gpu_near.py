@@ -58,6 +58,23 @@ def test_near_batch_matches_oracle(cuda, k, mode, digits, tol):
     assert info["items"] >= len(d["blocks"]) and info["graph_kernels"] >= 2
 
 
+@pytest.mark.parametrize("mode,digits,tol", [("f64", -1, 1e-12), ("mixed", 10, 1e-10)])
+def test_near_batch_panel_variant_matches_oracle(cuda, mode, digits, tol):
+    """The panel form of the uneven blocks: 10 x 10 panels upsampled k x per side (Ns = 100 k^2,
+    k = 1..8), Laplace3D_DxU."""
+    torch = cuda
+    d = W.near_blocks(96, 1, seed=11, panel=True)
+    assert set(np.unique(d["blocks"][:, 1]) // 100) <= {k * k for k in range(1, 9)}
+    ref = oracle_blocks(1, d)
+    dd = dev(torch, d)
+    out = torch.zeros(d["r_trg"].shape[0], dtype=torch.float64, device="cuda")
+    plan = NearPlan(1, d["blocks"], d["r_src"].shape[0], d["r_trg"].shape[0], mode=mode, digits=digits)
+    plan.execute(dd["r_trg"], dd["r_src"], dd["n_src"], dd["v_src"], out)
+    torch.cuda.synchronize()
+    assert O.rel_l2(out.cpu().numpy(), ref.reshape(-1)) < tol
+    assert plan.status() == capi.OK
+
+
 def test_near_batch_map_weights_accumulate_and_recapture(cuda):
     torch = cuda
     k = 1
