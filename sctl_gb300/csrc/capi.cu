@@ -204,10 +204,10 @@ cudaError_t run_kmat(KmatCall& c, int mode, int d) {
     if (mode == SCTLGPU_F32) return kmat_ext_f32(c, steps_for(mode, d));
     return kmat_ext_f64(c, steps_for(SCTLGPU_F64, d));
   }
-  // Matrix entries are stored in the caller's FP64, so the mixed mode computes them in FP64
-  // too: converting double-float entries to double costs more FP64 work per entry than the
-  // FP64 formula (measured: the FP64 kernel writes Stokes3D_FxU matrices 2.4x faster).
+  // Mixed mode: double-float entries rounded to FP64 by integer operations (no FP64 pipe per
+  // entry); beyond the double-float digits, the FP64 formula.
   if (mode == SCTLGPU_F32) return kmat_f32(c, steps_for(mode, d));
+  if (mode == SCTLGPU_MIXED && d <= kMixedDfMaxDigits) return kmat_mixed_df(c);
   return kmat_f64(c, steps_for(SCTLGPU_F64, d));
 }
 

@@ -101,35 +101,38 @@ __device__ __forceinline__ R newton_rsqrt(R y, R hx) {
 
 // ------------------------------------------------------------- double-float
 // Unnormalised pair h + l with |l| << |h|; error-free transforms after
-// Knuth (TwoSum) and Dekker/FMA (TwoProduct).
+// Knuth (TwoSum) and Dekker/FMA (TwoProduct).  The rounded products and sums
+// these rely on are written as __fmul_rn / __fadd_rn: the compiler never
+// merges those into a multiply-add, which would replace a rounded product
+// feeding a TwoSum by the exact one and break the transformation.
 struct f2 {
   float h, l;
 };
 
 __device__ __forceinline__ f2 two_sum(float a, float b) {
-  const float s = a + b;
+  const float s = __fadd_rn(a, b);
   const float bb = s - a;
   const float e = (a - (s - bb)) + (b - bb);
   return {s, e};
 }
 __device__ __forceinline__ f2 fast_two_sum(float a, float b) {  // requires |a| >= |b| or a == 0
-  const float s = a + b;
+  const float s = __fadd_rn(a, b);
   return {s, b - (s - a)};
 }
 __device__ __forceinline__ f2 two_prod(float a, float b) {
-  const float p = a * b;
+  const float p = __fmul_rn(a, b);
   return {p, fmaf(a, b, -p)};
 }
 __device__ __forceinline__ f2 df_norm(f2 x) { return fast_two_sum(x.h, x.l); }
 __device__ __forceinline__ f2 df_mul(f2 x, f2 y) {
-  const float p = x.h * y.h;
+  const float p = __fmul_rn(x.h, y.h);
   float e = fmaf(x.h, y.h, -p);
   e = fmaf(x.h, y.l, e);
   e = fmaf(x.l, y.h, e);
   return {p, e};
 }
 __device__ __forceinline__ f2 df_mulf(f2 x, float y) {
-  const float p = x.h * y;
+  const float p = __fmul_rn(x.h, y);
   float e = fmaf(x.h, y, -p);
   e = fmaf(x.l, y, e);
   return {p, e};

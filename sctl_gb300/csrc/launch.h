@@ -63,6 +63,8 @@ cudaError_t kmat_ext_f32(const KmatCall& c, int newton);
 // Kernel matrices.
 cudaError_t kmat_f64(const KmatCall& c, int newton);
 cudaError_t kmat_f32(const KmatCall& c, int newton);
+// Mixed precision (digits up to the double-float limit): double-float entries rounded to FP64.
+cudaError_t kmat_mixed_df(const KmatCall& c);
 
 // Bounding box of targets and sources for the mixed-precision frame; `bb` is
 // 64 bytes of device memory, initialised here.

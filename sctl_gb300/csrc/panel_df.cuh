@@ -26,20 +26,20 @@ using sctlgpu::two_prod;
 using sctlgpu::two_sum;
 
 __device__ __forceinline__ f2 norm(f2 x) {
-  const float s = x.h + x.l;
+  const float s = __fadd_rn(x.h, x.l);
   return {s, x.l - (s - x.h)};
 }
 __device__ __forceinline__ f2 neg(f2 x) { return {-x.h, -x.l}; }
 // Products keep the cross terms; sums are TwoSum on the high parts.
 __device__ __forceinline__ f2 mul(f2 a, f2 b) {
-  const float p = a.h * b.h;
+  const float p = __fmul_rn(a.h, b.h);
   float e = fmaf(a.h, b.h, -p);
   e = fmaf(a.h, b.l, e);
   e = fmaf(a.l, b.h, e);
   return {p, e};
 }
 __device__ __forceinline__ f2 mulf(f2 a, float b) {
-  const float p = a.h * b;
+  const float p = __fmul_rn(a.h, b);
   return {p, fmaf(a.l, b, fmaf(a.h, b, -p))};
 }
 __device__ __forceinline__ f2 add(f2 a, f2 b) {

@@ -97,6 +97,26 @@ def test_kernel_matrix_matches_reference(cuda, golden, k, mode):
     assert O.rel_l2(M, golden[f"{NAMES[k]}/kmat40x50/kmat_f64"]) < (1e-6 if mode == "f32" else 1e-12)
 
 
+@pytest.mark.parametrize("k", range(4))
+@pytest.mark.parametrize("digits", [6, 10, 11])
+def test_kernel_matrix_mixed_double_float(cuda, golden, k, digits):
+    """Mixed KernelMatrix at digits <= 11: double-float entries rounded to FP64 by integer
+    operations.  Against the reference's FP64 matrix, a larger FP64 matrix entry by entry, and
+    zero entries for coincident points (r = 0)."""
+    d = case(NAMES[k], "kmat40x50")
+    M = KER[k].KernelMatrix(d["r_trg"], d["r_src"], d["n_src"], mode="mixed", digits=digits)
+    assert O.rel_l2(M, golden[f"{NAMES[k]}/kmat40x50/kmat_f64"]) < 1e-12
+    e = W.sphere_ball(700, 300, k, seed=21)
+    xt = np.concatenate([e["r_trg"], e["r_src"][:5]])  # 5 targets on top of sources
+    M = KER[k].KernelMatrix(xt, e["r_src"], e["n_src"], mode="mixed", digits=digits)
+    M64 = KER[k].KernelMatrix(xt, e["r_src"], e["n_src"], mode="f64")
+    assert np.abs(M - M64).max() <= 1e-12 * np.abs(M64).max()
+    k0, k1 = O.DIMS[k][1], O.DIMS[k][2]
+    for i in range(5):  # source i coincides with target 300 + i
+        blk = M[i * k0:(i + 1) * k0, (300 + i) * k1:(301 + i) * k1]
+        assert np.all(blk == 0.0)
+
+
 def test_cube8192_f64_digits14(cuda, golden):
     d = W.cube(8192, 8192, 0, 0)
     out = run(0, d, "f64", 14)
