@@ -7,12 +7,15 @@
 // Method: Fast2Sum gives s + e = h + l exactly with |e| <= ulp(s)/2.  The
 // double image of s is its float bit pattern with the exponent rebiased
 // (+896) and the mantissa moved up 29 bits.  Adding e is an integer
-// adjustment of that pattern by round-to-nearest-even(e / ulp_d), with ulp_d
-// the double ulp at |s| (half of it when |s| is a power of two and the
-// adjustment points down, where the result lands in the binade below).  The
-// pattern's low 29 bits are zero, so rounding e alone and rounding the exact
-// sum agree, ties included.  Zero, subnormal, huge, infinite and NaN values
-// of s take the FP64 route.
+// adjustment of that pattern by round-to-nearest-even(|e| / ulp_d), with
+// ulp_d the double ulp at |s| (half of it when |s| is a power of two and the
+// adjustment points down, where the result lands in the binade below),
+// computed from e's mantissa by a shift with round-half-even (integer
+// operations only; GB300's float-to-integer conversion shares the slow
+// pipe).  The pattern's low 29 bits are zero, so rounding e alone and
+// rounding the exact sum agree, ties included.  No FP64 instruction is
+// issued, not even a predicated one: tiny, subnormal and huge values are
+// rescaled by a power of two, zeros and non-finite values are selected.
 //
 // The same code compiles for the host (g++), where a unit test compares it
 // with (double)h + (double)l over millions of cases.
@@ -24,7 +27,6 @@
 #if defined(__CUDACC__)
 #define SCTLGPU_DFC_HD __host__ __device__ __forceinline__
 #else
-#include <cmath>
 #define SCTLGPU_DFC_HD inline
 #endif
 
@@ -37,22 +39,6 @@ SCTLGPU_DFC_HD uint32_t dfc_bits(float x) {
   uint32_t u;
   std::memcpy(&u, &x, 4);
   return u;
-#endif
-}
-SCTLGPU_DFC_HD float dfc_float(uint32_t u) {
-#if defined(__CUDA_ARCH__)
-  return __uint_as_float(u);
-#else
-  float x;
-  std::memcpy(&x, &u, 4);
-  return x;
-#endif
-}
-SCTLGPU_DFC_HD int32_t dfc_rint(float x) {  // round to nearest, ties to even (|x| < 2^31)
-#if defined(__CUDA_ARCH__)
-  return __float2int_rn(x);
-#else
-  return (int32_t)std::lrintf(x);
 #endif
 }
 // Rounded sum that is never merged with a product into a multiply-add.
@@ -76,22 +62,38 @@ SCTLGPU_DFC_HD double dfc_double(uint64_t b) {
 // h + l with |l| no larger than |h| (any double-float pair from an
 // error-free transformation), rounded to nearest-even as a double.
 SCTLGPU_DFC_HD double df_to_double(float h, float l) {
-  const float s = dfc_add(h, l);
-  const float e = l - (s - h);
-  const uint32_t sb = dfc_bits(s);
-  const uint32_t E = (sb >> 23) & 0xffu;
-  // 64 <= E <= 253 keeps the scale factor below a normal float and |s| far from overflow.
-  if (E < 64u || E > 253u) return (double)h + (double)l;
-  const uint32_t neg = sb >> 31;
-  const float em = neg ? -e : e;  // adjustment of |s|
-  const bool down = (sb & 0x7fffffu) == 0u && em < 0.f;
-  // e / ulp_d = e * 2^k, ulp_d = 2^(E - 127 - 52) (half that below a power of two)
-  const int32_t k = 179 - (int32_t)E + (down ? 1 : 0);
-  const float t = em * dfc_float((uint32_t)(k + 127) << 23);  // exact: scaling by a power of two
-  const int32_t n = dfc_rint(t);                              // |t| <= 2^28
-  uint64_t mag = ((uint64_t)(sb & 0x7fffffffu) << 29) + (896ull << 52);
-  mag += (uint64_t)(int64_t)n;
-  return dfc_double(mag | ((uint64_t)neg << 63));
+  float s = dfc_add(h, l);
+  float e = l - (s - h);
+  uint32_t sb = dfc_bits(s);
+  uint32_t E = (sb >> 23) & 0xffu;
+  // Outside 64 <= E <= 253 (tiny, subnormal or huge |s|) both parts are rescaled
+  // by 2^100 or 2^-100 -- exact -- and the double's exponent is corrected at the
+  // end; the common path runs the same (branch-free) instructions.
+  const int32_t bias = E < 64u ? -100 : (E > 253u && E < 255u ? 100 : 0);
+  const float f = bias < 0 ? 0x1p100f : (bias > 0 ? 0x1p-100f : 1.0f);
+  s *= f;
+  e *= f;
+  sb = dfc_bits(s);
+  E = (sb >> 23) & 0xffu;
+  const uint32_t eb = dfc_bits(e);
+  const bool flip = ((sb ^ eb) >> 31) != 0u;  // e points towards zero
+  const bool down = (sb & 0x7fffffu) == 0u && flip && (eb & 0x7fffffffu) != 0u;
+  const int32_t Ee = (int32_t)((eb >> 23) & 0xffu);
+  const uint32_t me = (eb & 0x7fffffu) | (Ee ? 0x800000u : 0u);  // |e| = me * 2^(Ee - 150)
+  // |e| / ulp_d = me * 2^sh with ulp_d = 2^(E - 179), half that below a power of two.
+  const int32_t sh = Ee - (int32_t)E + 29 + (down ? 1 : 0);
+  uint32_t n;
+  if (sh >= 0) {
+    n = sh > 5 ? 0u : me << sh;  // sh <= 5, since |e| <= ulp_f(s) / 2 (= 2^28 ulp_d)
+  } else {
+    const int32_t k = -sh;  // shift right with round-half-even; beyond 25 bits the quotient is < 1/2
+    n = k > 25 ? 0u : (me + ((1u << (k - 1)) - 1u) + ((me >> k) & 1u)) >> k;
+  }
+  uint64_t mag = ((uint64_t)(sb & 0x7fffffffu) << 29) + ((uint64_t)(896 + bias) << 52);
+  mag = flip ? mag - n : mag + n;
+  if ((sb & 0x7fffffffu) == 0u) mag = 0u;                            // zero
+  if (E == 255u) mag = (0x7ffull << 52) | ((sb & 0x7fffffu) ? (1ull << 51) : 0u);  // inf, NaN
+  return dfc_double(mag | ((uint64_t)(sb >> 31) << 63));
 }
 
 }  // namespace sctlgpu

@@ -47,44 +47,26 @@ cudaError_t kmat_f32(const KmatCall& c, int newton) {
   }
 }
 
-// Mixed precision: bbox -> split targets and sources on the common grid ->
-// double-float entries.  Scratch from the stream-ordered allocator.
+// Mixed precision: one launch (points split in the kernel), no scratch.
 template <int KER>
 static cudaError_t run_kmat_df(const KmatCall& c) {
-  constexpr int ND = KDims<KER>::ND;
-  cudaStream_t st = c.stream;
-  const size_t bb_bytes = 256;
-  const size_t trg_off = bb_bytes;
-  const size_t src_off = trg_off + ((size_t)c.nt * sizeof(KmTrg) + 255) / 256 * 256;
-  const size_t total = src_off + (size_t)c.ns * sizeof(KmSrc<ND>);
-  char* scratch = nullptr;
-  SCTLGPU_TRY(cudaMallocAsync((void**)&scratch, total, st));
-  BBox* bb = reinterpret_cast<BBox*>(scratch);
-  KmTrg* trg = reinterpret_cast<KmTrg*>(scratch + trg_off);
-  KmSrc<ND>* src = reinterpret_cast<KmSrc<ND>*>(scratch + src_off);
-  cudaError_t err = cudaSuccess;
-  do {
-    if ((err = compute_bbox(st, c.nt, (const double*)c.r_trg, c.ns, (const double*)c.r_src, bb))) break;
-    kmat_pack_trg_kernel<<<grid_for(c.nt, 256, c.sms), 256, 0, st>>>(c.nt, (const double*)c.r_trg, trg, bb);
-    kmat_pack_src_kernel<ND><<<grid_for(c.ns, 256, c.sms), 256, 0, st>>>(c.ns, (const double*)c.r_src,
-                                                                         (const double*)c.n_src, src, bb);
-    g_launches.fetch_add(2, std::memory_order_relaxed);
-    const double scale = scale_of<KER>();
-    const float sh = (float)scale, sl = (float)(scale - (double)sh);
-    const int64_t tb = (c.nt + KM_THREADS - 1) / KM_THREADS;
-    const int64_t sg = (c.ns + KMD_SROWS - 1) / KMD_SROWS;
-    dim3 grid((unsigned)tb, (unsigned)std::min<int64_t>(sg, 65535));
-    if (c.timing && c.timing->enabled) cudaEventRecord(c.timing->start, st);
-    kernel_matrix_df_kernel<KER><<<grid, KM_THREADS, 0, st>>>(c.nt, trg, c.ns, src, (double*)c.M, sh, sl);
-    if (c.timing && c.timing->enabled) {
-      cudaEventRecord(c.timing->stop, st);
-      c.timing->recorded = true;
-    }
-    g_launches.fetch_add(1, std::memory_order_relaxed);
-    err = cudaGetLastError();
-  } while (0);
-  const cudaError_t e2 = cudaFreeAsync(scratch, st);
-  return err != cudaSuccess ? err : e2;
+  const double scale = scale_of<KER>();
+  const float sh = (float)scale, sl = (float)(scale - (double)sh);
+  const int64_t tb = (c.nt + KM_THREADS - 1) / KM_THREADS;
+  const int64_t sb = (c.ns + KMD_GROUPS * KMD_SROWS - 1) / (KMD_GROUPS * KMD_SROWS);
+  dim3 grid((unsigned)tb, (unsigned)std::min<int64_t>(sb, 65535));
+  // 16-byte row segments: M 16-byte aligned and an even row length (every row then starts aligned;
+  // each warp's segment starts 768 bytes after the previous one's)
+  const int vec = (((uintptr_t)c.M & 15) == 0 && ((c.nt * KDims<KER>::K1) & 1) == 0) ? 1 : 0;
+  if (c.timing && c.timing->enabled) cudaEventRecord(c.timing->start, c.stream);
+  kernel_matrix_df_kernel<KER><<<grid, KM_THREADS, 0, c.stream>>>(
+      c.nt, (const double*)c.r_trg, c.ns, (const double*)c.r_src, (const double*)c.n_src, (double*)c.M, sh, sl, vec);
+  if (c.timing && c.timing->enabled) {
+    cudaEventRecord(c.timing->stop, c.stream);
+    c.timing->recorded = true;
+  }
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  return cudaGetLastError();
 }
 
 cudaError_t kmat_mixed_df(const KmatCall& c) {

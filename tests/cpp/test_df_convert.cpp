@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <random>
 
 #include "../../sctl_gb300/csrc/df_convert.h"
@@ -68,12 +69,32 @@ int main() {
     }
     check(h, l);
   }
+  // tiny, subnormal and huge magnitudes (rescaled), zeros, infinities, NaN
+  for (int it = 0; it < 1000000; ++it) {
+    const int eh = (int)(u01(rng) * 300.0) - 150;  // 2^-150 .. 2^150 (subnormal .. overflow)
+    float h = (float)std::ldexp(1.0 + u01(rng), eh);
+    if (rng() & 1) h = -h;
+    const float l = (float)((u01(rng) - 0.5) * std::ldexp(1.0, eh - 23));
+    if (std::isfinite(h)) check(h, l);
+  }
   check(0.f, 0.f);
   check(-0.f, 0.f);
-  check(1e-30f, 1e-40f);  // below the integer route's range: FP64 route
+  check(-0.f, -0.f);
+  check(1e-30f, 1e-40f);
   check(3e38f, 1e30f);
+  check(-3.4e38f, -1e31f);
   check(1.0f, -1e-30f);
-  check(1.0f, 1e-45f);    // subnormal low part
+  check(1.0f, 1e-45f);  // subnormal low part
+  check(1e-45f, 0.f);   // subnormal
+  check(-1.2e-38f, 1e-45f);
+  {
+    const float inf = std::numeric_limits<float>::infinity();
+    const float nan = std::numeric_limits<float>::quiet_NaN();
+    ++n;
+    if (!(df_to_double(inf, 0.f) == (double)inf && df_to_double(-inf, 0.f) == -(double)inf)) ++bad;
+    ++n;
+    if (!std::isnan(df_to_double(nan, 0.f))) ++bad;
+  }
   std::printf("%ld cases, %ld mismatches\n", n, bad);
   return bad == 0 ? 0 : 1;
 }
