@@ -9,10 +9,9 @@
 // (+896) and the mantissa moved up 29 bits.  Adding e is an integer
 // adjustment of that pattern by round-to-nearest-even(|e| / ulp_d), with
 // ulp_d the double ulp at |s| (half of it when |s| is a power of two and the
-// adjustment points down, where the result lands in the binade below),
-// computed from e's mantissa by a shift with round-half-even (integer
-// operations only; GB300's float-to-integer conversion shares the slow
-// pipe).  The pattern's low 29 bits are zero, so rounding e alone and
+// adjustment points down, where the result lands in the binade below): one
+// exact power-of-two scaling and one float-to-integer conversion.  The
+// pattern's low 29 bits are zero, so rounding e alone and
 // rounding the exact sum agree, ties included.  No FP64 instruction is
 // issued, not even a predicated one: tiny, subnormal and huge values are
 // rescaled by a power of two, zeros and non-finite values are selected.
@@ -27,6 +26,7 @@
 #if defined(__CUDACC__)
 #define SCTLGPU_DFC_HD __host__ __device__ __forceinline__
 #else
+#include <cmath>
 #define SCTLGPU_DFC_HD inline
 #endif
 
@@ -39,6 +39,22 @@ SCTLGPU_DFC_HD uint32_t dfc_bits(float x) {
   uint32_t u;
   std::memcpy(&u, &x, 4);
   return u;
+#endif
+}
+SCTLGPU_DFC_HD float dfc_float(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(u);
+#else
+  float x;
+  std::memcpy(&x, &u, 4);
+  return x;
+#endif
+}
+SCTLGPU_DFC_HD uint32_t dfc_rint(float x) {  // round to nearest, ties to even (0 <= x < 2^31)
+#if defined(__CUDA_ARCH__)
+  return (uint32_t)__float2int_rn(x);
+#else
+  return (uint32_t)std::lrintf(x);
 #endif
 }
 // Rounded sum that is never merged with a product into a multiply-add.
@@ -78,17 +94,10 @@ SCTLGPU_DFC_HD double df_to_double(float h, float l) {
   const uint32_t eb = dfc_bits(e);
   const bool flip = ((sb ^ eb) >> 31) != 0u;  // e points towards zero
   const bool down = (sb & 0x7fffffu) == 0u && flip && (eb & 0x7fffffffu) != 0u;
-  const int32_t Ee = (int32_t)((eb >> 23) & 0xffu);
-  const uint32_t me = (eb & 0x7fffffu) | (Ee ? 0x800000u : 0u);  // |e| = me * 2^(Ee - 150)
-  // |e| / ulp_d = me * 2^sh with ulp_d = 2^(E - 179), half that below a power of two.
-  const int32_t sh = Ee - (int32_t)E + 29 + (down ? 1 : 0);
-  uint32_t n;
-  if (sh >= 0) {
-    n = sh > 5 ? 0u : me << sh;  // sh <= 5, since |e| <= ulp_f(s) / 2 (= 2^28 ulp_d)
-  } else {
-    const int32_t k = -sh;  // shift right with round-half-even; beyond 25 bits the quotient is < 1/2
-    n = k > 25 ? 0u : (me + ((1u << (k - 1)) - 1u) + ((me >> k) & 1u)) >> k;
-  }
+  // n = round-half-even(|e| / ulp_d), ulp_d = 2^(E - 179) (half that below a power of two):
+  // |e| * 2^k is exact (a power-of-two scaling, <= 2^28 since |e| <= ulp_f(s) / 2).
+  const int32_t k = 179 - (int32_t)E + (down ? 1 : 0);
+  const uint32_t n = dfc_rint(dfc_float(eb & 0x7fffffffu) * dfc_float((uint32_t)(k + 127) << 23));
   uint64_t mag = ((uint64_t)(sb & 0x7fffffffu) << 29) + ((uint64_t)(896 + bias) << 52);
   mag = flip ? mag - n : mag + n;
   if ((sb & 0x7fffffffu) == 0u) mag = 0u;                            // zero
