@@ -110,7 +110,7 @@ static void known_answers(R tol) {
 }
 
 // Eval vs KernelMatrix on the 7 x 5 inputs of test-kernel_functions.cpp:487-526.
-template <class K, class R>
+template <class K, class R, long DIG = -1>
 static void eval_vs_matrix(R tol, R* ctx = nullptr) {
   K ker;
   ker.SetCtxPtr(ctx);
@@ -124,9 +124,9 @@ static void eval_vs_matrix(R tol, R* ctx = nullptr) {
     Xn[i * 3 + 1] = 1;
     Xn[i * 3 + 2] = 0;
   }
-  ker.template Eval<R, false>(Vt, Xt, Xs, Xn, Vs);
+  ker.template Eval<R, false, DIG>(Vt, Xt, Xs, Xn, Vs);
   Mat<R> M;
-  ker.template KernelMatrix<R, false>(M, Xt, Xs, Xn);
+  ker.template KernelMatrix<R, false, DIG>(M, Xt, Xs, Xn);
   for (long t = 0; t < Nt; t++)
     for (long k1 = 0; k1 < K1; k1++) {
       R acc = 0;
@@ -155,6 +155,11 @@ int main() {
     eval_vs_matrix<sctlgpu::Laplace3D_DxU, double>(1e-10);
     eval_vs_matrix<sctlgpu::Stokes3D_FxU, double>(1e-10);
     eval_vs_matrix<sctlgpu::Stokes3D_DxU, double>(1e-10);
+    // digits 10: the mixed mode's double-float direct sum and kernel matrix
+    eval_vs_matrix<sctlgpu::Laplace3D_FxU, double, 10>(1e-10);
+    eval_vs_matrix<sctlgpu::Laplace3D_DxU, double, 10>(1e-10);
+    eval_vs_matrix<sctlgpu::Stokes3D_FxU, double, 10>(1e-10);
+    eval_vs_matrix<sctlgpu::Stokes3D_DxU, double, 10>(1e-10);
   }
   known_answers<float>(1e-5f);
   eval_vs_matrix<sctlgpu::Stokes3D_DxU, float>(1e-5f);
