@@ -99,13 +99,14 @@ def test_near_matrix_path_equals_adaptive_path(setup):
     assert capi.load().sctlgpu_device_status(None) == capi.OK
 
 
-@pytest.mark.parametrize("k0,k1", [(1, 1), (3, 3), (1, 9), (4, 3)])
+@pytest.mark.parametrize("k0,k1", [(1, 1), (3, 3), (1, 9), (4, 3), (2, 2), (1, 4)])
 def test_near_matrix_apply_general_layout(cuda, k0, k1):
     """sctlgpu_near_matrix_apply against a numpy restatement of ComputeNearInterac: uneven
     elements (1..7 nodes), element-major blocks, a permuted target-major order, targets without
     pairs (left untouched), accumulation into U."""
     torch = cuda
     from sctl_gb300 import capi
+    lib = capi.load()
     rng = np.random.default_rng(k0 * 10 + k1)
     n_elem, nt, n_pairs = 37, 53, 300
     cnt = rng.integers(1, 8, n_elem)
@@ -127,10 +128,10 @@ def test_near_matrix_apply_general_layout(cuda, k0, k1):
     d = lambda a, dt=torch.int64: torch.from_numpy(np.ascontiguousarray(a)).to(dt).cuda()  # noqa: E731
     g = {"tdsp": d(tdsp), "ord": d(order), "pe": d(pe), "kd": d(kdsp), "ed": d(dsp), "ec": d(cnt),
          "K": d(K, torch.float64), "F": d(F, torch.float64), "U": d(U0, torch.float64)}
-    rc = capi.load().sctlgpu_near_matrix_apply(k0, k1, nt, g["tdsp"].data_ptr(), n_pairs, g["ord"].data_ptr(),
-                                               n_pairs, g["pe"].data_ptr(), g["kd"].data_ptr(), n_elem,
-                                               g["ed"].data_ptr(), g["ec"].data_ptr(), K.size, g["K"].data_ptr(),
-                                               F.size, g["F"].data_ptr(), g["U"].data_ptr(), None)
+    rc = lib.sctlgpu_near_matrix_apply(k0, k1, nt, g["tdsp"].data_ptr(), n_pairs, g["ord"].data_ptr(),
+                                       n_pairs, g["pe"].data_ptr(), g["kd"].data_ptr(), n_elem,
+                                       g["ed"].data_ptr(), g["ec"].data_ptr(), K.size, g["K"].data_ptr(),
+                                       F.size, g["F"].data_ptr(), g["U"].data_ptr(), None)
     assert rc == capi.OK
     got = g["U"].cpu().numpy()
     np.testing.assert_allclose(got, want, rtol=1e-13, atol=1e-13)
