@@ -273,6 +273,23 @@ int sctlgpu_near_matrix_apply(int k0, int k1, int64_t n_trg, const int64_t* trg_
                               const double* F, double* U, void* stream);
 
 /*
+ * The same application with the blocks stored as float pairs: K2[2i], K2[2i+1] = hi, lo
+ * of weight i (hi + lo = the FP64 weight to ~2^-48; same 8 bytes per weight, made once by
+ * sctlgpu_to_float_pairs, in place if wanted), accumulated in double-float on the FP32
+ * pipe -- GB300's FP64 pipe cannot keep up with one FP64 multiply-add per 8 bytes at HBM
+ * speed.  Results within ~1e-14 relative of the FP64 application.  K2 8-byte aligned.
+ */
+int sctlgpu_near_matrix_apply_pairs(int k0, int k1, int64_t n_trg, const int64_t* trg_dsp, int64_t n_near,
+                                    const int64_t* trg_pair, int64_t n_pairs, const int64_t* pair_elem,
+                                    const int64_t* pair_kdsp, int64_t n_elem, const int64_t* elem_nds_dsp,
+                                    const int64_t* elem_nds_cnt, int64_t n_k, const float* K2, int64_t n_f,
+                                    const double* F, double* U, void* stream);
+
+/* x[0..n) -> out[2i], out[2i+1] = hi, lo float pair of x[i] (device pointers, 8-byte
+ * aligned; out may be x itself), asynchronous on `stream`. */
+int sctlgpu_to_float_pairs(int64_t n, const double* x, float* out, void* stream);
+
+/*
  * Arithmetic of sctlgpu_panel_near_correction / sctlgpu_panel_near_weights for the whole
  * process: SCTLGPU_MIXED (default; double-float error-free transformations on the FP32
  * pipe, within ~1e-13 of the FP64 form) or SCTLGPU_F64.  Returns the previous mode, or

@@ -70,6 +70,9 @@ SIGNATURES = {
     "sctlgpu_near_list_destroy": (_i, [_vp]),
     "sctlgpu_near_matrix_apply": (_i, [_i, _i, _i64, _vp, _i64, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp,
                                       _vp, _vp]),
+    "sctlgpu_near_matrix_apply_pairs": (_i, [_i, _i, _i64, _vp, _i64, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp,
+                                            _i64, _vp, _vp, _vp]),
+    "sctlgpu_to_float_pairs": (_i, [_i64, _vp, _vp, _vp]),
     "sctlgpu_panel_arithmetic": (_i, [_i]),
     "sctlgpu_tc_gemm_bf16": (_i, [_i, _i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _vp]),
     "sctlgpu_panel_near_correction": (_i, [_i, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _d,

@@ -106,10 +106,10 @@ class PanelSurface:
         blocks = np.stack([live * self.nn, np.full(live.size, self.nn), starts[live], counts[live]], 1)
         return NearPlan(kernel, blocks, self.np * self.nn, nt, mode=mode, digits=digits, trg_index=t)
 
-    def near_matrix(self, r_trg, pairs, kernel=1, alpha=1.0, max_depth=22):
+    def near_matrix(self, r_trg, pairs, kernel=1, alpha=1.0, max_depth=22, float_pairs=True):
         """SetupNear's precomputation for repeated applications (e.g. every iteration of an
         iterative solver): the accurate weights of every (target, panel) pair, see NearMatrix."""
-        return NearMatrix(self, r_trg, pairs, kernel, alpha, max_depth)
+        return NearMatrix(self, r_trg, pairs, kernel, alpha, max_depth, float_pairs)
 
     def evaluate(self, r_trg, sigma, kernel=1, mode="mixed", digits=10, near_factor=1.0, alpha=1.0, pairs=None,
                  plan=None, matrix=None):
@@ -140,11 +140,14 @@ class NearMatrix:
     :1311-1381) by `sctlgpu_near_matrix_apply`.
 
     Blocks are stored element-major like the reference's K_near: pair j (panel p_j, target t_j)
-    owns the 100 accurate weights W_j = scale * int K(x_t - y) l_a l_b dA (adaptive quadrature in
-    FP64, `sctlgpu_panel_near_weights`).  The target-major order in which each target's pairs are
-    summed (the reference's near_trg_dsp and scatter order) is a stable sort by target."""
+    owns the 100 accurate weights W_j = scale * int K(x_t - y) l_a l_b dA (adaptive quadrature,
+    `sctlgpu_panel_near_weights`).  The target-major order in which each target's pairs are
+    summed (the reference's near_trg_dsp and scatter order) is a stable sort by target.  With
+    `pairs` (default) the FP64 weights are converted in place to float pairs after the setup
+    and applied in double-float by `sctlgpu_near_matrix_apply_pairs` (the HBM-bound form on
+    GB300, whose FP64 pipe cannot keep up with the weights); otherwise in FP64."""
 
-    def __init__(self, S: PanelSurface, r_trg, pairs, kernel=1, alpha=1.0, max_depth=22):
+    def __init__(self, S: PanelSurface, r_trg, pairs, kernel=1, alpha=1.0, max_depth=22, float_pairs=True):
         xt = r_trg.reshape(-1).contiguous()
         self.nt = xt.numel() // 3
         t, p = pairs
@@ -156,6 +159,10 @@ class NearMatrix:
             capi.check(capi.load().sctlgpu_panel_near_weights(
                 kernel, self.n_pairs, t.data_ptr(), p.data_ptr(), self.nt, xt.data_ptr(), S.np, S.X.data_ptr(),
                 float(alpha), int(max_depth), self.W.data_ptr(), stream), "panel_near_weights")
+        self.float_pairs = bool(float_pairs)
+        if self.float_pairs and self.n_pairs:
+            capi.check(capi.load().sctlgpu_to_float_pairs(self.W.numel(), self.W.data_ptr(), self.W.data_ptr(),
+                                                          stream), "to_float_pairs")
         self.trg_pair = torch.argsort(t, stable=True).contiguous()
         counts = torch.bincount(t, minlength=self.nt)
         self.trg_dsp = torch.cat([torch.zeros(1, dtype=torch.int64, device=dev), counts.cumsum(0)]).contiguous()
@@ -172,7 +179,8 @@ class NearMatrix:
     def apply(self, sigma, out):
         """out[t] += sum over t's near pairs of W_j . sigma[panel_j]."""
         f = sigma.reshape(-1).contiguous()
-        capi.check(capi.load().sctlgpu_near_matrix_apply(
+        fn = capi.load().sctlgpu_near_matrix_apply_pairs if self.float_pairs else capi.load().sctlgpu_near_matrix_apply
+        capi.check(fn(
             1, 1, self.nt, self.trg_dsp.data_ptr(), self.n_pairs, self.trg_pair.data_ptr(), self.n_pairs,
             self.pair_elem.data_ptr(), self.pair_kdsp.data_ptr(), self.np, self.elem_nds_dsp.data_ptr(),
             self.elem_nds_cnt.data_ptr(), self.W.numel(), self.W.data_ptr(), f.numel(), f.data_ptr(),

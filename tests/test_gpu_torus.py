@@ -79,15 +79,17 @@ def test_green_identity_point_source(setup):
     assert err.max() < 1e-8, (err.max(), tg["h"][err.argmax()], tg["side"][err.argmax()])
 
 
-def test_near_matrix_path_equals_adaptive_path(setup):
+@pytest.mark.parametrize("float_pairs", [True, False])
+def test_near_matrix_path_equals_adaptive_path(setup, float_pairs):
     """SetupNear once (stored accurate weights), ComputeNearInterac per application: the
-    stored-matrix evaluation equals the matrix-free adaptive one, and keeps Gauss's law."""
+    stored-matrix evaluation equals the matrix-free adaptive one, and keeps Gauss's law, with
+    the weights stored in FP64 or as float pairs."""
     torch, T, S = setup
     tg = T.targets(3000, seed=16, hmin=1e-4, hmax=1.0)
     xt = torch.from_numpy(tg["r_trg"]).cuda().reshape(-1).contiguous()
     pairs = S.near_pairs(xt, 1.0)
     plan = S.smooth_subtraction_plan(3000, pairs)
-    M = S.near_matrix(xt, pairs)
+    M = S.near_matrix(xt, pairs, float_pairs=float_pairs)
     sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()
     a = S.evaluate(xt, sig, pairs=pairs, plan=plan, matrix=M)
     b = S.evaluate(xt, sig, pairs=pairs, plan=plan)
@@ -136,6 +138,20 @@ def test_near_matrix_apply_general_layout(cuda, k0, k1):
     got = g["U"].cpu().numpy()
     np.testing.assert_allclose(got, want, rtol=1e-13, atol=1e-13)
     np.testing.assert_array_equal(got[(nt - 5) * k1:], U0[(nt - 5) * k1:])
+    # the same blocks as float pairs (converted in place), double-float application
+    K2 = g["K"].clone()
+    assert lib.sctlgpu_to_float_pairs(K.size, K2.data_ptr(), K2.data_ptr(), None) == capi.OK
+    hl = K2.cpu().numpy().view(np.float32).reshape(-1, 2).astype(np.float64)
+    assert np.abs(hl.sum(1) - K).max() <= 2.0 ** -46 * np.abs(K).max()
+    U2 = d(U0, torch.float64)
+    rc = lib.sctlgpu_near_matrix_apply_pairs(k0, k1, nt, g["tdsp"].data_ptr(), n_pairs, g["ord"].data_ptr(),
+                                             n_pairs, g["pe"].data_ptr(), g["kd"].data_ptr(), n_elem,
+                                             g["ed"].data_ptr(), g["ec"].data_ptr(), K.size, K2.data_ptr(),
+                                             F.size, g["F"].data_ptr(), U2.data_ptr(), None)
+    assert rc == capi.OK
+    got2 = U2.cpu().numpy()
+    np.testing.assert_allclose(got2, want, rtol=1e-12, atol=1e-12)
+    np.testing.assert_array_equal(got2[(nt - 5) * k1:], U0[(nt - 5) * k1:])
     assert capi.load().sctlgpu_device_status(None) == capi.OK
 
 
