@@ -441,7 +441,7 @@ def torus_section(torch, n_eval=1 << 20, n_train=440000, steps=4000, learned=Tru
     res["labels"] = int(pt.numel())
     res["label_s"] = time.perf_counter() - t0
     f = pair_features_device(T, xtr, pt, pp)
-    L = LearnedCorrection(max_batch=1 << 14, singular=T)
+    L = LearnedCorrection(max_batch=1 << 14, singular=T, basis_inputs=True)
     t0 = time.perf_counter()
     res["train_losses"] = L.fit(f, W, steps=steps, batch=1 << 14, lr=3e-3)
     torch.cuda.synchronize()

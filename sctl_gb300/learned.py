@@ -163,9 +163,13 @@ class LearnedCorrection:
     CALIB_BINS = 16  # bins of |signed log distance feature| in [0, 1]
     CALIB_SAFETY = 2.0
 
-    def __init__(self, n_models=2, max_batch=1 << 14, seeds=(1, 2), singular=None):
-        self.models = [MLP(max_batch=max_batch, seed=s) for s in seeds[:n_models]]
+    def __init__(self, n_models=2, max_batch=1 << 14, seeds=(1, 2), singular=None, basis_inputs=False):
         self.singular = singular
+        # with basis_inputs the networks also see the panel's Lagrange bases at the foot point
+        # (from `singular.basis_features`, 2p more inputs)
+        self.basis_inputs = bool(basis_inputs) and singular is not None
+        in_dim = IN_DIM + (20 if self.basis_inputs else 0)
+        self.models = [MLP(in_dim=in_dim, max_batch=max_batch, seed=s) for s in seeds[:n_models]]
         self.fx = self.fy = None
         self.range = None
         self.calib = self.calib_sum = None
@@ -182,9 +186,11 @@ class LearnedCorrection:
         feats, w = feats[trn], w[trn]
         if self.singular is not None:
             w = w - self.singular.singular_weights(feats)
-        self.fx, self.fy = Standardizer(feats), Standardizer(w)
         self.range = (feats.min(0).values, feats.max(0).values)
-        X, Y = self.fx.fwd(feats).contiguous(), self.fy.fwd(w).contiguous()
+        inp = self.inputs(feats)
+        self.fx, self.fy = Standardizer(inp), Standardizer(w)
+        X, Y = self.fx.fwd(inp).contiguous(), self.fy.fwd(w).contiguous()
+        del inp
         del w
         n = X.shape[0]
         losses = []
@@ -232,6 +238,12 @@ class LearnedCorrection:
         m = sig.mean(1)
         return self.calib_sum[b] * m.abs() + self.calib[b] * (sig - m[:, None]).abs().sum(1)
 
+    def inputs(self, feats):
+        """Network inputs of pairs with features `feats`."""
+        if not self.basis_inputs:
+            return feats
+        return torch.cat([feats, self.singular.basis_features(feats)], 1)
+
     def in_range(self, feats):
         lo, hi = self.range
         return ((feats >= lo) & (feats <= hi)).all(1)
@@ -239,7 +251,7 @@ class LearnedCorrection:
     def predict(self, feats: torch.Tensor):
         """Per-model network outputs in weight units, (n_models, n, 100) FP64: the accurate weights,
         or with `singular` the accurate weights minus their singular part."""
-        x = self.fx.fwd(feats).contiguous()
+        x = self.fx.fwd(self.inputs(feats)).contiguous()
         return torch.stack([self.fy.inv(m.forward(x)) for m in self.models])
 
     def predict_weights(self, feats: torch.Tensor):
@@ -277,7 +289,7 @@ def learned_near_field(S, T, L: LearnedCorrection, r_trg: torch.Tensor, sigma: t
     dens = (sig * L.fy.sd[None]).contiguous()
     const = (sig * L.fy.mu[None]).sum(1)
     idx = torch.nonzero(ok, as_tuple=True)[0]
-    x = L.fx.fwd(f[idx]).contiguous()
+    x = L.fx.fwd(L.inputs(f[idx])).contiguous()
     preds = []
     for m in L.models:
         o = torch.zeros(idx.numel(), dtype=torch.float64, device=xt.device)

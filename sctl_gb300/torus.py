@@ -124,6 +124,9 @@ class Torus:
     def singular_dot(self, f, sig, pp):
         return singular_dot(self, f, sig, pp)
 
+    def basis_features(self, f):
+        return basis_features(self, f)
+
     def upsample_matrix(self, k: int):
         """Interpolation matrix (k*k*p*p, p*p) from a panel's nodes to k x k sub-panels with
         p x p Chebyshev nodes each, the sub-panel weights (fraction of the panel rule), and the
@@ -236,6 +239,13 @@ def singular_part(T: "Torus", f, h0=SINGULAR_H0):
     omega = corner(x2, y2) - corner(x1, y2) - corner(x2, y1) + corner(x1, y1)
     fac = torch.sign(hf) * omega / (4.0 * np.pi) / (1.0 + (z / h0) ** 2)
     return fac, _basis_device(T, s), _basis_device(T, t)
+
+
+def basis_features(T: "Torus", f):
+    """The panel's 1-D Lagrange bases at the pair's clamped foot-point coordinates (s, t),
+    (n, 2p): the functions the weights are built from, as extra network inputs."""
+    import torch
+    return torch.cat([_basis_device(T, f[:, 0]), _basis_device(T, f[:, 1])], 1)
 
 
 def singular_weights(T: "Torus", f):

@@ -45,6 +45,16 @@ def test_singular_part_sharpens_the_network_near_the_surface(trained):
         assert L.calib[b] < 0.25 * L0.calib[b], (b, L.calib[b].item(), L0.calib[b].item())
 
 
+def test_basis_inputs_lower_the_training_loss(trained):
+    """Networks that also see the panel's Lagrange bases at the foot point fit the weights
+    better than networks on the 15 geometric features alone."""
+    torch, T, S, L, losses, (f, W) = trained
+    from sctl_gb300.learned import LearnedCorrection
+    Lb = LearnedCorrection(max_batch=8192, singular=T, basis_inputs=True)
+    lb = Lb.fit(f, W, steps=4000, batch=8192, lr=3e-3)
+    assert max(lb) < 0.8 * min(losses), (lb, losses)
+
+
 def test_learned_correction_gain_over_smooth_rule(trained):
     torch, T, S, L, _, _ = trained
     from sctl_gb300.learned import learned_near_field
