@@ -74,6 +74,18 @@ def test_argument_errors_without_gpu():
     assert na(1, 1, p, n_near=2) == capi.ERR_INVALID_SIZE  # identity order needs n_near <= n_pairs
     assert na(1, 1, None) == capi.ERR_NULL_POINTER
     assert na(1, 0, None) == capi.OK
+    # the float-pair form: same checks, plus 8-byte alignment of the pairs
+    nb = lambda k1, nt, tdsp, K2=p: lib.sctlgpu_near_matrix_apply_pairs(  # noqa: E731
+        1, k1, nt, tdsp, 0, None, 1, p, p, 1, p, p, 6, K2, 6, p, p, None)
+    assert nb(5, 1, p) == capi.ERR_INVALID_SIZE
+    assert nb(1, 1, None) == capi.ERR_NULL_POINTER
+    assert nb(1, 1, p, K2=None) == capi.ERR_NULL_POINTER
+    assert nb(1, 1, p, K2=p + 4) == capi.ERR_INVALID_SIZE
+    assert nb(1, 0, None) == capi.OK
+    assert lib.sctlgpu_to_float_pairs(-1, p, p, None) == capi.ERR_INVALID_SIZE
+    assert lib.sctlgpu_to_float_pairs(3, None, p, None) == capi.ERR_NULL_POINTER
+    assert lib.sctlgpu_to_float_pairs(3, p, p + 4, None) == capi.ERR_INVALID_SIZE
+    assert lib.sctlgpu_to_float_pairs(0, None, None, None) == capi.OK
     for code in (0, -1, -2, -3, -4, -5, -6, -7, -8, -9):
         assert lib.sctlgpu_strerror(code)
 
