@@ -199,8 +199,12 @@ int sctlgpu_near_plan_destroy(sctlgpu_near_plan plan);
  * 0 and subtract with a near plan in the far field's arithmetic when the far field
  * is mixed precision), and scale x the result is
  * atomically added to v_out[trg_map ? trg_map[t] : t].  Kernels: Laplace3D_FxU,
- * Laplace3D_DxU (double arrays, FP64 arithmetic); device pointers, asynchronous on
- * `stream`.  Out-of-range pair indices are skipped and flagged in the device status.
+ * Laplace3D_DxU (double arrays; arithmetic per sctlgpu_panel_arithmetic); device
+ * pointers, asynchronous on `stream`.  Out-of-range pair indices are skipped (status
+ * bit 4).  Each warp queues at most 256 boxes per level, which holds the refinement
+ * for alpha <= ~2.5 (alpha = 1: ~1e-10 relative on the torus workload; alpha = 2:
+ * ~1e-13); when a level would overflow, boxes are integrated unrefined instead of
+ * dropped and status bit 2 is set.
  */
 int sctlgpu_panel_near_correction(int kernel, int64_t n_pairs, const int64_t* pair_trg, const int64_t* pair_panel,
                                   int64_t nt, const double* r_trg, int64_t n_panels, const double* X,
@@ -389,10 +393,17 @@ const char* sctlgpu_last_cuda_error(void);
 
 /*
  * Reads and clears the device-side status word of the current device after
- * synchronising `stream` (bounded-wait timeouts of asynchronous calls made
- * with SCTLGPU_DEVICE_PTRS).  Returns SCTLGPU_OK or SCTLGPU_ERR_DEVICE_TIMEOUT.
+ * synchronising `stream` (what asynchronous calls made with SCTLGPU_DEVICE_PTRS
+ * report).  Returns SCTLGPU_OK or SCTLGPU_ERR_DEVICE_TIMEOUT (any bit set).
  */
 int sctlgpu_device_status(void* stream);
+
+/*
+ * The same, with the word itself in *word: bit 1 a bounded wait gave up (tile copy or
+ * work queue), bit 2 a panel refinement was cut short (boxes integrated unrefined),
+ * bit 4 an index out of range was skipped (near plans, panel pairs, near matrices).
+ */
+int sctlgpu_device_status_word(void* stream, unsigned* word);
 
 /* Number of kernels this library has launched in this process (all threads). */
 int64_t sctlgpu_launch_count(void);

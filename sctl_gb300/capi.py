@@ -73,6 +73,7 @@ SIGNATURES = {
     "sctlgpu_near_matrix_apply_pairs": (_i, [_i, _i, _i64, _vp, _i64, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp,
                                             _i64, _vp, _vp, _vp]),
     "sctlgpu_to_float_pairs": (_i, [_i64, _vp, _vp, _vp]),
+    "sctlgpu_device_status_word": (_i, [_vp, ctypes.POINTER(ctypes.c_uint)]),
     "sctlgpu_panel_arithmetic": (_i, [_i]),
     "sctlgpu_tc_gemm_bf16": (_i, [_i, _i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _vp]),
     "sctlgpu_panel_near_correction": (_i, [_i, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _d,

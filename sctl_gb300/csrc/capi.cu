@@ -444,6 +444,22 @@ int sctlgpu_device_status(void* stream) {
   return take_status(status, (cudaStream_t)stream);
 }
 
+int sctlgpu_device_status_word(void* stream, unsigned* word) {
+  if (!word) return SCTLGPU_ERR_NULL_POINTER;
+  *word = 0;
+  int dev;
+  unsigned* status;
+  int sms;
+  int rc = device_state(&dev, &status, &sms);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(word, status, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(status, 0, sizeof(unsigned), s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? SCTLGPU_OK : record(e);
+}
+
 int64_t sctlgpu_launch_count(void) { return g_launches.load(); }
 
 int sctlgpu_set_timing(int enable) {

@@ -192,15 +192,132 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
       int nnext = 0;
       nleaf = 0;
       const float bz = ldexpf(1.0f, -depth);  // every box of this round has this size
+      // Integrates the queued leaves of this round and empties the leaf buffer.
+      auto integrate_leaves = [&]() {
+        for (int lf = 0; lf < nleaf; ++lf) {
+          const float bs = sm.leaf[lf][0], bt = sm.leaf[lf][1];
+          if (lane < 2 * PQ_GL) {
+            const int i = lane % PQ_GL;
+            // s = b0 + bz * g_i (b0, bz dyadic: exact floats)
+            const f2 g = {c_gl_xh[i], c_gl_xl[i]};
+            const f2 s = dfq::add({lane < PQ_GL ? bs : bt, 0.f}, dfq::mulf(g, bz));
+            f2 l[PQ_P], d[PQ_P];
+            basis_df(s, l, d);
+  #pragma unroll
+            for (int a = 0; a < PQ_P; ++a) {
+              if (lane < PQ_GL) {
+                sm.Ls[i][a] = l[a];
+                sm.Lds[i][a] = d[a];
+              } else {
+                sm.Lt[i][a] = l[a];
+                sm.Ldt[i][a] = d[a];
+              }
+            }
+          }
+          __syncwarp();
+          for (int e = lane; e < 7 * PQ_GL * PQ_P; e += 32) {
+            const int m = e / (PQ_GL * PQ_P), i = (e / PQ_P) % PQ_GL, b = e % PQ_P;
+            if (WEIGHTS && m == 3) continue;  // no density in weights mode
+            const int c = m < 4 ? m : m - 4;
+            const f2* L = m < 4 ? sm.Ls[i] : sm.Lds[i];
+            f2 v = {0.f, 0.f};
+  #pragma unroll
+            for (int a = 0; a < PQ_P; ++a) dfq::fma_acc(v, L[a], sm.F[c][a * PQ_P + b]);
+            sm.A[m][i][b] = dfq::norm(v);
+          }
+          __syncwarp();
+          const float bz2 = bz * bz;
+          for (int gq = lane; gq < PQ_GL * PQ_GL; gq += 32) {
+            const int i = gq / PQ_GL, j = gq % PQ_GL;
+            f2 X[3] = {}, Xs[3] = {}, Xt[3] = {}, sg = {0.f, 0.f};
+  #pragma unroll 2
+            for (int b = 0; b < PQ_P; ++b) {
+              const f2 lt = sm.Lt[j][b], ldt = sm.Ldt[j][b];
+  #pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                dfq::fma_acc(X[c], sm.A[c][i][b], lt);
+                dfq::fma_acc(Xt[c], sm.A[c][i][b], ldt);
+                dfq::fma_acc(Xs[c], sm.A[4 + c][i][b], lt);
+              }
+              if (!WEIGHTS) dfq::fma_acc(sg, sm.A[3][i][b], lt);
+            }
+  #pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              X[c] = dfq::norm(X[c]);  // X = x_s - x_t = -r
+              Xs[c] = dfq::norm(Xs[c]);
+              Xt[c] = dfq::norm(Xt[c]);
+            }
+            // unnormalised normal n = Xs x Xt (|n| = area element of the parameter square)
+            const f2 n0 = dfq::sub(dfq::mul(Xs[1], Xt[2]), dfq::mul(Xs[2], Xt[1]));
+            const f2 n1 = dfq::sub(dfq::mul(Xs[2], Xt[0]), dfq::mul(Xs[0], Xt[2]));
+            const f2 n2 = dfq::sub(dfq::mul(Xs[0], Xt[1]), dfq::mul(Xs[1], Xt[0]));
+            f2 R = dfq::add(dfq::add(dfq::mul(X[0], X[0]), dfq::mul(X[1], X[1])), dfq::mul(X[2], X[2]));
+            float rho, y0;
+            const f2 y = dfq::rsqrt(R, &rho, &y0);
+            const f2 w = dfq::mulf(dfq::mul({c_gl_wh[i], c_gl_wl[i]}, {c_gl_wh[j], c_gl_wl[j]}), bz2);
+            f2 kda;
+            if (KER == 0) {  // single layer: |n| / r
+              const f2 J2 = dfq::add(dfq::add(dfq::mul(n0, n0), dfq::mul(n1, n1)), dfq::mul(n2, n2));
+              const float jh = sqrtf(J2.h);
+              const f2 jp = two_prod(jh, jh);
+              const f2 J = dfq::norm({jh, jh > 0.f ? ((J2.h - jp.h - jp.l) + J2.l) / (2.f * jh) : 0.f});
+              kda = dfq::mul(dfq::mul(J, y), w);
+            } else {  // double layer: (r . n) / r^3 with r = -X
+              const f2 rn = dfq::neg(
+                  dfq::add(dfq::add(dfq::mul(X[0], n0), dfq::mul(X[1], n1)), dfq::mul(X[2], n2)));
+              f2 y3 = dfq::mulf(two_prod(y0, y0), y0);  // y0^3 (1 + 3 rho / 2)
+              y3.l = fmaf(y3.h, 1.5f * rho, y3.l);
+              kda = dfq::mul(dfq::mul(rn, y3), w);
+            }
+            if constexpr (WEIGHTS)
+              sm.Kd[i][j] = dfq::norm(kda);
+            else
+              dfq::fma_acc(acc, kda, dfq::norm(sg));
+          }
+          __syncwarp();
+          if constexpr (WEIGHTS) {
+            for (int e = lane; e < PQ_GL * PQ_P; e += 32) {
+              const int i = e / PQ_P, b = e % PQ_P;
+              f2 v = {0.f, 0.f};
+  #pragma unroll
+              for (int j = 0; j < PQ_GL; ++j) dfq::fma_acc(v, sm.Kd[i][j], sm.Lt[j][b]);
+              sm.T[i][b] = dfq::norm(v);
+            }
+            __syncwarp();
+            for (int e = lane; e < PQ_NODES; e += 32) {
+              const int a = e / PQ_P, b = e % PQ_P;
+              f2 v = sm.W[e];
+  #pragma unroll
+              for (int i = 0; i < PQ_GL; ++i) dfq::fma_acc(v, sm.Ls[i][a], sm.T[i][b]);
+              sm.W[e] = dfq::norm(v);
+            }
+            __syncwarp();
+          }
+          acc = dfq::norm(acc);
+        }
+        nleaf = 0;
+      };
       for (int base = 0; base < ncur; base += 32) {
+        // a batch adds at most 32 leaves: flush the leaves when they might not fit
+        if (nleaf + 32 > PQ_QUEUE) {
+          __syncwarp();
+          integrate_leaves();
+          __syncwarp();
+        }
         const int i = base + lane;
-        bool accept = false, valid = i < ncur;
+        bool accept = false, far = true, valid = i < ncur;
         float bs = 0, bt = 0;
         if (valid) {
           bs = sm.box[cur][i][0];
           bt = sm.box[cur][i][1];
-          accept = box_far_enough([&](int c, int q) { return sm.F[c][q].h; }, bs, bt, bz, (float)p.alpha) ||
-                   depth == p.max_depth;
+          far = box_far_enough([&](int c, int q) { return sm.F[c][q].h; }, bs, bt, bz, (float)p.alpha);
+          accept = far || depth == p.max_depth;
+        }
+        {  // boxes whose four children no longer fit in the next level's queue are integrated
+           // unrefined (flagged) rather than dropped
+          const unsigned want = __ballot_sync(0xffffffffu, valid && !accept);
+          if (valid && !accept && nnext + 4 * __popc(want & ((1u << lane) - 1u)) + 4 > PQ_QUEUE) accept = true;
+          if (lane == 0 && p.status && nnext + 4 * __popc(want) > PQ_QUEUE) atomicOr(p.status, 2u);
         }
         const unsigned acc_mask = __ballot_sync(0xffffffffu, valid && accept);
         const unsigned ref_mask = __ballot_sync(0xffffffffu, valid && !accept);
@@ -221,114 +338,11 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
               sm.box[cur ^ 1][slot + c][1] = bt + (c >> 1) * h;
             }
         }
-        nleaf = min(PQ_QUEUE, nleaf + __popc(acc_mask));
-        nnext = min(PQ_QUEUE, nnext + 4 * __popc(ref_mask));
-        if (nleaf >= PQ_QUEUE || nnext >= PQ_QUEUE) {
-          if (lane == 0 && p.status) atomicOr(p.status, 2u);
-        }
+        nleaf += __popc(acc_mask);  // <= PQ_QUEUE by the flush above
+        nnext += 4 * __popc(ref_mask);  // <= PQ_QUEUE by the room check
       }
       __syncwarp();
-      for (int lf = 0; lf < nleaf; ++lf) {
-        const float bs = sm.leaf[lf][0], bt = sm.leaf[lf][1];
-        if (lane < 2 * PQ_GL) {
-          const int i = lane % PQ_GL;
-          // s = b0 + bz * g_i (b0, bz dyadic: exact floats)
-          const f2 g = {c_gl_xh[i], c_gl_xl[i]};
-          const f2 s = dfq::add({lane < PQ_GL ? bs : bt, 0.f}, dfq::mulf(g, bz));
-          f2 l[PQ_P], d[PQ_P];
-          basis_df(s, l, d);
-#pragma unroll
-          for (int a = 0; a < PQ_P; ++a) {
-            if (lane < PQ_GL) {
-              sm.Ls[i][a] = l[a];
-              sm.Lds[i][a] = d[a];
-            } else {
-              sm.Lt[i][a] = l[a];
-              sm.Ldt[i][a] = d[a];
-            }
-          }
-        }
-        __syncwarp();
-        for (int e = lane; e < 7 * PQ_GL * PQ_P; e += 32) {
-          const int m = e / (PQ_GL * PQ_P), i = (e / PQ_P) % PQ_GL, b = e % PQ_P;
-          if (WEIGHTS && m == 3) continue;  // no density in weights mode
-          const int c = m < 4 ? m : m - 4;
-          const f2* L = m < 4 ? sm.Ls[i] : sm.Lds[i];
-          f2 v = {0.f, 0.f};
-#pragma unroll
-          for (int a = 0; a < PQ_P; ++a) dfq::fma_acc(v, L[a], sm.F[c][a * PQ_P + b]);
-          sm.A[m][i][b] = dfq::norm(v);
-        }
-        __syncwarp();
-        const float bz2 = bz * bz;
-        for (int gq = lane; gq < PQ_GL * PQ_GL; gq += 32) {
-          const int i = gq / PQ_GL, j = gq % PQ_GL;
-          f2 X[3] = {}, Xs[3] = {}, Xt[3] = {}, sg = {0.f, 0.f};
-#pragma unroll 2
-          for (int b = 0; b < PQ_P; ++b) {
-            const f2 lt = sm.Lt[j][b], ldt = sm.Ldt[j][b];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              dfq::fma_acc(X[c], sm.A[c][i][b], lt);
-              dfq::fma_acc(Xt[c], sm.A[c][i][b], ldt);
-              dfq::fma_acc(Xs[c], sm.A[4 + c][i][b], lt);
-            }
-            if (!WEIGHTS) dfq::fma_acc(sg, sm.A[3][i][b], lt);
-          }
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            X[c] = dfq::norm(X[c]);  // X = x_s - x_t = -r
-            Xs[c] = dfq::norm(Xs[c]);
-            Xt[c] = dfq::norm(Xt[c]);
-          }
-          // unnormalised normal n = Xs x Xt (|n| = area element of the parameter square)
-          const f2 n0 = dfq::sub(dfq::mul(Xs[1], Xt[2]), dfq::mul(Xs[2], Xt[1]));
-          const f2 n1 = dfq::sub(dfq::mul(Xs[2], Xt[0]), dfq::mul(Xs[0], Xt[2]));
-          const f2 n2 = dfq::sub(dfq::mul(Xs[0], Xt[1]), dfq::mul(Xs[1], Xt[0]));
-          f2 R = dfq::add(dfq::add(dfq::mul(X[0], X[0]), dfq::mul(X[1], X[1])), dfq::mul(X[2], X[2]));
-          float rho, y0;
-          const f2 y = dfq::rsqrt(R, &rho, &y0);
-          const f2 w = dfq::mulf(dfq::mul({c_gl_wh[i], c_gl_wl[i]}, {c_gl_wh[j], c_gl_wl[j]}), bz2);
-          f2 kda;
-          if (KER == 0) {  // single layer: |n| / r
-            const f2 J2 = dfq::add(dfq::add(dfq::mul(n0, n0), dfq::mul(n1, n1)), dfq::mul(n2, n2));
-            const float jh = sqrtf(J2.h);
-            const f2 jp = two_prod(jh, jh);
-            const f2 J = dfq::norm({jh, jh > 0.f ? ((J2.h - jp.h - jp.l) + J2.l) / (2.f * jh) : 0.f});
-            kda = dfq::mul(dfq::mul(J, y), w);
-          } else {  // double layer: (r . n) / r^3 with r = -X
-            const f2 rn = dfq::neg(
-                dfq::add(dfq::add(dfq::mul(X[0], n0), dfq::mul(X[1], n1)), dfq::mul(X[2], n2)));
-            f2 y3 = dfq::mulf(two_prod(y0, y0), y0);  // y0^3 (1 + 3 rho / 2)
-            y3.l = fmaf(y3.h, 1.5f * rho, y3.l);
-            kda = dfq::mul(dfq::mul(rn, y3), w);
-          }
-          if constexpr (WEIGHTS)
-            sm.Kd[i][j] = dfq::norm(kda);
-          else
-            dfq::fma_acc(acc, kda, dfq::norm(sg));
-        }
-        __syncwarp();
-        if constexpr (WEIGHTS) {
-          for (int e = lane; e < PQ_GL * PQ_P; e += 32) {
-            const int i = e / PQ_P, b = e % PQ_P;
-            f2 v = {0.f, 0.f};
-#pragma unroll
-            for (int j = 0; j < PQ_GL; ++j) dfq::fma_acc(v, sm.Kd[i][j], sm.Lt[j][b]);
-            sm.T[i][b] = dfq::norm(v);
-          }
-          __syncwarp();
-          for (int e = lane; e < PQ_NODES; e += 32) {
-            const int a = e / PQ_P, b = e % PQ_P;
-            f2 v = sm.W[e];
-#pragma unroll
-            for (int i = 0; i < PQ_GL; ++i) dfq::fma_acc(v, sm.Ls[i][a], sm.T[i][b]);
-            sm.W[e] = dfq::norm(v);
-          }
-          __syncwarp();
-        }
-        acc = dfq::norm(acc);
-      }
+      integrate_leaves();
       cur ^= 1;
       ncur = nnext;
     }

@@ -245,8 +245,8 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel(PanelParams p
     for (int q = lane; q < PQ_NODES; q += 32) {
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        sm.F[c][q] = p.X[(pix * PQ_NODES + q) * 3 + c];
-        sm.Fo[c][q] = (float)(sm.F[c][q] - xt[c]);
+        sm.F[c][q] = p.X[(pix * PQ_NODES + q) * 3 + c] - xt[c];  // relative to the target: no cancellation in r
+        sm.Fo[c][q] = (float)sm.F[c][q];
       }
       sm.F[3][q] = p.sigma[pix * PQ_NODES + q];
     }
@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel(PanelParams p
     // Smooth-rule part of this panel, to be subtracted (unless the caller
     // subtracts it in the arithmetic of its far field).
     for (int q = lane; q < PQ_NODES && p.subtract_smooth && !WEIGHTS; q += 32) {
-      const double r[3] = {xt[0] - sm.F[0][q], xt[1] - sm.F[1][q], xt[2] - sm.F[2][q]};
+      const double r[3] = {-sm.F[0][q], -sm.F[1][q], -sm.F[2][q]};
       const double n[3] = {p.N[(pix * PQ_NODES + q) * 3], p.N[(pix * PQ_NODES + q) * 3 + 1],
                            p.N[(pix * PQ_NODES + q) * 3 + 2]};
       acc -= kernel_val<KER>(r, n) * sm.F[3][q] * p.Q[pix * PQ_NODES + q];
@@ -274,17 +274,111 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel(PanelParams p
       // each lane tests boxes of the current round
       int nnext = 0;
       nleaf = 0;
+      auto integrate_leaves = [&]() {
+        // Integrate this round's leaves.  Per box, tensor-product interpolation:
+        // basis matrices at the box's Gauss points (lanes 0-19), then A = L_s F and
+        // L_s' F (stage 1), then every node from two 10-term dot products per field.
+        for (int lf = 0; lf < nleaf; ++lf) {
+          const double bs = sm.leaf[lf][0], bt = sm.leaf[lf][1], bz = sm.leaf[lf][2];
+          if (lane < 2 * PQ_GL) {
+            const int i = lane % PQ_GL;
+            Basis Bq;
+            basis((lane < PQ_GL ? bs : bt) + bz * c_gl_x[i], Bq);
+  #pragma unroll
+            for (int a = 0; a < PQ_P; ++a) {
+              if (lane < PQ_GL) {
+                sm.Ls[i][a] = Bq.l[a];
+                sm.Lds[i][a] = Bq.d[a];
+              } else {
+                sm.Lt[i][a] = Bq.l[a];
+                sm.Ldt[i][a] = Bq.d[a];
+              }
+            }
+          }
+          __syncwarp();
+          for (int e = lane; e < 7 * PQ_GL * PQ_P; e += 32) {
+            const int m = e / (PQ_GL * PQ_P), i = (e / PQ_P) % PQ_GL, b = e % PQ_P;
+            const int c = m < 4 ? m : m - 4;  // m = 0..3: L_s F_c ; m = 4..6: L_s' F_c
+            const double* L = m < 4 ? sm.Ls[i] : sm.Lds[i];
+            double v = 0.0;
+  #pragma unroll
+            for (int a = 0; a < PQ_P; ++a) v = fma(L[a], sm.F[c][a * PQ_P + b], v);
+            sm.A[m][i][b] = v;
+          }
+          __syncwarp();
+          for (int g = lane; g < PQ_GL * PQ_GL; g += 32) {
+            const int i = g / PQ_GL, j = g % PQ_GL;
+            double X[3] = {0, 0, 0}, Xs[3] = {0, 0, 0}, Xt[3] = {0, 0, 0}, sg = 0;
+  #pragma unroll
+            for (int b = 0; b < PQ_P; ++b) {
+              const double lt = sm.Lt[j][b], ldt = sm.Ldt[j][b];
+  #pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                X[c] = fma(sm.A[c][i][b], lt, X[c]);
+                Xt[c] = fma(sm.A[c][i][b], ldt, Xt[c]);
+                Xs[c] = fma(sm.A[4 + c][i][b], lt, Xs[c]);
+              }
+              sg = fma(sm.A[3][i][b], lt, sg);
+            }
+            double n[3] = {Xs[1] * Xt[2] - Xs[2] * Xt[1], Xs[2] * Xt[0] - Xs[0] * Xt[2],
+                           Xs[0] * Xt[1] - Xs[1] * Xt[0]};
+            const double J = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+            const double iJ = 1.0 / J;
+            n[0] *= iJ;
+            n[1] *= iJ;
+            n[2] *= iJ;
+            const double r[3] = {-X[0], -X[1], -X[2]};  // X = x_s - x_t
+            const double kda = kernel_val<KER>(r, n) * J * (bz * bz * c_gl_w[i] * c_gl_w[j]);
+            if (WEIGHTS)
+              sm.Kd[i][j] = kda;
+            else
+              acc += kda * sg;
+          }
+          __syncwarp();
+          if (WEIGHTS) {
+            for (int e = lane; e < PQ_GL * PQ_P; e += 32) {
+              const int i = e / PQ_P, b = e % PQ_P;
+              double v = 0.0;
+  #pragma unroll
+              for (int j = 0; j < PQ_GL; ++j) v = fma(sm.Kd[i][j], sm.Lt[j][b], v);
+              sm.T[i][b] = v;
+            }
+            __syncwarp();
+            for (int e = lane; e < PQ_NODES; e += 32) {  // each entry owned by one lane
+              const int a = e / PQ_P, b = e % PQ_P;
+              double v = sm.W[e];
+  #pragma unroll
+              for (int i = 0; i < PQ_GL; ++i) v = fma(sm.Ls[i][a], sm.T[i][b], v);
+              sm.W[e] = v;
+            }
+            __syncwarp();
+          }
+        }
+        nleaf = 0;
+      };
       for (int base = 0; base < ncur; base += 32) {
+        // a batch adds at most 32 leaves: flush the leaves when they might not fit
+        if (nleaf + 32 > PQ_QUEUE) {
+          __syncwarp();
+          integrate_leaves();
+          __syncwarp();
+        }
         const int i = base + lane;
-        bool accept = false, valid = i < ncur;
+        bool accept = false, far = true, valid = i < ncur;
         double bs = 0, bt = 0, bz = 0;
         if (valid) {
           bs = sm.box[cur][i][0];
           bt = sm.box[cur][i][1];
           bz = sm.box[cur][i][2];
-          accept = box_far_enough([&](int c, int q) { return sm.Fo[c][q]; }, (float)bs, (float)bt, (float)bz,
-                                  (float)p.alpha) ||
-                   depth == p.max_depth;
+          far = box_far_enough([&](int c, int q) { return sm.Fo[c][q]; }, (float)bs, (float)bt, (float)bz,
+                               (float)p.alpha);
+          accept = far || depth == p.max_depth;
+        }
+        {  // boxes whose four children no longer fit in the next level's queue are integrated
+           // unrefined (flagged) rather than dropped
+          const unsigned want = __ballot_sync(0xffffffffu, valid && !accept);
+          if (valid && !accept && nnext + 4 * __popc(want & ((1u << lane) - 1u)) + 4 > PQ_QUEUE) accept = true;
+          if (lane == 0 && p.status && nnext + 4 * __popc(want) > PQ_QUEUE) atomicOr(p.status, 2u);
         }
         const unsigned acc_mask = __ballot_sync(0xffffffffu, valid && accept);
         const unsigned ref_mask = __ballot_sync(0xffffffffu, valid && !accept);
@@ -307,92 +401,11 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel(PanelParams p
               sm.box[cur ^ 1][slot + c][2] = (float)h;
             }
         }
-        nleaf = min(PQ_QUEUE, nleaf + __popc(acc_mask));
-        nnext = min(PQ_QUEUE, nnext + 4 * __popc(ref_mask));
-        if (nleaf >= PQ_QUEUE || nnext >= PQ_QUEUE) {
-          if (lane == 0 && p.status) atomicOr(p.status, 2u);  // queue overflow: result truncated
-        }
+        nleaf += __popc(acc_mask);  // <= PQ_QUEUE by the flush above
+        nnext += 4 * __popc(ref_mask);  // <= PQ_QUEUE by the room check
       }
       __syncwarp();
-      // Integrate this round's leaves.  Per box, tensor-product interpolation:
-      // basis matrices at the box's Gauss points (lanes 0-19), then A = L_s F and
-      // L_s' F (stage 1), then every node from two 10-term dot products per field.
-      for (int lf = 0; lf < nleaf; ++lf) {
-        const double bs = sm.leaf[lf][0], bt = sm.leaf[lf][1], bz = sm.leaf[lf][2];
-        if (lane < 2 * PQ_GL) {
-          const int i = lane % PQ_GL;
-          Basis Bq;
-          basis((lane < PQ_GL ? bs : bt) + bz * c_gl_x[i], Bq);
-#pragma unroll
-          for (int a = 0; a < PQ_P; ++a) {
-            if (lane < PQ_GL) {
-              sm.Ls[i][a] = Bq.l[a];
-              sm.Lds[i][a] = Bq.d[a];
-            } else {
-              sm.Lt[i][a] = Bq.l[a];
-              sm.Ldt[i][a] = Bq.d[a];
-            }
-          }
-        }
-        __syncwarp();
-        for (int e = lane; e < 7 * PQ_GL * PQ_P; e += 32) {
-          const int m = e / (PQ_GL * PQ_P), i = (e / PQ_P) % PQ_GL, b = e % PQ_P;
-          const int c = m < 4 ? m : m - 4;  // m = 0..3: L_s F_c ; m = 4..6: L_s' F_c
-          const double* L = m < 4 ? sm.Ls[i] : sm.Lds[i];
-          double v = 0.0;
-#pragma unroll
-          for (int a = 0; a < PQ_P; ++a) v = fma(L[a], sm.F[c][a * PQ_P + b], v);
-          sm.A[m][i][b] = v;
-        }
-        __syncwarp();
-        for (int g = lane; g < PQ_GL * PQ_GL; g += 32) {
-          const int i = g / PQ_GL, j = g % PQ_GL;
-          double X[3] = {0, 0, 0}, Xs[3] = {0, 0, 0}, Xt[3] = {0, 0, 0}, sg = 0;
-#pragma unroll
-          for (int b = 0; b < PQ_P; ++b) {
-            const double lt = sm.Lt[j][b], ldt = sm.Ldt[j][b];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              X[c] = fma(sm.A[c][i][b], lt, X[c]);
-              Xt[c] = fma(sm.A[c][i][b], ldt, Xt[c]);
-              Xs[c] = fma(sm.A[4 + c][i][b], lt, Xs[c]);
-            }
-            sg = fma(sm.A[3][i][b], lt, sg);
-          }
-          double n[3] = {Xs[1] * Xt[2] - Xs[2] * Xt[1], Xs[2] * Xt[0] - Xs[0] * Xt[2],
-                         Xs[0] * Xt[1] - Xs[1] * Xt[0]};
-          const double J = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-          const double iJ = 1.0 / J;
-          n[0] *= iJ;
-          n[1] *= iJ;
-          n[2] *= iJ;
-          const double r[3] = {xt[0] - X[0], xt[1] - X[1], xt[2] - X[2]};
-          const double kda = kernel_val<KER>(r, n) * J * (bz * bz * c_gl_w[i] * c_gl_w[j]);
-          if (WEIGHTS)
-            sm.Kd[i][j] = kda;
-          else
-            acc += kda * sg;
-        }
-        __syncwarp();
-        if (WEIGHTS) {
-          for (int e = lane; e < PQ_GL * PQ_P; e += 32) {
-            const int i = e / PQ_P, b = e % PQ_P;
-            double v = 0.0;
-#pragma unroll
-            for (int j = 0; j < PQ_GL; ++j) v = fma(sm.Kd[i][j], sm.Lt[j][b], v);
-            sm.T[i][b] = v;
-          }
-          __syncwarp();
-          for (int e = lane; e < PQ_NODES; e += 32) {  // each entry owned by one lane
-            const int a = e / PQ_P, b = e % PQ_P;
-            double v = sm.W[e];
-#pragma unroll
-            for (int i = 0; i < PQ_GL; ++i) v = fma(sm.Ls[i][a], sm.T[i][b], v);
-            sm.W[e] = v;
-          }
-          __syncwarp();
-        }
-      }
+      integrate_leaves();
       cur ^= 1;
       ncur = nnext;
     }

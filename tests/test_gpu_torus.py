@@ -181,3 +181,76 @@ def test_double_float_panel_quadrature_matches_fp64(setup, kernel):
     assert np.abs(cdf - c64).max() <= 1e-11 * np.abs(c64).max(), np.abs(cdf - c64).max() / np.abs(c64).max()
     assert np.abs(wdf - w64).max() <= 2e-11 * np.abs(w64).max()
     assert lib.sctlgpu_device_status(None) == capi.OK
+
+
+@pytest.fixture(scope="module")
+def oracle_pairs(setup):
+    """Ten (target, panel) pairs -- targets 1e-4 .. 0.5 panel sizes off their own panel, each with
+    its own and the next panel -- and their weights from the CPU restatement of the quadrature
+    (oracle/panel_oracle.py: alpha = 2 and 14 x 14 Gauss points, converged to rounding)."""
+    torch, T, S = setup
+    from oracle import panel_oracle as PO
+    hs = [1e-4, 1e-3, 1e-2, 0.1, 0.5]
+    panels = [100, 777, 1500, 2047, 31]
+    xt = np.concatenate([T.targets(1, seed=19 + i, hmin=h, hmax=h, panels=[p])["r_trg"]
+                         for i, (h, p) in enumerate(zip(hs, panels))])
+    pt, pp = [], []
+    for i, p in enumerate(panels):
+        pt += [i, i]
+        pp += [p, p // T.n_phi * T.n_phi + (p % T.n_phi + 1) % T.n_phi]  # own panel, next along phi
+    ref = np.stack([PO.panel_weights(T.X[p], xt[i], kernel=1) for i, p in zip(pt, pp)])
+    return xt, np.array(pt), np.array(pp), ref
+
+
+@pytest.mark.parametrize("arith", ["mixed", "f64"])
+@pytest.mark.parametrize("alpha", [1.0, 2.0])
+def test_panel_weights_match_cpu_oracle(setup, oracle_pairs, arith, alpha):
+    """The GPU's near-singular weights (`sctlgpu_panel_near_weights`, double-float and FP64 forms)
+    against the CPU oracle.  With the oracle's acceptance ratio (alpha = 2) node by node to
+    1e-11; with the default alpha = 1 the weights applied to the torus density (what a potential
+    sees) to 1e-9 -- single weights of the far neighbours differ up to ~1e-7 there, as the
+    8-point rule at one diameter resolves the weights' sum far better than each weight."""
+    torch, T, S = setup
+    from sctl_gb300 import capi
+    from sctl_gb300.learned import panel_weights
+    xt, pt, pp, ref = oracle_pairs
+    lib = capi.load()
+    prev = lib.sctlgpu_panel_arithmetic(capi.MIXED if arith == "mixed" else capi.F64)
+    try:
+        xd = torch.from_numpy(xt).cuda().reshape(-1).contiguous()
+        W = panel_weights(1, torch.from_numpy(pt).cuda(), torch.from_numpy(pp).cuda(), xd, S.X,
+                          alpha=alpha).cpu().numpy()
+    finally:
+        lib.sctlgpu_panel_arithmetic(prev)
+    assert lib.sctlgpu_device_status(None) == capi.OK
+    node = max(np.abs(W[k] - ref[k]).max() / np.abs(ref[k]).max() for k in range(len(pt)))
+    pot = max(abs((W[k] - ref[k]) @ T.sigma[p]) / abs(ref[k] @ T.sigma[p]) for k, p in enumerate(pp))
+    print(f"{arith} alpha {alpha}: node weights {node:.2e}, density-weighted {pot:.2e}")
+    if alpha == 2.0:
+        assert node < 1e-11, node
+    else:
+        assert pot < 1e-9 and node < 1e-6, (pot, node)
+
+
+def test_refinement_overflow_is_flagged_not_dropped(setup, oracle_pairs):
+    """A per-level box queue too small for the refinement (alpha = 4 next to the panel) integrates
+    the remaining boxes unrefined instead of dropping them -- the weights stay finite -- and sets
+    bit 2 of the status word; an ordinary call leaves the word clear."""
+    import ctypes
+    torch, T, S = setup
+    from sctl_gb300 import capi
+    from sctl_gb300.learned import panel_weights
+    xt, pt, pp, ref = oracle_pairs
+    lib = capi.load()
+    word = ctypes.c_uint(0)
+    assert lib.sctlgpu_device_status_word(None, ctypes.byref(word)) == capi.OK
+    xd = torch.from_numpy(xt).cuda().reshape(-1).contiguous()
+    sel = torch.tensor([0]).cuda()  # 1e-4 panel sizes off its own panel
+    W = panel_weights(1, torch.from_numpy(pt).cuda()[sel], torch.from_numpy(pp).cuda()[sel], xd, S.X, alpha=4.0)
+    assert lib.sctlgpu_device_status_word(None, ctypes.byref(word)) == capi.OK
+    assert word.value & 2, word.value
+    w = W.cpu().numpy()[0]
+    assert np.all(np.isfinite(w))
+    panel_weights(1, torch.from_numpy(pt).cuda()[sel], torch.from_numpy(pp).cuda()[sel], xd, S.X, alpha=1.0)
+    assert lib.sctlgpu_device_status_word(None, ctypes.byref(word)) == capi.OK
+    assert word.value == 0
