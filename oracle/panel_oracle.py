@@ -16,8 +16,9 @@ with alpha = 2 and q = 14 (the nearest singularity of a box's integrand lies
 >= 5.6 half-sides away, so each box is exact to rounding), against alpha = 1
 and 8 points on the GPU.
 
-Pinned by a closed form (tests/test_panel_oracle.py): on a flat square panel
-sum_ab W_ab is the solid angle of the square over 4 pi, for any target.
+Pinned by closed forms (tests/test_panel_oracle.py): on a flat square panel
+sum_ab W_ab is, for any target, the solid angle of the square over 4 pi
+(double layer) or the square's 1/r potential over 4 pi (single layer).
 """
 from __future__ import annotations
 
@@ -122,3 +123,19 @@ def square_solid_angle(L, s0, t0, h):
 
     om = f(x2, y2) - f(x1, y2) - f(x2, y1) + f(x1, y1)
     return np.sign(h) * om / (4.0 * np.pi)
+
+
+def square_single_layer(L, s0, t0, h):
+    """int over the square [0, L]^2 (z = 0) of 1 / (4 pi |x - y|) dA, x = (s0 L, t0 L, h)."""
+    x1, x2, y1, y2 = -s0 * L, (1 - s0) * L, -t0 * L, (1 - t0) * L
+    z = abs(h)
+
+    def F(x, y):
+        r = np.sqrt(x * x + y * y + z * z)
+        v = x * np.log(y + r) + y * np.log(x + r)
+        if z > 0:
+            v -= z * np.arctan(x * y / (z * r))
+        return v
+
+    return (F(x2, y2) - F(x1, y2) - F(x2, y1) + F(x1, y1)) / (4.0 * np.pi)
+

@@ -198,13 +198,14 @@ def oracle_pairs(setup):
     for i, p in enumerate(panels):
         pt += [i, i]
         pp += [p, p // T.n_phi * T.n_phi + (p % T.n_phi + 1) % T.n_phi]  # own panel, next along phi
-    ref = np.stack([PO.panel_weights(T.X[p], xt[i], kernel=1) for i, p in zip(pt, pp)])
+    ref = {k: np.stack([PO.panel_weights(T.X[p], xt[i], kernel=k) for i, p in zip(pt, pp)]) for k in (0, 1)}
     return xt, np.array(pt), np.array(pp), ref
 
 
 @pytest.mark.parametrize("arith", ["mixed", "f64"])
 @pytest.mark.parametrize("alpha", [1.0, 2.0])
-def test_panel_weights_match_cpu_oracle(setup, oracle_pairs, arith, alpha):
+@pytest.mark.parametrize("kernel", [1, 0])
+def test_panel_weights_match_cpu_oracle(setup, oracle_pairs, arith, alpha, kernel):
     """The GPU's near-singular weights (`sctlgpu_panel_near_weights`, double-float and FP64 forms)
     against the CPU oracle.  With the oracle's acceptance ratio (alpha = 2) node by node to
     1e-11; with the default alpha = 1 the weights applied to the torus density (what a potential
@@ -213,19 +214,20 @@ def test_panel_weights_match_cpu_oracle(setup, oracle_pairs, arith, alpha):
     torch, T, S = setup
     from sctl_gb300 import capi
     from sctl_gb300.learned import panel_weights
-    xt, pt, pp, ref = oracle_pairs
+    xt, pt, pp, refs = oracle_pairs
+    ref = refs[kernel]
     lib = capi.load()
     prev = lib.sctlgpu_panel_arithmetic(capi.MIXED if arith == "mixed" else capi.F64)
     try:
         xd = torch.from_numpy(xt).cuda().reshape(-1).contiguous()
-        W = panel_weights(1, torch.from_numpy(pt).cuda(), torch.from_numpy(pp).cuda(), xd, S.X,
+        W = panel_weights(kernel, torch.from_numpy(pt).cuda(), torch.from_numpy(pp).cuda(), xd, S.X,
                           alpha=alpha).cpu().numpy()
     finally:
         lib.sctlgpu_panel_arithmetic(prev)
     assert lib.sctlgpu_device_status(None) == capi.OK
     node = max(np.abs(W[k] - ref[k]).max() / np.abs(ref[k]).max() for k in range(len(pt)))
     pot = max(abs((W[k] - ref[k]) @ T.sigma[p]) / abs(ref[k] @ T.sigma[p]) for k, p in enumerate(pp))
-    print(f"{arith} alpha {alpha}: node weights {node:.2e}, density-weighted {pot:.2e}")
+    print(f"kernel {kernel} {arith} alpha {alpha}: node weights {node:.2e}, density-weighted {pot:.2e}")
     if alpha == 2.0:
         assert node < 1e-11, node
     else:
@@ -240,7 +242,7 @@ def test_refinement_overflow_is_flagged_not_dropped(setup, oracle_pairs):
     torch, T, S = setup
     from sctl_gb300 import capi
     from sctl_gb300.learned import panel_weights
-    xt, pt, pp, ref = oracle_pairs
+    xt, pt, pp, refs = oracle_pairs
     lib = capi.load()
     word = ctypes.c_uint(0)
     assert lib.sctlgpu_device_status_word(None, ctypes.byref(word)) == capi.OK

@@ -27,6 +27,18 @@ def test_flat_square_solid_angle(s0, t0, h):
     assert abs(W.sum() - want) < 1e-13, (W.sum(), want)
 
 
+@pytest.mark.parametrize("s0,t0", [(0.3, 0.6), (0.97, 0.02), (1.3, 0.4)])
+@pytest.mark.parametrize("h", [1e-4, 1e-2, -1.0])
+def test_flat_square_single_layer(s0, t0, h):
+    """The single layer's weights of a flat square sum to the square's 1/r potential / 4 pi."""
+    L = 0.1
+    X = flat_square(L)
+    xt = np.array([s0 * L, t0 * L, h * L])
+    W = PO.panel_weights(X, xt, kernel=0)
+    want = PO.square_single_layer(L, s0, t0, h * L)
+    assert abs(W.sum() - want) < 1e-13 * max(1.0, abs(want)), (W.sum(), want)
+
+
 def test_oracle_cost_is_small():
     X = flat_square()
     t0 = time.perf_counter()
