@@ -14,9 +14,16 @@
 // The result is the correction that turns the far-field smooth sum into the
 // accurate value; it is added into v_out[map[target]].
 //
-// One warp per pair; each round, each lane tests one queued box (interpolation
-// at the box centre), then the lanes share the Gauss nodes of the accepted
-// boxes.  FP64 throughout; loops are bounded by the depth and queue limits.
+// One warp per pair, pairs taken from a device work queue; each round, each
+// lane tests one queued box (FP32 interpolation at the box centre: a
+// threshold), then the lanes share the Gauss nodes of the accepted boxes.
+// Node coordinates are kept relative to the target, so r needs no
+// cancellation.  This file holds the FP64 form (behind
+// sctlgpu_panel_arithmetic(SCTLGPU_F64)); panel_df.cuh the default
+// double-float form with the same refinement.  Loops are bounded by the depth
+// and queue limits; leaves are integrated whenever their buffer fills, and a
+// level whose children would overflow the queue integrates the rest unrefined
+// (status bit 2) instead of dropping them.
 #include <cstdint>
 #include <cuda_runtime.h>
 
