@@ -1,7 +1,6 @@
 """The C-ABI library loads, exports every symbol include/*.h declares, and
 rejects bad arguments with status codes -- no GPU needed (the argument checks
 run before any device call)."""
-import ctypes
 import os
 import re
 

@@ -3,7 +3,6 @@ against the CPU oracle evaluated block by block."""
 import numpy as np
 import pytest
 
-import sctl_gb300 as S
 from oracle import oracle as O
 from sctl_gb300 import capi
 from sctl_gb300 import workloads as W
