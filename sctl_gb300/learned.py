@@ -267,8 +267,10 @@ def learned_near_field(S, T, L: LearnedCorrection, r_trg: torch.Tensor, sigma: t
                        stats=None, h_cut=0.1):
     """Potential with learned near corrections where the pair is near-singular (the target's foot point
     inside the panel and its distance below h_cut panel sizes -- elsewhere the smooth rule is already
-    accurate and the network would only add its own error), inside the trained feature range, and the
-    two networks agree to `tol`; the plain adaptive path for every other near pair."""
+    accurate and the network would only add its own error), inside the trained feature range, its
+    calibrated error bound is within `tol` and the two networks agree to `tol`; the plain adaptive path
+    for every other near pair.  The bound needs only the features and the density, so it is checked
+    before the networks run: pairs it rules out cost no inference."""
     from .torus import pair_features_device
     xt = r_trg.reshape(-1).contiguous()
     nt = xt.numel() // 3
@@ -289,26 +291,32 @@ def learned_near_field(S, T, L: LearnedCorrection, r_trg: torch.Tensor, sigma: t
     dens = (sig * L.fy.sd[None]).contiguous()
     const = (sig * L.fy.mu[None]).sum(1)
     idx = torch.nonzero(ok, as_tuple=True)[0]
-    x = L.fx.fwd(L.inputs(f[idx])).contiguous()
-    preds = []
-    for m in L.models:
-        o = torch.zeros(idx.numel(), dtype=torch.float64, device=xt.device)
-        m.forward_dot(x, dens, pp[idx].contiguous(), o)
-        preds.append(o + const[pp[idx]])
-    if L.singular is not None:
-        base = L.singular.singular_dot(f[idx], sig, pp[idx])
-        preds = [p + base for p in preds]
-    bound = L.error_bound(f[idx], sig[pp[idx]])
-    agree = ((preds[0] - preds[1]).abs() <= tol) & (bound <= tol)
-    acc_idx = idx[agree]
-    out.index_add_(0, pt[acc_idx], 0.5 * (preds[0][agree] + preds[1][agree]))
-    rej = torch.ones(pt.numel(), dtype=torch.bool, device=xt.device)
-    rej[acc_idx] = False
-    rt, rp = pt[rej].contiguous(), pp[rej].contiguous()
+    idx = idx[L.error_bound(f[idx], sig[pp[idx]]) <= tol]
+    if idx.numel():
+        x = L.fx.fwd(L.inputs(f[idx])).contiguous()
+        preds = []
+        for m in L.models:
+            o = torch.zeros(idx.numel(), dtype=torch.float64, device=xt.device)
+            m.forward_dot(x, dens, pp[idx].contiguous(), o)
+            preds.append(o + const[pp[idx]])
+        if L.singular is not None:
+            base = L.singular.singular_dot(f[idx], sig, pp[idx])
+            preds = [p + base for p in preds]
+        agree = (preds[0] - preds[1]).abs() <= tol
+        acc_idx = idx[agree]
+        out.index_add_(0, pt[acc_idx], 0.5 * (preds[0][agree] + preds[1][agree]))
+    else:
+        acc_idx = idx
+    if acc_idx.numel():
+        rej = torch.ones(pt.numel(), dtype=torch.bool, device=xt.device)
+        rej[acc_idx] = False
+        rt, rp = pt[rej].contiguous(), pp[rej].contiguous()
+    else:
+        rt, rp = pt, pp
     if rt.numel():
         S.near_correction(xt, sigma, (rt, rp), kernel, alpha, out=out, subtract_smooth=False)
     if stats is not None:
-        stats.update(pairs=int(pt.numel()), candidates=int(ok.sum()), accepted=int(acc_idx.numel()),
-                     fallback=int(rt.numel()),
+        stats.update(pairs=int(pt.numel()), candidates=int(ok.sum()), inferred=int(idx.numel()),
+                     accepted=int(acc_idx.numel()), fallback=int(rt.numel()),
                      accepted_per_target=torch.bincount(pt[acc_idx], minlength=nt))
     return out

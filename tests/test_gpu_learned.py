@@ -81,6 +81,7 @@ def test_tight_tolerance_falls_back_to_plain_path(trained):
     st = {}
     out = learned_near_field(S, T, L, xt, sig, tol=1e-12, stats=st).cpu().numpy()
     assert st["fallback"] >= 0.99 * st["pairs"]
+    assert st["inferred"] == 0  # the calibrated bound rules every pair out before any inference
     assert np.abs(out - plain).max() / np.abs(plain).max() < 1e-8
 
 
@@ -100,7 +101,7 @@ def test_calibrated_gate_bounds_the_error(trained):
         out = learned_near_field(S, T, L, xt, sig, tol=tol, stats=st).cpu().numpy()
         dev = np.abs(out - plain)
         n_acc = st["accepted_per_target"].cpu().numpy()
-        assert st["accepted"] <= st["candidates"]
+        assert st["accepted"] <= st["inferred"] <= st["candidates"]
         assert np.all(dev <= tol * n_acc + 1e-12 * np.abs(plain).max()), (tol, (dev - tol * n_acc).max())
         accepted[tol] = st["accepted"]
     assert accepted[1.0] > 0 and accepted[1.0] >= accepted[1e-1] >= accepted[1e-3], accepted
