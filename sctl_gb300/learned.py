@@ -248,6 +248,43 @@ class LearnedCorrection:
         lo, hi = self.range
         return ((feats >= lo) & (feats <= hi)).all(1)
 
+    def save(self, path: str):
+        """Checkpoint (`sctl_gb300.checkpoint` container): every network's parameters, the feature
+        and weight standardizers, the trained feature range and the calibration tables -- all a
+        trained correction needs to be used again or trained further (Adam restarts)."""
+        from . import checkpoint
+        arrays = {f"model{i}": m.get_params() for i, m in enumerate(self.models)}
+        for tag, st in (("fx", self.fx), ("fy", self.fy)):
+            arrays[f"{tag}_mu"] = st.mu.double().cpu().numpy()
+            arrays[f"{tag}_sd"] = st.sd.double().cpu().numpy()
+        arrays["range_lo"], arrays["range_hi"] = (r.double().cpu().numpy() for r in self.range)
+        arrays["calib"], arrays["calib_sum"] = self.calib.cpu().numpy(), self.calib_sum.cpu().numpy()
+        meta = {"n_models": len(self.models), "in_dim": self.models[0].in_dim, "out_dim": self.models[0].out_dim,
+                "basis_inputs": self.basis_inputs, "singular": self.singular is not None,
+                "calib_bins": self.CALIB_BINS, "calib_safety": self.CALIB_SAFETY}
+        checkpoint.save(path, arrays, meta)
+
+    def load(self, path: str, device="cuda"):
+        """Restores a checkpoint written by `save` into this object (same network shape, the same
+        singular-part and basis-input settings)."""
+        from . import checkpoint
+        arrays, meta = checkpoint.load(path)
+        if (meta.get("n_models") != len(self.models) or meta.get("in_dim") != self.models[0].in_dim or
+                meta.get("out_dim") != self.models[0].out_dim or
+                bool(meta.get("basis_inputs")) != self.basis_inputs or
+                bool(meta.get("singular")) != (self.singular is not None) or
+                meta.get("calib_bins") != self.CALIB_BINS):
+            raise checkpoint.CheckpointError(f"checkpoint {path!r} was written for another configuration: {meta}")
+        for i, m in enumerate(self.models):
+            m.set_params(arrays[f"model{i}"])
+        t = lambda a: torch.from_numpy(a).to(device)  # noqa: E731
+        self.fx, self.fy = Standardizer.__new__(Standardizer), Standardizer.__new__(Standardizer)
+        for tag, st in (("fx", self.fx), ("fy", self.fy)):
+            st.mu, st.sd = t(arrays[f"{tag}_mu"]), t(arrays[f"{tag}_sd"])
+        self.range = (t(arrays["range_lo"]), t(arrays["range_hi"]))
+        self.calib, self.calib_sum = t(arrays["calib"]), t(arrays["calib_sum"])
+        return self
+
     def predict(self, feats: torch.Tensor):
         """Per-model network outputs in weight units, (n_models, n, 100) FP64: the accurate weights,
         or with `singular` the accurate weights minus their singular part."""

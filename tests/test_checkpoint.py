@@ -1,0 +1,47 @@
+"""The checkpoint container of the learned correction (sctl_gb300/checkpoint.py): round trips
+every array and the metadata exactly, and refuses damaged, truncated or foreign files."""
+import numpy as np
+import pytest
+
+from sctl_gb300 import checkpoint as C
+
+
+def sample():
+    rng = np.random.default_rng(0)
+    return {"w": rng.standard_normal(1000).astype(np.float32), "mu": rng.standard_normal((3, 5)),
+            "idx": np.arange(7, dtype=np.int64), "flag": np.array(True), "empty": np.zeros((0, 4))}
+
+
+def test_round_trip(tmp_path):
+    a = sample()
+    path = str(tmp_path / "m.ckpt")
+    C.save(path, a, {"n_models": 2, "note": "x"})
+    b, meta = C.load(path)
+    assert meta == {"n_models": 2, "note": "x"}
+    assert set(a) == set(b)
+    for k in a:
+        assert a[k].dtype == b[k].dtype and a[k].shape == b[k].shape
+        assert np.array_equal(a[k], b[k])
+
+
+@pytest.mark.parametrize("where", [20, -40, -1])
+def test_damage_is_detected(where):
+    blob = bytearray(C.dumps(sample(), {"k": 1}))
+    blob[where] ^= 0x10
+    with pytest.raises(C.CheckpointError):
+        C.loads(bytes(blob))
+
+
+def test_truncated_and_foreign_files_are_refused():
+    blob = C.dumps(sample())
+    with pytest.raises(C.CheckpointError):
+        C.loads(blob[:-5])
+    with pytest.raises(C.CheckpointError):
+        C.loads(b"NOTACKPT" + blob[8:])
+    with pytest.raises(C.CheckpointError):
+        C.loads(b"")
+
+
+def test_unsupported_dtype_is_refused():
+    with pytest.raises(C.CheckpointError):
+        C.dumps({"s": np.array(["a", "b"])})

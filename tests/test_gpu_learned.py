@@ -55,6 +55,22 @@ def test_basis_inputs_lower_the_training_loss(trained):
     assert max(lb) < 0.8 * min(losses), (lb, losses)
 
 
+def test_checkpoint_round_trip(trained, tmp_path):
+    """A trained correction saved and loaded into a fresh object predicts the same weights; a
+    checkpoint of another configuration is refused."""
+    torch, T, S, L, _, (f, W) = trained
+    from sctl_gb300.checkpoint import CheckpointError
+    from sctl_gb300.learned import LearnedCorrection
+    path = str(tmp_path / "corr.ckpt")
+    L.save(path)
+    L2 = LearnedCorrection(max_batch=8192, singular=T).load(path)
+    x = f[:3000]
+    assert torch.equal(L.predict_weights(x), L2.predict_weights(x))
+    assert torch.equal(L.calib, L2.calib) and torch.equal(L.calib_sum, L2.calib_sum)
+    with pytest.raises(CheckpointError):
+        LearnedCorrection(max_batch=8192, singular=T, basis_inputs=True).load(path)
+
+
 def test_learned_correction_gain_over_smooth_rule(trained):
     torch, T, S, L, _, _ = trained
     from sctl_gb300.learned import learned_near_field
