@@ -4,8 +4,11 @@
 torch.distributed: targets and sources are partitioned evenly by global count
 (:565-571), source blocks travel round a ring of np steps (:598-617) and each
 rank adds every visiting block's contribution to its own targets with the
-local evaluator (the GPU library by default).  `max_over_ranks` is the timing
-reduction bench.py uses for replicas.  Covered on CPU with the gloo backend.
+local evaluator (the GPU library by default).  `partition_blocks` shards a
+near list's independent blocks across ranks (longest-processing-time first by
+interactions, no data exchange: each block owns its targets).  `max_over_ranks`
+is the timing reduction bench.py uses for replicas.  Covered on CPU with the
+gloo backend.
 """
 from __future__ import annotations
 
@@ -16,6 +19,25 @@ import torch.distributed as dist
 def partition_range(n: int, rank: int, world: int) -> tuple[int, int]:
     """[begin, end) of rank's share of n items (fmm-wrapper.txx:565-569)."""
     return n * rank // world, n * (rank + 1) // world
+
+
+def partition_blocks(blocks, world: int):
+    """Indices of the near blocks (rows of (src_begin, src_count, trg_begin, trg_count)) each of
+    `world` ranks evaluates: largest first (Ns x Nt interactions), each to the least-loaded rank
+    so far; every rank's list in ascending block order.  Deterministic (ties to the lower rank)."""
+    import heapq
+
+    import numpy as np
+    b = np.asarray(blocks, dtype=np.int64).reshape(-1, 4)
+    cost = b[:, 1] * b[:, 3]
+    order = np.argsort(-cost, kind="stable")
+    heap = [(0, r) for r in range(world)]
+    own = [[] for _ in range(world)]
+    for i in order:
+        load, r = heapq.heappop(heap)
+        own[r].append(int(i))
+        heapq.heappush(heap, (load + int(cost[i]), r))
+    return [np.array(sorted(o), dtype=np.int64) for o in own]
 
 
 def max_over_ranks(x: float, group=None) -> float:

@@ -1,6 +1,7 @@
 """World-size-2 gloo runs of the multi-rank direct sum (ring over ranks, as
-ParticleFMM::EvalDirect) and the max-over-ranks timing reduction, on CPU with
-the oracle as the per-rank evaluator."""
+ParticleFMM::EvalDirect), of near blocks sharded across ranks, and of the
+max-over-ranks timing reduction, on CPU with the oracle as the per-rank
+evaluator."""
 import os
 import socket
 
@@ -69,3 +70,59 @@ def test_partition_range_matches_reference_rule():
     assert parts[0][0] == 0 and parts[-1][1] == n
     assert all(parts[i][1] == parts[i + 1][0] for i in range(world - 1))
     assert max(b - a for a, b in parts) - min(b - a for a, b in parts) <= 1
+
+
+def _blocks_worker(rank, world, port, out_q):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        from oracle import oracle as O
+        from sctl_gb300 import parallel as P
+        from sctl_gb300 import workloads as W
+        d = W.near_blocks(40, 1, seed=9)
+        nt = d["r_trg"].shape[0]
+        mine = P.partition_blocks(d["blocks"], world)[rank]
+        v = np.zeros(nt)
+        for s0, n, t0, m in d["blocks"][mine]:  # this rank's blocks, evaluated locally
+            v[t0:t0 + m] = O.eval(1, d["r_trg"][t0:t0 + m], d["r_src"][s0:s0 + n], d["n_src"][s0:s0 + n],
+                                  d["v_src"][s0:s0 + n])
+        tot = torch.from_numpy(v)
+        dist.all_reduce(tot)  # only to compare: the blocks' targets are disjoint, so this is a gather
+        ref = np.zeros(nt)
+        for s0, n, t0, m in d["blocks"]:
+            ref[t0:t0 + m] = O.eval(1, d["r_trg"][t0:t0 + m], d["r_src"][s0:s0 + n], d["n_src"][s0:s0 + n],
+                                    d["v_src"][s0:s0 + n])
+        out_q.put((rank, float(np.abs(tot.numpy() - ref).max()), len(mine)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_near_blocks_sharded_world2():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_blocks_worker, args=(r, 2, port, q)) for r in range(2)]
+    [p.start() for p in procs]
+    res = [q.get(timeout=120) for _ in range(2)]
+    [p.join(timeout=60) for p in procs]
+    assert all(p.exitcode == 0 for p in procs)
+    assert sum(n for _, _, n in res) == 40
+    for rank, err, _ in res:
+        assert err == 0.0, (rank, err)
+
+
+def test_partition_blocks_covers_and_balances():
+    from sctl_gb300 import workloads as W
+    from sctl_gb300.parallel import partition_blocks
+    b = W.near_blocks(4096, 1, seed=0)["blocks"]
+    cost = b[:, 1] * b[:, 3]
+    for world in (1, 2, 3, 8):
+        parts = partition_blocks(b, world)
+        allidx = np.concatenate(parts)
+        assert np.array_equal(np.sort(allidx), np.arange(len(b)))
+        loads = np.array([cost[p].sum() for p in parts])
+        assert loads.max() <= 1.01 * loads.mean() + cost.max()
+        assert all(np.all(np.diff(p) > 0) for p in parts)
+    assert [p.tolist() for p in partition_blocks(b[:50], 4)] == [p.tolist() for p in partition_blocks(b[:50], 4)]
+
