@@ -126,3 +126,41 @@ def test_partition_blocks_covers_and_balances():
         assert all(np.all(np.diff(p) > 0) for p in parts)
     assert [p.tolist() for p in partition_blocks(b[:50], 4)] == [p.tolist() for p in partition_blocks(b[:50], 4)]
 
+
+
+def _dying_worker(rank, world, port, out_q):
+    import datetime
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=20))
+    if rank == 1:  # this rank fails between steps, before the ring starts, and exits
+        out_q.put((rank, "died"))
+        out_q.close()
+        out_q.join_thread()
+        os._exit(3)
+    try:
+        from sctl_gb300 import parallel as P
+        x = torch.zeros(6, dtype=torch.float64)
+        P.eval_direct(lambda *a: None, x, x, x, torch.zeros(2, dtype=torch.float64), 1)
+        out_q.put((rank, "no error"))
+    except Exception as e:  # the peer's loss surfaces as an error on the ring, not a hang
+        out_q.put((rank, "error: " + type(e).__name__))
+
+
+def test_ring_reports_a_lost_rank():
+    """A rank that dies before the ring makes the other rank's exchange fail with an error within
+    the process-group timeout instead of hanging (failure detected on the host)."""
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_dying_worker, args=(r, 2, port, q)) for r in range(2)]
+    [p.start() for p in procs]
+    try:
+        res = dict(q.get(timeout=120) for _ in range(2))
+        [p.join(timeout=60) for p in procs]
+    finally:
+        for p in procs:  # never leave a rank behind, whatever happened
+            if p.is_alive():
+                p.terminate()
+    assert res[1] == "died" and procs[1].exitcode == 3
+    assert res[0].startswith("error"), res[0]
