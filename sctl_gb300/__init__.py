@@ -26,7 +26,17 @@ from .capi import F32, F64, MIXED, SctlGpuError, kernel_dims, launch_count  # no
 __all__ = ["GenericKernel", "Laplace3D_FxU", "Laplace3D_DxU", "Stokes3D_FxU", "Stokes3D_DxU", "Laplace3D_FxdU",
            "Laplace3D_Fxd2U", "Laplace3D_DxdU", "BiotSavart3D_FxU", "BiotSavart3D_FxdU", "Stokes3D_FxT",
            "Stokes3D_FSxU", "Stokes3D_FxUP", "SctlGpuError", "F64", "F32", "MIXED", "eval_device",
-           "kernel_matrix_device"]
+           "kernel_matrix_device", "digits_for_tolerance"]
+
+
+def digits_for_tolerance(tol: float) -> int:
+    """The `digits` a boundary-integral operator passes to its far-field evaluator for accuracy
+    `tol`: BoundaryIntegralOp::SetAccuracy (boundary_integral.txx:588-595) uses
+    (Integer)(log(tol) / log(0.1)) + 1, truncation toward zero."""
+    import math
+    if not tol > 0:
+        raise ValueError("tolerance must be positive")
+    return int(math.log(tol) / math.log(0.1)) + 1
 
 
 def _is_torch(x):

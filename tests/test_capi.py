@@ -109,3 +109,16 @@ def test_newton_schedule():
 def test_launch_counter_starts_readable():
     assert isinstance(capi.launch_count(), int)
     assert capi.load().sctlgpu_last_kernel_ms() < 0 or True
+
+
+def test_digits_for_tolerance_follows_set_accuracy():
+    """BoundaryIntegralOp::SetAccuracy's tolerance -> digits rule (boundary_integral.txx:588-595),
+    on tolerances away from exact powers of ten (where the floating log ratio may fall either side
+    of the integer)."""
+    import sctl_gb300 as S
+    assert S.digits_for_tolerance(3e-7) == 7
+    assert S.digits_for_tolerance(5e-11) == 11
+    assert S.digits_for_tolerance(0.5) == 1
+    assert S.digits_for_tolerance(2.0) == 0  # log(2)/log(0.1) = -0.30 truncates to 0
+    with pytest.raises(ValueError):
+        S.digits_for_tolerance(0.0)
