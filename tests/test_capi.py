@@ -119,6 +119,6 @@ def test_digits_for_tolerance_follows_set_accuracy():
     assert S.digits_for_tolerance(3e-7) == 7
     assert S.digits_for_tolerance(5e-11) == 11
     assert S.digits_for_tolerance(0.5) == 1
-    assert S.digits_for_tolerance(2.0) == 0  # log(2)/log(0.1) = -0.30 truncates to 0
+    assert S.digits_for_tolerance(2.0) == 1  # log(2)/log(0.1) = -0.30 truncates to 0, plus one
     with pytest.raises(ValueError):
         S.digits_for_tolerance(0.0)
