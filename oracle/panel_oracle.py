@@ -16,9 +16,13 @@ with alpha = 2 and q = 14 (the nearest singularity of a box's integrand lies
 >= 5.6 half-sides away, so each box is exact to rounding), against alpha = 1
 and 8 points on the GPU.
 
-Pinned by closed forms (tests/test_panel_oracle.py): on a flat square panel
-sum_ab W_ab is, for any target, the solid angle of the square over 4 pi
-(double layer) or the square's 1/r potential over 4 pi (single layer).
+Parity unpinned against the reference: the reference has no runnable
+implementation of this path (the QuadElemList NearInterac stubs assert,
+quad_element.cpp:278-286) and no test or fixture for it.  The restatement is
+pinned by closed forms instead (tests/test_panel_oracle.py): on a flat square
+panel sum_ab W_ab is, for any target, the solid angle of the square over
+4 pi (double layer) or the square's 1/r potential over 4 pi (single layer),
+and far from a panel every node's weight equals one dense Gauss rule.
 """
 from __future__ import annotations
 
