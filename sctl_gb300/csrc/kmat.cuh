@@ -1,8 +1,10 @@
 // Dense kernel-matrix emission for GenericKernel::KernelMatrix
 // (generic-kernel.txx:213-329): M[(s*K0+k0)][(t*K1+k1)] = scale * K_{k0,k1}(x_t - y_s, n_s),
-// row-major, source-major.  Write-bandwidth bound for large blocks: each CTA
-// row covers KM_SROWS sources, threads run along targets so every store of a
-// warp is one contiguous segment of a matrix row.
+// row-major, source-major.  Threads run along targets, so a warp's stores to a
+// matrix row are one contiguous segment; grid.y strides over groups of sources.
+// FP64 and FP32 entries come from the plain formula (write-bandwidth bound in
+// FP32, FP64-pipe bound in FP64); the mixed mode evaluates double-float entries
+// and rounds them to FP64 without FP64 instructions (df_convert.h).
 #pragma once
 
 #include "df_convert.h"

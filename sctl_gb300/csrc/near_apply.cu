@@ -12,8 +12,8 @@
 // scatter order), the lanes stream the pair's matrix rows (coalesced, 8-byte
 // loads) against the element's density (L2-resident), and the warp reduces in
 // a fixed order before one add into U -- deterministic, no atomics.  The
-// kernel reads each matrix entry once: it is HBM-bound (8 bytes per
-// multiply-add), so the roofline is the copy bandwidth.
+// kernel reads each matrix entry once, 8 bytes per multiply-add, so its
+// roofline is the copy bandwidth.
 //
 // GB300's FP64 pipe cannot issue one FP64 multiply-add per 8 bytes at HBM
 // speed, so a second form takes the blocks stored as float pairs (hi, lo of
