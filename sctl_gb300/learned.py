@@ -140,9 +140,17 @@ def smooth_weights(kernel, pairs_t, pairs_p, r_trg, X, N, Q):
 
 
 class Standardizer:
+    """Per-column affine map to zero mean and unit deviation (deviations floored at 1e-12)."""
+
     def __init__(self, x: torch.Tensor):
         self.mu = x.mean(0)
         self.sd = x.std(0).clamp_min(1e-12)
+
+    @classmethod
+    def from_arrays(cls, mu: torch.Tensor, sd: torch.Tensor) -> "Standardizer":
+        st = cls.__new__(cls)
+        st.mu, st.sd = mu, sd
+        return st
 
     def fwd(self, x):
         return ((x - self.mu) / self.sd).float()
@@ -278,9 +286,8 @@ class LearnedCorrection:
         for i, m in enumerate(self.models):
             m.set_params(arrays[f"model{i}"])
         t = lambda a: torch.from_numpy(a).to(device)  # noqa: E731
-        self.fx, self.fy = Standardizer.__new__(Standardizer), Standardizer.__new__(Standardizer)
-        for tag, st in (("fx", self.fx), ("fy", self.fy)):
-            st.mu, st.sd = t(arrays[f"{tag}_mu"]), t(arrays[f"{tag}_sd"])
+        self.fx = Standardizer.from_arrays(t(arrays["fx_mu"]), t(arrays["fx_sd"]))
+        self.fy = Standardizer.from_arrays(t(arrays["fy_mu"]), t(arrays["fy_sd"]))
         self.range = (t(arrays["range_lo"]), t(arrays["range_hi"]))
         self.calib, self.calib_sum = t(arrays["calib"]), t(arrays["calib_sum"])
         return self

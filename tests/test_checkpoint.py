@@ -45,3 +45,14 @@ def test_truncated_and_foreign_files_are_refused():
 def test_unsupported_dtype_is_refused():
     with pytest.raises(C.CheckpointError):
         C.dumps({"s": np.array(["a", "b"])})
+
+
+def test_standardizer_from_arrays_matches_fitted():
+    import torch
+    from sctl_gb300.learned import Standardizer
+    x = torch.randn(500, 7, dtype=torch.float64)
+    a = Standardizer(x)
+    b = Standardizer.from_arrays(a.mu.clone(), a.sd.clone())
+    assert torch.equal(a.fwd(x), b.fwd(x))
+    y = torch.randn(10, 7)
+    assert torch.equal(a.inv(y), b.inv(y))
