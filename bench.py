@@ -12,7 +12,7 @@ Prints one JSON line (rank 0).  `value` = whole-job Ginteractions/s with inputs
 resident in HBM; `e2e` = the same through the public host-array API with the
 host<->device copies inside the timed region; `roofline` = the dominant
 kernel's interactions/s against the FP32-issue roofline; `cpu_baseline` = the
-reference's algorithm (the CPU oracle) on this host's cores.
+reference's own CPU Eval (built from its installed headers) on this host's cores.
 """
 from __future__ import annotations
 
@@ -121,31 +121,50 @@ def dist_env():
     return rank, world, local
 
 
-def cpu_baseline(threads=0, n_trg=4096, kernels=KERNELS):
-    """The reference's algorithm on this host (oracle port, FP64, OpenMP), bounded sample."""
+def cpu_baseline(threads=0, n_trg=4096, kernels=KERNELS, digits=DIGITS):
+    """The reference's CPU Eval on this host, FP64, all host cores, on a bounded sample (n_trg
+    targets x all 2^20 sources per kernel; cost is exactly Ns*Nt, so interactions/s compare).
+
+    kind "reference": the reference's own GenericKernel::Eval<double,true> (its SIMD code, built
+    from baseline/_ref by `make -C oracle hot`, OpenMP over all cores), at the same digits as the
+    GPU step.  kind "port" (only where the reference is not installed): the plain-C restatement
+    (oracle/sctl_oracle.c, exact 1/sqrt), which is slower than the reference's SIMD code."""
     from oracle import oracle as O
     from sctl_gb300 import workloads as W
+    use_ref = O.ref_hot_available()
     pairs, secs = 0, 0.0
     for k in kernels:
         d = W.sphere_ball(N_SRC, n_trg, k, seed=100 + k)
         t0 = time.perf_counter()
-        O.eval(k, d["r_trg"], d["r_src"], d["n_src"], d["v_src"], nthreads=threads)
+        if use_ref:
+            O.ref_hot_eval(k, d["r_trg"], d["r_src"], d["n_src"], d["v_src"], digits=digits)
+        else:
+            O.eval(k, d["r_trg"], d["r_src"], d["n_src"], d["v_src"], nthreads=threads)
         secs += time.perf_counter() - t0
         pairs += N_SRC * n_trg
+    names = [NAMES[k] for k in kernels]
+    if use_ref:
+        return {"value": pairs / secs / 1e9, "unit": "Ginteractions/s", "cores": O.ref_hot_threads(),
+                "kind": "reference",
+                "sample": f"{n_trg} targets x 2^{N_SRC.bit_length() - 1} sources per kernel, kernels {names}, FP64, "
+                          f"digits {digits}: the reference's GenericKernel::Eval<double,true> (static digits "
+                          f"dispatcher, OpenMP; built from baseline/_ref with -O3 -mcpu/-march=native), "
+                          f"{secs:.1f} s"}
     cores = threads if threads > 0 else O.max_threads()
     return {"value": pairs / secs / 1e9, "unit": "Ginteractions/s", "cores": cores, "kind": "port",
-            "sample": f"{n_trg} targets x 2^20 sources per kernel, kernels {[NAMES[k] for k in kernels]}, FP64 "
-                      f"(oracle/sctl_oracle.c restating generic-kernel.txx Eval), {secs:.1f} s"}
+            "sample": f"{n_trg} targets x 2^{N_SRC.bit_length() - 1} sources per kernel, kernels {names}, FP64 "
+                      f"(fallback: the reference is not installed in baseline/_ref; oracle/sctl_oracle.c restating "
+                      f"generic-kernel.txx Eval, exact 1/sqrt), {secs:.1f} s"}
 
 
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    n_trg = 2048
+    n_trg = 4096
     samples = []
     for _ in range(args.warmup):
-        cpu_baseline(n_trg=n_trg // 4)
+        cpu_baseline(n_trg=n_trg // 8)
     for _ in range(args.steps):
         samples.append(cpu_baseline(n_trg=n_trg))
     val = statistics.median(s["value"] for s in samples)
@@ -622,7 +641,7 @@ def main():
         d2h += hk["out"].size * 8
         host_in[k] = hk
     kern_objs = {1: S.Laplace3D_DxU, 2: S.Stokes3D_FxU, 3: S.Stokes3D_DxU}
-    e2e_steps = max(1, min(2, args.steps))
+    e2e_steps = max(1, args.steps)
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):

@@ -7,7 +7,11 @@ this module.  It wraps
   Eval / KernelMatrix (sctl_oracle.c), and
 * ``_ref/libsctlref.so`` -- the reference's own header-only implementation,
   wrapped by ref_driver.cpp (only present where the reference checkout was
-  available at build time).
+  available at build time), and
+* ``_ref/libsctlref_hot.so`` -- the reference's own Eval of the four hot-path
+  kernels (ref_hot.cpp), built by ``make -C oracle hot`` wherever the
+  reference is installed in baseline/_ref (also on the GPU host, where it is
+  the timed CPU baseline).
 """
 from __future__ import annotations
 
@@ -20,6 +24,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "libsctl_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libsctlref.so")
+REF_HOT_SO = os.path.join(HERE, "_ref", "libsctlref_hot.so")
 
 KERNELS = {"Laplace3D_FxU": 0, "Laplace3D_DxU": 1, "Stokes3D_FxU": 2, "Stokes3D_DxU": 3,
            "Laplace3D_FxdU": 4, "Laplace3D_Fxd2U": 5, "Laplace3D_DxdU": 6, "BiotSavart3D_FxU": 7,
@@ -33,6 +38,7 @@ HELMHOLTZ = (9, 10, 11, 12)
 
 _lib = None
 _ref = None
+_ref_hot = None
 
 
 def build(force: bool = False) -> None:
@@ -98,6 +104,51 @@ def ref():
         L.ref_near_list_get.restype = i32
         _ref = L
     return _ref
+
+
+def ref_hot_available() -> bool:
+    return os.path.exists(REF_HOT_SO)
+
+
+def ref_hot():
+    global _ref_hot
+    if _ref_hot is None:
+        if not ref_hot_available():
+            raise RuntimeError("reference hot-kernel wrapper not built (oracle/_ref/libsctlref_hot.so)")
+        L = ctypes.CDLL(REF_HOT_SO)
+        i64, vp, i32 = ctypes.c_int64, ctypes.c_void_p, ctypes.c_int
+        L.ref_hot_eval.argtypes = [i32, i32, i32, i64, vp, i64, vp, vp, vp, vp]
+        L.ref_hot_eval.restype = i32
+        L.ref_hot_threads.argtypes = []
+        L.ref_hot_threads.restype = i32
+        _ref_hot = L
+    return _ref_hot
+
+
+def ref_hot_eval(kernel, r_trg, r_src, n_src, v_src, digits=-1, precision="f64", v_trg=None):
+    """The reference's own GenericKernel::Eval<Real,true>(..., digits, self) for kernel ids 0-3
+    (oracle/_ref/libsctlref_hot.so); adds into v_trg when given."""
+    k = _kid(kernel)
+    if k > 3:
+        raise ValueError("ref_hot_eval covers the four hot-path kernels (ids 0-3)")
+    nd, sd, td = DIMS[k]
+    dt = np.float32 if precision == "f32" else np.float64
+    r_trg = np.ascontiguousarray(r_trg, dt).reshape(-1)
+    r_src = np.ascontiguousarray(r_src, dt).reshape(-1)
+    v_src = np.ascontiguousarray(v_src, dt).reshape(-1)
+    n_src = np.ascontiguousarray(n_src, dt).reshape(-1) if nd else None
+    nt, ns = r_trg.size // 3, r_src.size // 3
+    if v_trg is None:
+        v_trg = np.zeros(nt * td, dt)
+    rc = ref_hot().ref_hot_eval(k, int(dt == np.float64), int(digits), nt, _ptr(r_trg), ns, _ptr(r_src),
+                                _ptr(n_src), _ptr(v_src), _ptr(v_trg))
+    if rc:
+        raise RuntimeError(f"reference eval failed: {rc}")
+    return v_trg
+
+
+def ref_hot_threads() -> int:
+    return ref_hot().ref_hot_threads()
 
 
 def _kid(kernel):

@@ -40,7 +40,8 @@ def small_deterministic(k):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=os.environ.get("SCTL_REF", "/root/reference"))
+    ap.add_argument("--ref", default=os.environ.get("SCTL_REF", os.path.join(ROOT, "baseline", "_ref")),
+                    help="installed reference (oracle/install_ref.sh fills baseline/_ref)")
     args = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={args.ref}"], check=True)
     meta = {"reference_veclen_f64": O.ref().ref_vec_len(1), "reference_veclen_f32": O.ref().ref_vec_len(0),

@@ -9,7 +9,8 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INC = os.path.join(ROOT, "include")
 LIBDIR = os.path.join(ROOT, "sctl_gb300")
-REF = os.environ.get("SCTL_REF", "/root/reference")
+# the installed reference (oracle/install_ref.sh), or SCTL_REF=<checkout>
+REF = os.environ.get("SCTL_REF", os.path.join(ROOT, "baseline", "_ref"))
 CXX = shutil.which("g++") or "g++"
 
 
