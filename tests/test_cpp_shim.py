@@ -42,3 +42,27 @@ def test_reference_unit_tests_through_shim(cuda, tmp_path):
     exe = build_shim_test(tmp_path)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and "PASS (0 check(s) failed)" in r.stdout, r.stdout + r.stderr
+
+
+def build_dropin_test(tmp_path):
+    exe = os.path.join(str(tmp_path), "test_dropin_bio")
+    cmd = [CXX, "-std=c++17", "-O2", "-fopenmp", "-I", os.path.join(REF, "include"), "-I", INC,
+           os.path.join(ROOT, "tests", "cpp", "test_dropin_bio.cpp"), "-L", LIBDIR, "-lsctlgpu",
+           "-Wl,-rpath," + LIBDIR, "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
+    return exe
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not os.path.exists(os.path.join(REF, "include", "sctl.hpp")),
+                    reason="reference not installed (oracle/install_ref.sh)")
+def test_reference_call_sites_run_the_gpu_kernel(cuda, tmp_path):
+    """SCTL's own BoundaryIntegralOp::ComputePotential and ParticleFMM::Eval, compiled from the
+    installed reference, with sctlgpu::GpuKernel as their kernel type: equal to the same objects
+    with SCTL's kernels (FP64 <= 1e-12, mixed <= 1e-10)."""
+    exe = build_dropin_test(tmp_path)
+    env = dict(os.environ, OMP_NUM_THREADS=os.environ.get("OMP_NUM_THREADS", "8"))
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=600, env=env)
+    print(r.stdout)
+    assert r.returncode == 0 and "PASS (0 check(s) failed)" in r.stdout, r.stdout + r.stderr

@@ -1,0 +1,114 @@
+"""GPU parity on the sphere/ball workload at full source count (2^20 sources on
+the unit sphere, a 256-target sample of the radius-2 ball) for Laplace3D_DxU,
+Stokes3D_FxU and Stokes3D_DxU in FP64, FP32 and mixed precision at digits 6,
+10 and 14, against the reference's own Eval at the same digits and the FP64
+oracle (the reference's Eval<double> at full digits) --
+tests/golden/reference_config2.npz, made by make_config2_golden.py.
+
+Tolerances (relative l2):
+* FP64 at digits d: within 10^-d of the oracle (the meaning of `digits`,
+  generic-kernel.txx:72-100), and within 1e-12 of the reference's FP64 Eval at
+  the same digits wherever d >= 12 (both then run at full precision).
+* mixed at digits d: within 2 * 10^-d of the oracle (1e-12 at d = 14, where
+  the mixed mode runs the FP64 arithmetic).
+* FP32: the reference's FP32 Eval drifts from the oracle as the source count
+  grows (its per-target sum is one FP32 running sum); the GPU's FP32 form must
+  be at least as close to the oracle (within 10 %, plus 1e-7), and within
+  1e-6 of the reference's FP32 Eval where that one is itself within 5e-7 of
+  the FP64 result for the same FP32 inputs (the source-count sweep locates
+  that N: 2^10 sources for all three kernels on this workload).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import sctl_gb300 as S
+from oracle import oracle as O
+from sctl_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+META = json.load(open(os.path.join(HERE, "golden", "reference_config2.json")))
+NAMES = {1: "Laplace3D_DxU", 2: "Stokes3D_FxU", 3: "Stokes3D_DxU"}
+KER = {1: S.Laplace3D_DxU, 2: S.Stokes3D_FxU, 3: S.Stokes3D_DxU}
+DIGITS = (6, 10, 14)
+
+
+@pytest.fixture(scope="module")
+def g2():
+    return np.load(os.path.join(HERE, "golden", "reference_config2.npz"))
+
+
+_cache = {}
+
+
+def inputs(k, ns=None):
+    ns = ns or META["n_src"]
+    key = (k, ns)
+    if key not in _cache:
+        _cache[key] = W.sphere_ball(ns, META["n_trg"], k, META["seed_base"] + k)
+    return _cache[key]
+
+
+def run(k, d, mode, digits, dtype=np.float64):
+    return KER[k].Eval(None, d["r_trg"].astype(dtype), d["r_src"].astype(dtype), d["n_src"].astype(dtype),
+                       d["v_src"].astype(dtype), digits=digits, mode=mode)
+
+
+@pytest.mark.parametrize("k", sorted(NAMES))
+@pytest.mark.parametrize("digits", DIGITS)
+def test_f64_digits(cuda, g2, k, digits):
+    name = NAMES[k]
+    out = run(k, inputs(k), "f64", digits)
+    oracle = g2[f"{name}/f64_d-1"]
+    assert O.rel_l2(out, oracle) < 10.0 ** (-digits)
+    if digits >= 12:
+        assert O.rel_l2(out, g2[f"{name}/f64_d{digits}"]) < 1e-12
+
+
+@pytest.mark.parametrize("k", sorted(NAMES))
+@pytest.mark.parametrize("digits", DIGITS)
+def test_mixed_digits(cuda, g2, k, digits):
+    name = NAMES[k]
+    out = run(k, inputs(k), "mixed", digits)
+    err = O.rel_l2(out, g2[f"{name}/f64_d-1"])
+    assert err < (1e-12 if digits >= 14 else 2 * 10.0 ** (-digits)), err
+
+
+@pytest.mark.parametrize("k", sorted(NAMES))
+@pytest.mark.parametrize("digits", DIGITS)
+def test_f32_digits_no_worse_than_reference_f32(cuda, g2, k, digits):
+    name = NAMES[k]
+    out = run(k, inputs(k), "f32", digits, np.float32)
+    assert out.dtype == np.float32
+    oracle = g2[f"{name}/f64_d-1"]
+    ref32 = g2[f"{name}/f32_d{digits}"]
+    err, ref_err = O.rel_l2(out, oracle), O.rel_l2(ref32, oracle)
+    print(f"{name} f32 d{digits}: GPU {err:.3e}, reference FP32 {ref_err:.3e}, apart {O.rel_l2(out, ref32):.3e}")
+    assert err <= 1.1 * ref_err + 1e-7
+
+
+@pytest.mark.parametrize("k", sorted(NAMES))
+def test_f32_source_count_sweep(cuda, g2, k):
+    """GPU FP32 against the reference's FP32 Eval over 2^10..2^20 sources (256 targets)."""
+    name = NAMES[k]
+    rows = []
+    for ns in META["sweep_n_src"]:
+        d = inputs(k, ns)
+        out = run(k, d, "f32", -1, np.float32)
+        ref32, ref64 = g2[f"{name}/sweep{ns}/f32_d-1"], g2[f"{name}/sweep{ns}/f64_d-1"]
+        # the FP64 result for the FP32-rounded inputs: what FP32 arithmetic aims at
+        f64r = O.eval(k, *(np.asarray(d[a], np.float32).astype(np.float64)
+                           for a in ("r_trg", "r_src", "n_src", "v_src")))
+        apart, ref_arith = O.rel_l2(out, ref32), O.rel_l2(ref32, f64r)
+        rows.append((ns, apart, ref_arith, O.rel_l2(out, ref64), O.rel_l2(ref32, ref64)))
+        if ref_arith <= 5e-7:
+            assert apart <= 1e-6, (ns, apart, ref_arith)
+        assert O.rel_l2(out, ref64) <= 1.1 * O.rel_l2(ref32, ref64) + 1e-7
+    for r in rows:
+        print(f"{name} ns={r[0]:8d}: GPU vs ref FP32 {r[1]:.2e} (ref FP32 arithmetic error {r[2]:.2e}); "
+              f"vs FP64 oracle: GPU {r[3]:.2e}, ref {r[4]:.2e}")
+    assert rows[0][1] <= 1e-6  # the smallest sweep size: 1e-6 against the reference's FP32 Eval

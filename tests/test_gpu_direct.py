@@ -55,11 +55,17 @@ def test_f64_reduced_digits_within_budget(cuda, golden, k, digits):
 @pytest.mark.parametrize("k", range(4))
 @pytest.mark.parametrize("tag", ["ragged", "one_target"])
 def test_f32_matches_reference_f32(cuda, golden, k, tag):
+    """FP32 against the reference's FP32 Eval: within 1e-6 wherever the reference's own FP32 sum
+    is within 5e-7 of the FP64 result for the same FP32 inputs; and never further from the FP64
+    oracle than the reference's FP32 Eval is (both carry their FP32 summation error)."""
     d = case(NAMES[k], tag)
     out = run(k, d, "f32", -1, np.float32)
     assert out.dtype == np.float32
-    assert O.rel_l2(out, golden[f"{NAMES[k]}/{tag}/eval_f32"]) < 2 * TOL_F32_SMALL
-    assert O.rel_l2(out, golden[f"{NAMES[k]}/{tag}/eval_f64_d-1"]) < 2 * TOL_F32_SMALL
+    ref32, ref64 = golden[f"{NAMES[k]}/{tag}/eval_f32"], golden[f"{NAMES[k]}/{tag}/eval_f64_d-1"]
+    f64r = O.eval(k, *(np.asarray(d[a], np.float32).astype(np.float64) for a in ("r_trg", "r_src", "n_src", "v_src")))
+    if O.rel_l2(ref32, f64r) <= 5e-7:
+        assert O.rel_l2(out, ref32) < TOL_F32_SMALL
+    assert O.rel_l2(out, ref64) <= max(1.5 * O.rel_l2(ref32, ref64), TOL_F32_SMALL)
 
 
 @pytest.mark.parametrize("k", range(4))
