@@ -40,6 +40,7 @@ N_SRC = N_TRG = 1 << 20
 DIGITS = 10
 SMS = 152
 FP32_LANES = 128
+FP64_PER_SM = 2  # FP64 FMA per SM per clock on GB300 (measured 1.9 at the 2070 MHz nominal clock)
 MUFU_PER_SM = 16
 
 
@@ -52,9 +53,12 @@ def peaks():
     return p
 
 
-def roofline_peak_int_s(kernel, sm_mhz):
+def roofline_peak_int_s(kernel, sm_mhz, fp64=False):
+    """Interactions/s at the issue roofline: the algorithmic ops of one interaction on the FP32
+    pipe (128 lanes per SM) or, for the FP64 form, the FP64 pipe (FP64_PER_SM per clock), and one
+    reciprocal square root on the MUFU unit (16 per SM per clock)."""
     ops, mufu = ALG_OPS[kernel]
-    per_clk = min(FP32_LANES / ops, MUFU_PER_SM / mufu)
+    per_clk = min((FP64_PER_SM if fp64 else FP32_LANES) / ops, MUFU_PER_SM / mufu)
     return SMS * sm_mhz * 1e6 * per_clk
 
 
@@ -178,6 +182,29 @@ def run_reference(args):
             "cpu_baseline": cb,
             "e2e": {"value": val, "unit": "Ginteractions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def ref_full_section(kernel=1, digits=DIGITS):
+    """Confirms that the bounded CPU sample extrapolates: the reference's own Eval<double,true> for
+    one kernel over the full 2^20 x 2^20 sphere/ball problem (one call), against the 4096-target
+    sample the CPU legs time.  Cost is exactly Ns*Nt, so the two interaction rates should agree."""
+    from oracle import oracle as O
+    from sctl_gb300 import workloads as W
+    if not O.ref_hot_available():
+        return {"unavailable": "the reference is not installed in baseline/_ref"}
+    d = W.sphere_ball(N_SRC, N_TRG, kernel, seed=100 + kernel)
+    res = {"kernel": NAMES[kernel], "digits": digits, "threads": O.ref_hot_threads()}
+    sub = {a: (v[:4096] if a == "r_trg" else v) for a, v in d.items()}
+    t0 = time.perf_counter()
+    O.ref_hot_eval(kernel, sub["r_trg"], sub["r_src"], sub["n_src"], sub["v_src"], digits=digits)
+    s = time.perf_counter() - t0
+    res["sample_4096_targets"] = {"s": s, "gint_s": 4096 * N_SRC / s / 1e9}
+    t0 = time.perf_counter()
+    O.ref_hot_eval(kernel, d["r_trg"], d["r_src"], d["n_src"], d["v_src"], digits=digits)
+    s = time.perf_counter() - t0
+    res["full_2p20_x_2p20"] = {"s": s, "gint_s": N_TRG * N_SRC / s / 1e9}
+    res["full_over_sample"] = res["full_2p20_x_2p20"]["gint_s"] / res["sample_4096_targets"]["gint_s"]
+    return res
 
 
 def _ev_ms(torch, fn, reps=3):
@@ -495,13 +522,16 @@ def main():
     ap.add_argument("--quick", action="store_true", help="timed region only (for profiler runs)")
     ap.add_argument("--skip-torus", action="store_true", help="omit the near-singular torus section")
     ap.add_argument("--section", choices=["near", "near_panel", "clusters", "cube", "torus", "torus_plain", "mlp",
-                                          "ext", "kmat"],
+                                          "ext", "kmat", "ref_full"],
                     help="run only this secondary workload and print its JSON (profiling of one kernel family)")
     ap.add_argument("--torus-n", type=int, default=1 << 20, help="targets of the torus section")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.section == "ref_full":
+        print(json.dumps({"section": args.section, **ref_full_section()}), flush=True)
+        return
     if args.section:
         import torch
         from sctl_gb300 import capi
@@ -589,31 +619,45 @@ def main():
         return
 
     # --- everything below is outside the timed region ---
-    # FP64 and FP32 plain forms on a 2^16-target slice, for the "mixed vs FP64" ratio.
+    # The precision x digits grid on target slices against all 2^20 sources: FP64 and FP32 at digits
+    # 6 / 10 / 14 (the reference's two real types) and the mixed form at the same digits; throughput,
+    # roofline fraction (FP32 issue for FP32 and mixed, FP64 pipe for FP64) and rel-l2 against the
+    # FP64 oracle on the slice's first 256 targets.
+    from oracle import oracle as O
     detail = {}
-    sub = min(args.n, 1 << 16)
+    sm_mhz = peaks().get("sm_max_mhz", 2070.0)
     for k in KERNELS:
         d = data[k]
         row = {"mixed_ms_per_launch": statistics.median(kern_ms[k]),
                "mixed_gint_s": N_SRC * args.n / (statistics.median(kern_ms[k]) * 1e-3) / 1e9}
-        for mode, dg in (("f64", -1), ("f32", -1), ("mixed", 10)):
-            r_trg = d["r_trg"][:sub * 3] if mode != "f32" else d["r_trg"][:sub * 3].float()
-            args_ = [d[a] if mode != "f32" else d[a].float() for a in ("r_src", "n_src", "v_src")]
-            out = torch.empty(sub * (3 if k >= 2 else 1), dtype=torch.float32 if mode == "f32" else torch.float64,
-                              device=dev)
-            capi.set_timing(True)
-            t = []
-            for _ in range(2):
-                S.eval_device(k, capi.MODE_IDS[mode], dg, sub, r_trg.data_ptr(), N_SRC, args_[0].data_ptr(),
-                              args_[1].data_ptr() if args_[1].numel() else 0, args_[2].data_ptr(), out.data_ptr(),
-                              False, stream.cuda_stream)
-                t.append(capi.last_kernel_ms())
-            capi.set_timing(False)
-            row[f"{mode}_d{dg}_gint_s_slice"] = N_SRC * sub / (min(t) * 1e-3) / 1e9
-        row["mixed_vs_f64"] = row["mixed_d10_gint_s_slice"] / row["f64_d-1_gint_s_slice"]
-        ops, mufu = ALG_OPS[k]
-        peak = roofline_peak_int_s(k, peaks().get("sm_max_mhz", 2070.0))
-        row["roofline_frac_fp32_issue"] = row["mixed_gint_s"] * 1e9 / peak
+        host = {a: d[a].cpu().numpy() for a in ("r_trg", "r_src", "n_src", "v_src")}
+        ref = O.eval(k, host["r_trg"].reshape(-1, 3)[:256], host["r_src"], host["n_src"], host["v_src"])
+        for mode in ("f64", "f32", "mixed"):
+            for dg in (6, 10, 14):
+                sub = min(args.n, (1 << 13) if mode == "f64" else (1 << 16))
+                r_trg = d["r_trg"][:sub * 3] if mode != "f32" else d["r_trg"][:sub * 3].float()
+                args_ = [d[a] if mode != "f32" else d[a].float() for a in ("r_src", "n_src", "v_src")]
+                out = torch.empty(sub * (3 if k >= 2 else 1), dtype=torch.float32 if mode == "f32" else torch.float64,
+                                  device=dev)
+                capi.set_timing(True)
+                t = []
+                for _ in range(2):
+                    S.eval_device(k, capi.MODE_IDS[mode], dg, sub, r_trg.data_ptr(), N_SRC, args_[0].data_ptr(),
+                                  args_[1].data_ptr() if args_[1].numel() else 0, args_[2].data_ptr(), out.data_ptr(),
+                                  False, stream.cuda_stream)
+                    t.append(capi.last_kernel_ms())
+                capi.set_timing(False)
+                gint = N_SRC * sub / (min(t) * 1e-3) / 1e9
+                if mode == "f64":
+                    frac = gint * 1e9 / roofline_peak_int_s(k, sm_mhz, fp64=True)
+                else:
+                    frac = gint * 1e9 / roofline_peak_int_s(k, sm_mhz)
+                got = out.cpu().numpy().astype(np.float64).reshape(sub, -1)[:256].reshape(-1)
+                row[f"{mode}_d{dg}"] = {"gint_s": gint, "targets": sub, "roofline_frac": frac,
+                                        "roofline": "fp64_pipe" if mode == "f64" else "fp32_issue",
+                                        "rel_l2_vs_fp64_oracle": O.rel_l2(got, ref)}
+        row["mixed_d10_vs_f64_d10"] = row["mixed_d10"]["gint_s"] / row["f64_d10"]["gint_s"]
+        row["roofline_frac_fp32_issue"] = row["mixed_gint_s"] * 1e9 / roofline_peak_int_s(k, sm_mhz)
         detail[NAMES[k]] = row
 
     # Accuracy vs the FP64 oracle on 256 targets per kernel.

@@ -186,6 +186,14 @@ int steps_for(int mode, int d) {
   return newton_for(d, kSeedDigitsF64);
 }
 
+// Arithmetic of SCTLGPU_MIXED at `d` digits (the one routing rule, shared with
+// the allocation-free entry).
+int mixed_arith(int d) {
+  if (d <= 7) return MIXED_ARITH_F32;
+  if (d <= kMixedDfMaxDigits) return MIXED_ARITH_DF;
+  return MIXED_ARITH_F64;
+}
+
 cudaError_t run_eval(EvalCall& c, int mode, int d) {
   if (c.kernel > SCTLGPU_STOKES3D_DXU) {  // FP64 arithmetic also for SCTLGPU_MIXED
     if (mode == SCTLGPU_F32) return eval_ext_f32(c, steps_for(mode, d));
@@ -194,9 +202,11 @@ cudaError_t run_eval(EvalCall& c, int mode, int d) {
   const int n = steps_for(mode, d);
   if (mode == SCTLGPU_F64) return eval_f64(c, n);
   if (mode == SCTLGPU_F32) return eval_f32(c, n);
-  if (d <= 7) return eval_mixed_lo(c, n);
-  if (d <= kMixedDfMaxDigits) return eval_mixed_df(c);
-  return eval_f64(c, n);
+  switch (mixed_arith(d)) {
+    case MIXED_ARITH_F32: return eval_mixed_lo(c, n);
+    case MIXED_ARITH_DF: return eval_mixed_df(c);
+    default: return eval_f64(c, n);
+  }
 }
 
 cudaError_t run_kmat(KmatCall& c, int mode, int d) {
@@ -219,6 +229,7 @@ int runtime_record(cudaError_t e) { return record(e); }
 int runtime_effective_digits(int mode, int digits) { return effective_digits(mode, digits); }
 int runtime_steps(int mode, int digits) { return steps_for(mode, digits); }
 int runtime_mixed_df_max_digits() { return kMixedDfMaxDigits; }
+int runtime_mixed_arith(int digits) { return mixed_arith(digits); }
 
 }  // namespace sctlgpu
 

@@ -1,5 +1,6 @@
 // Mixed-precision direct sums (SCTLGPU_MIXED): FP32 arithmetic on split
-// coordinates for digits <= 7, double-float arithmetic for digits 8..13.
+// coordinates for digits <= 7, double-float arithmetic on the packed FP32 pipe
+// (direct_pk.cuh) for digits 8..11.
 #include "launch_direct.cuh"
 
 namespace sctlgpu {
@@ -44,10 +45,10 @@ cudaError_t eval_mixed_lo(const EvalCall& c, int newton) {
 
 cudaError_t eval_mixed_df(const EvalCall& c) {
   switch (c.kernel) {
-    case KER_LFXU: return run_direct<KER_LFXU, MODE_MXDF, 1>(c);
-    case KER_LDXU: return run_direct<KER_LDXU, MODE_MXDF, 1>(c);
-    case KER_SFXU: return run_direct<KER_SFXU, MODE_MXDF, 1>(c);
-    default: return run_direct<KER_SDXU, MODE_MXDF, 1>(c);
+    case KER_LFXU: return run_direct_pk<KER_LFXU>(c);
+    case KER_LDXU: return run_direct_pk<KER_LDXU>(c);
+    case KER_SFXU: return run_direct_pk<KER_SFXU>(c);
+    default: return run_direct_pk<KER_SDXU>(c);
   }
 }
 

@@ -99,5 +99,8 @@ int runtime_record(cudaError_t e);
 int runtime_effective_digits(int mode, int digits);
 int runtime_steps(int mode, int digits);
 int runtime_mixed_df_max_digits();
+// SCTLGPU_MIXED's arithmetic at a digits value (after runtime_effective_digits).
+enum { MIXED_ARITH_F32 = 0, MIXED_ARITH_DF = 1, MIXED_ARITH_F64 = 2 };
+int runtime_mixed_arith(int digits);
 
 }  // namespace sctlgpu

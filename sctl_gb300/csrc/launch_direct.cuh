@@ -8,6 +8,7 @@
 #include <mutex>
 
 #include "direct.cuh"
+#include "direct_pk.cuh"
 #include "launch.h"
 
 namespace sctlgpu {
@@ -112,6 +113,78 @@ cudaError_t run_direct(const EvalCall& c) {
     const int64_t nout = c.nt * K1;
     reduce_partials_kernel<Real><<<grid_for(nout, 256, c.sms), 256, 0, st>>>(
         nout, nsplit, partial, scale_of<KER>(), c.accumulate ? 1 : 0, (Real*)c.v_trg);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    err = cudaGetLastError();
+  } while (0);
+  cudaError_t e2 = cudaFreeAsync(scratch, st);
+  return err != cudaSuccess ? err : e2;
+}
+
+// Mixed precision, double-float arithmetic on the packed FP32 pipe (direct_pk.cuh):
+// the same sequence with pair records.
+template <int KER>
+cudaError_t run_direct_pk(const EvalCall& c) {
+  using RecT = RecPk<KER>;
+  using Cfg = TileCfgPk<KER>;
+  constexpr int K1 = KDims<KER>::K1;
+  cudaStream_t st = c.stream;
+
+  const size_t smem = 2 * Cfg::S * sizeof(RecT) + 2 * sizeof(uint64_t);
+  static int occ = [&] {
+    int o = 0;
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(direct_sum_pk_kernel<KER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, direct_sum_pk_kernel<KER>, Cfg::THREADS, smem);
+    return o > 0 ? o : 1;
+  }();
+
+  const int64_t npairs = (c.ns + 1) / 2;
+  const int64_t per_cta = (int64_t)Cfg::THREADS * Cfg::T;
+  const int64_t tblocks = (c.nt + per_cta - 1) / per_cta;
+  const int nsplit0 = choose_nsplit(tblocks, npairs, Cfg::S, c.sms * occ);
+  int64_t chunk = (npairs + nsplit0 - 1) / nsplit0;
+  chunk = ((chunk + Cfg::S - 1) / Cfg::S) * Cfg::S;
+  const int nsplit = (int)((npairs + chunk - 1) / chunk);
+
+  const size_t rec_bytes = (size_t)npairs * sizeof(RecT);
+  const size_t part_bytes = (size_t)nsplit * (size_t)c.nt * K1 * sizeof(double);
+  const size_t part_off = (rec_bytes + 255) / 256 * 256;
+  const size_t bbox_off = part_off + (part_bytes + 255) / 256 * 256;
+  char* scratch = nullptr;
+  SCTLGPU_TRY(cudaMallocAsync((void**)&scratch, bbox_off + 256, st));
+  RecT* recs = reinterpret_cast<RecT*>(scratch);
+  double* partial = reinterpret_cast<double*>(scratch + part_off);
+  BBox* bb = reinterpret_cast<BBox*>(scratch + bbox_off);
+
+  cudaError_t err = cudaSuccess;
+  do {
+    err = compute_bbox(st, c.nt, (const double*)c.r_trg, c.ns, (const double*)c.r_src, bb);
+    if (err != cudaSuccess) break;
+    pack_pairs_kernel<KER><<<grid_for(npairs, 256, c.sms), 256, 0, st>>>(
+        c.ns, (const double*)c.r_src, (const double*)c.n_src, (const double*)c.v_src, recs, bb);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+
+    DirectParams p;
+    p.nt = c.nt;
+    p.ns = npairs;
+    p.r_trg = c.r_trg;
+    p.recs = recs;
+    p.chunk = chunk;
+    p.partial = partial;
+    p.bbox = bb;
+    p.status = c.status;
+    dim3 grid((unsigned)tblocks, (unsigned)nsplit);
+    if (c.timing && c.timing->enabled) cudaEventRecord(c.timing->start, st);
+    direct_sum_pk_kernel<KER><<<grid, Cfg::THREADS, smem, st>>>(p);
+    if (c.timing && c.timing->enabled) {
+      cudaEventRecord(c.timing->stop, st);
+      c.timing->recorded = true;
+    }
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+
+    const int64_t nout = c.nt * K1;
+    reduce_partials_kernel<double><<<grid_for(nout, 256, c.sms), 256, 0, st>>>(
+        nout, nsplit, partial, scale_of<KER>(), c.accumulate ? 1 : 0, (double*)c.v_trg);
     g_launches.fetch_add(1, std::memory_order_relaxed);
     err = cudaGetLastError();
   } while (0);

@@ -20,6 +20,7 @@
 //     it and produce wrong results; order them on one stream;
 //   - problems whose packed sources and partial sums exceed the array are
 //     rejected with SCTLGPU_ERR_TOO_LARGE before anything is launched.
+#include <atomic>
 #include <mutex>
 
 #include "../../include/sctlgpu.h"
@@ -33,15 +34,16 @@ constexpr size_t kHeaderBytes = 512;  // [0,256): bounding box, [256,260): devic
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
+constexpr int kMaxNoAllocDevices = 64;
 std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[64] = {};
+void* g_noalloc_ptr[kMaxNoAllocDevices] = {};
 
 // Device address of the scratch array on the current device (resolved once per device).
 cudaError_t noalloc_scratch(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (dev < 0 || dev >= kMaxNoAllocDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
   if (!g_noalloc_ptr[dev]) {
     void* p = nullptr;
@@ -56,6 +58,7 @@ cudaError_t noalloc_scratch(void** out) {
 struct NoAllocCall {
   EvalCall c;
   char* scratch;
+  int dev = 0;
   bool too_large = false;
 };
 
@@ -69,13 +72,18 @@ cudaError_t run_noalloc(NoAllocCall& a) {
   cudaStream_t st = c.stream;
 
   const size_t smem = 2 * Cfg::S * sizeof(RecT) + 2 * sizeof(uint64_t);
-  static int occ = [&] {
-    int o = 0;
+  // Resident CTAs per SM, per device (devices of one process may differ).
+  static std::atomic<int> occ_by_dev[kMaxNoAllocDevices] = {};
+  int occ = occ_by_dev[a.dev].load(std::memory_order_relaxed);
+  if (occ <= 0) {
     if (smem > 48 * 1024)
-      cudaFuncSetAttribute(direct_sum_kernel<KER, MODE, NEWTON>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, direct_sum_kernel<KER, MODE, NEWTON>, Cfg::THREADS, smem);
-    return o > 0 ? o : 1;
-  }();
+      SCTLGPU_TRY(cudaFuncSetAttribute(direct_sum_kernel<KER, MODE, NEWTON>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    SCTLGPU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, direct_sum_kernel<KER, MODE, NEWTON>,
+                                                              Cfg::THREADS, smem));
+    occ = occ > 0 ? occ : 1;
+    occ_by_dev[a.dev].store(occ, std::memory_order_relaxed);
+  }
 
   const int64_t per_cta = (int64_t)Cfg::THREADS * Cfg::T;
   const int64_t tblocks = (c.nt + per_cta - 1) / per_cta;
@@ -100,7 +108,7 @@ cudaError_t run_noalloc(NoAllocCall& a) {
   // at zero and the box must start empty; records and partials are fully
   // overwritten below before they are read.
   SCTLGPU_TRY(cudaMemsetAsync(status, 0, sizeof(unsigned), st));
-  if (MODE == MODE_MXLO || MODE == MODE_MXDF)
+  if (MODE == MODE_MXLO)
     SCTLGPU_TRY(compute_bbox(st, c.nt, (const double*)c.r_trg, c.ns, (const double*)c.r_src, bb));
   pack_sources_kernel<KER, MODE, Real><<<grid_for(c.ns, 256, c.sms), 256, 0, st>>>(
       c.ns, (const Real*)c.r_src, (const Real*)c.n_src, (const Real*)c.v_src, recs, bb);
@@ -124,15 +132,93 @@ cudaError_t run_noalloc(NoAllocCall& a) {
   return cudaGetLastError();
 }
 
+// The double-float arithmetic of sctlgpu_eval (pair records on the packed FP32
+// pipe, direct_pk.cuh) in the same fixed scratch layout.
+template <int KER>
+cudaError_t run_noalloc_pk(NoAllocCall& a) {
+  using RecT = RecPk<KER>;
+  using Cfg = TileCfgPk<KER>;
+  constexpr int K1 = KDims<KER>::K1;
+  const EvalCall& c = a.c;
+  cudaStream_t st = c.stream;
+
+  const size_t smem = 2 * Cfg::S * sizeof(RecT) + 2 * sizeof(uint64_t);
+  static std::atomic<int> occ_by_dev[kMaxNoAllocDevices] = {};
+  int occ = occ_by_dev[a.dev].load(std::memory_order_relaxed);
+  if (occ <= 0) {
+    if (smem > 48 * 1024)
+      SCTLGPU_TRY(cudaFuncSetAttribute(direct_sum_pk_kernel<KER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+    SCTLGPU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, direct_sum_pk_kernel<KER>, Cfg::THREADS, smem));
+    occ = occ > 0 ? occ : 1;
+    occ_by_dev[a.dev].store(occ, std::memory_order_relaxed);
+  }
+
+  const int64_t npairs = (c.ns + 1) / 2;
+  const int64_t per_cta = (int64_t)Cfg::THREADS * Cfg::T;
+  const int64_t tblocks = (c.nt + per_cta - 1) / per_cta;
+  const size_t rec_bytes = ((size_t)npairs * sizeof(RecT) + 255) / 256 * 256;
+  auto need = [&](int nsplit) { return kHeaderBytes + rec_bytes + (size_t)nsplit * (size_t)c.nt * K1 * sizeof(double); };
+  int nsplit0 = choose_nsplit(tblocks, npairs, Cfg::S, c.sms * occ);
+  while (nsplit0 > 1 && need(nsplit0) > kNoAllocBytes) --nsplit0;
+  int64_t chunk = (npairs + nsplit0 - 1) / nsplit0;
+  chunk = ((chunk + Cfg::S - 1) / Cfg::S) * Cfg::S;
+  const int nsplit = (int)((npairs + chunk - 1) / chunk);
+  if (need(nsplit) > kNoAllocBytes) {
+    a.too_large = true;
+    return cudaSuccess;
+  }
+
+  BBox* bb = reinterpret_cast<BBox*>(a.scratch);
+  unsigned* status = reinterpret_cast<unsigned*>(a.scratch + 256);
+  RecT* recs = reinterpret_cast<RecT*>(a.scratch + kHeaderBytes);
+  double* partial = reinterpret_cast<double*>(a.scratch + kHeaderBytes + rec_bytes);
+
+  // The array keeps the previous call's contents: status word and box are
+  // reset; records and partials are fully overwritten before they are read.
+  SCTLGPU_TRY(cudaMemsetAsync(status, 0, sizeof(unsigned), st));
+  SCTLGPU_TRY(compute_bbox(st, c.nt, (const double*)c.r_trg, c.ns, (const double*)c.r_src, bb));
+  pack_pairs_kernel<KER><<<grid_for(npairs, 256, c.sms), 256, 0, st>>>(
+      c.ns, (const double*)c.r_src, (const double*)c.n_src, (const double*)c.v_src, recs, bb);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+
+  DirectParams p;
+  p.nt = c.nt;
+  p.ns = npairs;
+  p.r_trg = c.r_trg;
+  p.recs = recs;
+  p.chunk = chunk;
+  p.partial = partial;
+  p.bbox = bb;
+  p.status = status;
+  direct_sum_pk_kernel<KER><<<dim3((unsigned)tblocks, (unsigned)nsplit), Cfg::THREADS, smem, st>>>(p);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  const int64_t nout = c.nt * K1;
+  reduce_partials_kernel<double><<<grid_for(nout, 256, c.sms), 256, 0, st>>>(nout, nsplit, partial, scale_of<KER>(),
+                                                                              c.accumulate ? 1 : 0, (double*)c.v_trg);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  return cudaGetLastError();
+}
+
 template <int KER>
 cudaError_t noalloc_kernel(NoAllocCall& a, int digits) {
-  // The same routing as SCTLGPU_MIXED in sctlgpu_eval: FP32 arithmetic up to 7
-  // digits (no Newton step up to 6 digits, one at 7, from the 2^-22.28 rsqrt
-  // seed), double-float 8..11, FP64 with two Newton steps from 12 digits on.
-  if (digits <= 6) return run_noalloc<KER, MODE_MXLO, 0>(a);
-  if (digits == 7) return run_noalloc<KER, MODE_MXLO, 1>(a);
-  if (digits <= 11) return run_noalloc<KER, MODE_MXDF, 1>(a);
-  return run_noalloc<KER, MODE_F64, 2>(a);
+  // The routing of SCTLGPU_MIXED in sctlgpu_eval, from the same rule
+  // (runtime_mixed_arith) and the same Newton schedule (runtime_steps): FP32
+  // arithmetic on split coordinates, double-float, or FP64.
+  const int steps = runtime_steps(SCTLGPU_MIXED, digits);
+  switch (runtime_mixed_arith(digits)) {
+    case MIXED_ARITH_F32:
+      return steps <= 0 ? run_noalloc<KER, MODE_MXLO, 0>(a) : run_noalloc<KER, MODE_MXLO, 1>(a);
+    case MIXED_ARITH_DF:
+      return run_noalloc_pk<KER>(a);
+    default:
+      switch (steps) {
+        case 0: return run_noalloc<KER, MODE_F64, 0>(a);
+        case 1: return run_noalloc<KER, MODE_F64, 1>(a);
+        case 2: return run_noalloc<KER, MODE_F64, 2>(a);
+        default: return run_noalloc<KER, MODE_F64, 3>(a);
+      }
+  }
 }
 
 }  // namespace
@@ -150,23 +236,26 @@ extern "C" int sctlgpu_eval_mixed_noalloc(int kernel, int digits, int64_t nt, co
   if (flags & ~(unsigned)(SCTLGPU_ACCUMULATE | SCTLGPU_DEVICE_PTRS)) return SCTLGPU_ERR_INVALID_ARGUMENT;
   if ((nt > 0 && (!r_trg || !v_trg)) || (ns > 0 && (!r_src || !v_src || (nd && !n_src))))
     return SCTLGPU_ERR_NULL_POINTER;
-  const int d = (digits < 0 || digits >= 16) ? 15 : digits;
+  const int d = runtime_effective_digits(SCTLGPU_MIXED, digits);
   if (nt == 0) return SCTLGPU_OK;
   cudaStream_t st = (cudaStream_t)stream;
-  if (ns == 0) {
+  if (ns == 0) {  // no sources: v_trg = 0 (or unchanged when accumulating); synchronous like every call
     if (flags & SCTLGPU_ACCUMULATE) return SCTLGPU_OK;
-    return cudaMemsetAsync(v_trg, 0, (size_t)nt * td * sizeof(double), st) == cudaSuccess ? SCTLGPU_OK
-                                                                                           : SCTLGPU_ERR_CUDA;
+    cudaError_t e = cudaMemsetAsync(v_trg, 0, (size_t)nt * td * sizeof(double), st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return runtime_record(e);
   }
   void* scratch = nullptr;
-  if (noalloc_scratch(&scratch) != cudaSuccess) return SCTLGPU_ERR_CUDA;
+  cudaError_t ce = noalloc_scratch(&scratch);
+  if (ce != cudaSuccess) return runtime_record(ce);
   int dev = 0, sms = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess ||
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-    return SCTLGPU_ERR_CUDA;
+  if ((ce = cudaGetDevice(&dev)) != cudaSuccess ||
+      (ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+    return runtime_record(ce);
 
   NoAllocCall a;
   a.scratch = (char*)scratch;
+  a.dev = dev;
   a.c.kernel = kernel;
   a.c.nt = nt;
   a.c.ns = ns;
@@ -188,12 +277,12 @@ extern "C" int sctlgpu_eval_mixed_noalloc(int kernel, int digits, int64_t nt, co
     default: e = noalloc_kernel<KER_SDXU>(a, d); break;
   }
   if (a.too_large) return SCTLGPU_ERR_TOO_LARGE;
-  if (e != cudaSuccess) return SCTLGPU_ERR_CUDA;
+  if (e != cudaSuccess) return runtime_record(e);
   // Synchronous: wait for the stream, then report a device-side wait timeout
   // recorded in the scratch header (copied into a local, not a new buffer).
   unsigned h = 0;
-  if (cudaMemcpyAsync(&h, (char*)scratch + 256, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess)
-    return SCTLGPU_ERR_CUDA;
+  if ((e = cudaMemcpyAsync(&h, (char*)scratch + 256, sizeof(unsigned), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(st)) != cudaSuccess)
+    return runtime_record(e);
   return h ? SCTLGPU_ERR_DEVICE_TIMEOUT : SCTLGPU_OK;
 }

@@ -1,0 +1,66 @@
+"""Generates tests/golden/legacy_torus_dl.npz: the near-singular Laplace
+double-layer potential of the torus workload computed by the REFERENCE's own
+legacy boundary quadrature (sctl::Quadrature, boundary_quadrature.hpp:362-1827,
+built from the installed reference by `make -C oracle legacy`, see
+oracle/legacy_quad.cpp for the three interface gaps it bridges).
+
+    python tests/golden/make_legacy_golden.py
+
+Surface and density: sctl_gb300.torus.Torus(seed=0) -- 64 x 32 panels of
+10 x 10 Chebyshev nodes, R = 1, r = 0.3, the Fourier-mode density.  Targets:
+Torus.targets(256, seed=21, hmin=1e-4, hmax=1) (off-surface distances
+log-uniform in [1e-4, 1] panel sizes, either side).  Quadrature orders
+(order_singular, order_direct) = (24, 24): against the CPU restatement
+(oracle/panel_oracle.py, exact to rounding) the legacy values then agree to
+2.4e-10 rel-l2 and 2.4e-9 at worst on 16 targets; 16 is 200x and 32 is 20x
+less accurate.  Only the potentials are stored; inputs are regenerated.
+"""
+from __future__ import annotations
+
+import json
+import os
+import struct
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from sctl_gb300.torus import Torus  # noqa: E402
+
+N_TRG, SEED, ORDERS = 256, 21, (24, 24)
+
+
+def legacy_potential(T, xt, orders=ORDERS, green=False):
+    exe = os.path.join(ROOT, "oracle", "_ref", "legacy_quad")
+    with tempfile.TemporaryDirectory() as tmp:
+        fin, fout = os.path.join(tmp, "in.bin"), os.path.join(tmp, "out.bin")
+        with open(fin, "wb") as f:
+            f.write(struct.pack("qqddqq", T.n_theta, T.n_phi, 1.0, 0.3, *orders))
+            f.write(np.ascontiguousarray(T.sigma.reshape(-1), np.float64).tobytes())
+            f.write(struct.pack("q", xt.shape[0]))
+            f.write(np.ascontiguousarray(xt, np.float64).tobytes())
+        subprocess.run([exe, fin, fout] + (["green"] if green else []), check=True)
+        out = np.fromfile(fout)
+    return out[:xt.shape[0]], out[xt.shape[0]]
+
+
+def main():
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "legacy"], check=True)
+    T = Torus(seed=0)
+    tg = T.targets(N_TRG, seed=SEED, hmin=1e-4, hmax=1.0)
+    U, green = legacy_potential(T, tg["r_trg"], green=True)
+    np.savez_compressed(os.path.join(HERE, "legacy_torus_dl.npz"), U=U)
+    meta = {"generator": "tests/golden/make_legacy_golden.py", "torus_seed": 0, "n_trg": N_TRG, "target_seed": SEED,
+            "hmin": 1e-4, "hmax": 1.0, "orders": list(ORDERS), "legacy_greens_identity_max_err": green}
+    with open(os.path.join(HERE, "legacy_torus_dl.json"), "w") as fh:
+        json.dump(meta, fh, indent=1, sort_keys=True)
+    print(json.dumps(meta))
+
+
+if __name__ == "__main__":
+    main()

@@ -7,8 +7,9 @@ tests/golden/reference_config2.npz, made by make_config2_golden.py.
 
 Tolerances (relative l2):
 * FP64 at digits d: within 10^-d of the oracle (the meaning of `digits`,
-  generic-kernel.txx:72-100), and within 1e-12 of the reference's FP64 Eval at
-  the same digits wherever d >= 12 (both then run at full precision).
+  generic-kernel.txx:72-100) -- 1e-13 at d = 14, where two FP64 sums of 2^20
+  terms in different orders already differ by ~3e-14 -- and within 1e-12 of
+  the reference's FP64 Eval at the same digits wherever d >= 12.
 * mixed at digits d: within 2 * 10^-d of the oracle (1e-12 at d = 14, where
   the mixed mode runs the FP64 arithmetic).
 * FP32: the reference's FP32 Eval drifts from the oracle as the source count
@@ -64,7 +65,10 @@ def test_f64_digits(cuda, g2, k, digits):
     name = NAMES[k]
     out = run(k, inputs(k), "f64", digits)
     oracle = g2[f"{name}/f64_d-1"]
-    assert O.rel_l2(out, oracle) < 10.0 ** (-digits)
+    err = O.rel_l2(out, oracle)
+    print(f"{name} f64 d{digits}: {err:.3e} from the oracle")
+    # below 1e-13 the two FP64 sums of 2^20 terms differ by their own rounding (summation order)
+    assert err < max(10.0 ** (-digits), 1e-13)
     if digits >= 12:
         assert O.rel_l2(out, g2[f"{name}/f64_d{digits}"]) < 1e-12
 

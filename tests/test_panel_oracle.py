@@ -78,3 +78,24 @@ def test_adaptive_weights_equal_a_dense_rule_away_from_the_panel(panel):
         W = PO.panel_weights(X, xt, kernel=1)
         D = dense_rule_weights(X, xt)
         assert np.abs(W - D).max() <= 1e-13 * np.abs(D).max(), (dist, np.abs(W - D).max() / np.abs(D).max())
+
+
+def test_oracle_matches_the_reference_legacy_quadrature():
+    """Pinned to the reference itself: the near-singular double-layer potential of the torus
+    workload from SCTL's legacy boundary quadrature (boundary_quadrature.hpp, orders 24/24,
+    tests/golden/legacy_torus_dl.npz from make_legacy_golden.py) for targets 1e-4..1 panel sizes
+    off the surface, against the full panel-by-panel sum of the oracle's weights."""
+    import json
+    import os
+
+    from sctl_gb300.torus import Torus
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    meta = json.load(open(os.path.join(here, "legacy_torus_dl.json")))
+    U = np.load(os.path.join(here, "legacy_torus_dl.npz"))["U"]
+    T = Torus(seed=meta["torus_seed"])
+    tg = T.targets(meta["n_trg"], seed=meta["target_seed"], hmin=meta["hmin"], hmax=meta["hmax"])
+    picks = [int(i) for i in np.argsort(tg["h"])[[0, 40, 90, 140, 200, 255]]]  # 1e-4 .. 1 panel sizes
+    for t in picks:
+        v = sum(PO.panel_weights(T.X[p], tg["r_trg"][t], kernel=1) @ T.sigma[p] for p in range(T.np))
+        # the legacy rule's own error is up to ~1e-8 of the potential at 0.1-0.3 panel sizes
+        assert abs(v - U[t]) <= 3e-8 * max(abs(U[t]), 1e-3), (t, tg["h"][t], v, U[t])

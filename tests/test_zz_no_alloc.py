@@ -89,3 +89,35 @@ def test_noalloc_rejects_oversize_before_launch(cuda):
     assert capi.launch_count() == n0
     assert capi.load().sctlgpu_eval_mixed_noalloc(9, 10, 1, x.data_ptr(), 1, x.data_ptr(), None, x.data_ptr(),
                                                   x.data_ptr(), 0, None) == capi.ERR_INVALID_KERNEL
+
+
+@pytest.mark.parametrize("digits", list(range(0, 16)) + [-1])
+def test_noalloc_routing_matches_existing_entry_every_digits(cuda, digits):
+    """Both entries pick the arithmetic and Newton schedule from one rule: equal results for every digits."""
+    torch = cuda
+    d = W.sphere_ball(1200, 700, 2, 60)
+    dd = _dev(torch, d)
+    ref = _existing(torch, 2, dd, digits, 700, 1200, 3)
+    got = _noalloc(torch, 2, dd, digits, 700, 1200, 3)
+    assert O.rel_l2(got, ref) < 1e-13
+
+
+def test_noalloc_just_under_the_limit(cuda):
+    """2^20 Laplace FxU sources and 2^20 targets: 32 MiB of records plus the partial sums of as many
+    source slices as fit in the rest of the 64 MiB array (fewer slices than sctlgpu_eval would use)."""
+    torch = cuda
+    n = 1 << 20
+    d = W.sphere_ball(n, n, 0, 61)
+    dd = _dev(torch, d)
+    ref = _existing(torch, 0, dd, 10, n, n, 1)
+    got = _noalloc(torch, 0, dd, 10, n, n, 1)
+    assert O.rel_l2(got, ref) < 1e-12
+    # 8 Mi targets: their partial sums alone (one slice, 64 MiB) no longer fit beside the records:
+    # refused before anything launches (the buffers are real, so nothing could read out of bounds)
+    big_nt = (64 << 20) // 8
+    xt = torch.zeros(big_nt * 3, dtype=torch.float64, device="cuda")
+    vt = torch.zeros(big_nt, dtype=torch.float64, device="cuda")
+    n0 = capi.launch_count()
+    rc = capi.load().sctlgpu_eval_mixed_noalloc(0, 10, big_nt, xt.data_ptr(), n, _ptr(dd["r_src"]), None,
+                                                _ptr(dd["v_src"]), vt.data_ptr(), 0, None)
+    assert rc == capi.ERR_TOO_LARGE and capi.launch_count() == n0
