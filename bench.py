@@ -434,7 +434,7 @@ def torus_section(torch, n_eval=1 << 20, n_train=440000, steps=4000, learned=Tru
     xt = torch.from_numpy(tg["r_trg"]).cuda().reshape(-1).contiguous()
     one = torch.ones(T.np * 100, dtype=torch.float64, device="cuda")
     sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()
-    pairs = S.near_pairs(xt, 1.0)
+    pairs = S.near_pairs(xt, 1.5)
     plan = S.smooth_subtraction_plan(n_eval, pairs)
     res["near_pairs"] = int(pairs[0].numel())
     # BuildNearList on the GPU (node radius 1.5 panel sizes), timed as a whole (it synchronises once)
@@ -480,7 +480,7 @@ def torus_section(torch, n_eval=1 << 20, n_train=440000, steps=4000, learned=Tru
     # learned path
     tt = T.targets(n_train, seed=100)
     xtr = torch.from_numpy(tt["r_trg"]).cuda().reshape(-1).contiguous()
-    pt, pp = S.near_pairs(xtr, 1.0)
+    pt, pp = S.near_pairs(xtr, 1.5)
     t0 = time.perf_counter()
     W = panel_weights(1, pt, pp, xtr, S.X)
     torch.cuda.synchronize()
@@ -508,6 +508,41 @@ def torus_section(torch, n_eval=1 << 20, n_train=440000, steps=4000, learned=Tru
     return res
 
 
+def learning_curve_section(torch, n_train=220000, steps_list=(2000, 8000, 32000, 96000), batch=1 << 14):
+    """Held-out accuracy of the correction network against training length: one network (the
+    15 -> 256 -> 256 -> 256 -> 100 GELU MLP on the tcgen05 kernels, singular part subtracted, basis
+    inputs) trained for each step count on the same labels (adaptive-quadrature weights of the near
+    pairs of n_train torus targets), with the cosine learning-rate schedule stretched to the run.
+    Reports the final training loss, the held-out max weight error per distance bin (the quantity
+    the acceptance gate is calibrated on) and its worst bin."""
+    from sctl_gb300.learned import LearnedCorrection, panel_weights
+    from sctl_gb300.nearquad import PanelSurface
+    from sctl_gb300.torus import Torus, pair_features_device
+    T = Torus(seed=0)
+    S = PanelSurface(T.X, T.N, T.Q, T.size)
+    tt = T.targets(n_train, seed=100)
+    xtr = torch.from_numpy(tt["r_trg"]).cuda().reshape(-1).contiguous()
+    pt, pp = S.near_pairs(xtr, 1.5)
+    W = panel_weights(1, pt, pp, xtr, S.X)
+    f = pair_features_device(T, xtr, pt, pp)
+    res = {"labels": int(pt.numel()), "batch": batch, "runs": []}
+    for steps in steps_list:
+        L = LearnedCorrection(n_models=1, max_batch=batch, singular=T, basis_inputs=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        loss = L.fit(f, W, steps=steps, batch=batch, lr=3e-3)
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        per_bin = (L.calib / L.CALIB_SAFETY).tolist()  # measured held-out maxima (without the safety factor)
+        res["runs"].append({"steps": steps, "train_s": secs, "final_loss": loss[0],
+                            "epochs": steps * batch / (0.9 * pt.numel()),
+                            "held_out_max_weight_err_by_bin": [float(f"{x:.3g}") for x in per_bin],
+                            "held_out_max_weight_err_worst": float(max(per_bin))})
+        for m in L.models:
+            m.close()
+    return res
+
+
 def main():
     global KERNELS, N_SRC
     ap = argparse.ArgumentParser()
@@ -522,7 +557,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="timed region only (for profiler runs)")
     ap.add_argument("--skip-torus", action="store_true", help="omit the near-singular torus section")
     ap.add_argument("--section", choices=["near", "near_panel", "clusters", "cube", "torus", "torus_plain", "mlp",
-                                          "ext", "kmat", "ref_full"],
+                                          "ext", "kmat", "ref_full", "learning_curve"],
                     help="run only this secondary workload and print its JSON (profiling of one kernel family)")
     ap.add_argument("--torus-n", type=int, default=1 << 20, help="targets of the torus section")
     args = ap.parse_args()
@@ -543,7 +578,8 @@ def main():
               "cube": lambda: cube_section(torch, stream), "mlp": lambda: mlp_section(torch, stream),
               "ext": lambda: ext_section(torch, stream), "kmat": lambda: kmat_section(torch, stream),
               "torus": lambda: torus_section(torch, n_eval=args.torus_n),
-              "torus_plain": lambda: torus_section(torch, n_eval=args.torus_n, learned=False)}[args.section]
+              "torus_plain": lambda: torus_section(torch, n_eval=args.torus_n, learned=False),
+              "learning_curve": lambda: learning_curve_section(torch)}[args.section]
         print(json.dumps({"section": args.section, **fn()}), flush=True)
         return
 
@@ -712,7 +748,7 @@ def main():
             traffic = json.load(open(tpath)).get(NAMES[dom])
         except Exception:
             traffic = None
-    roofline = {"bound": "fp32_issue", "kernel": f"direct_sum_kernel<{NAMES[dom]}, mixed double-float>",
+    roofline = {"bound": "fp32_issue", "kernel": f"direct_sum_pk_kernel<{NAMES[dom]}> (mixed, double-float on packed FP32)",
                 "achieved": achieved / 1e9, "peak": peak_int / 1e9, "unit": "Ginteractions/s",
                 "frac": achieved / peak_int, "traffic": traffic,
                 "peak_basis": f"{SMS} SMs x {sm_max:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json) x "

@@ -225,6 +225,14 @@ int sctlgpu_panel_near_weights(int kernel, int64_t n_pairs, const int64_t* pair_
                                double alpha, int max_depth, double* w_out, void* stream);
 
 /*
+ * Far-field densities (replaces the density weighting of
+ * BoundaryIntegralOp::ComputeFarField, boundary_integral.txx:1266-1285):
+ * f_far[i*dof + k] = f[i*dof + k] * w[i] for i < n, k < dof.  Device pointers,
+ * asynchronous on `stream`; f_far may alias f.
+ */
+int sctlgpu_far_densities(int64_t n, int dof, const double* f, const double* w, double* f_far, void* stream);
+
+/*
  * Near lists (replaces BuildNearList, boundary_integral.txx:50-522, single rank).
  * Target t is near element e when some node s of e (nodes elem_nds_dsp[e] ..
  * elem_nds_dsp[e] + elem_nds_cnt[e] - 1 of r_src) has |x_t - x_s|^2 < src_radius[s]^2,
@@ -252,6 +260,11 @@ int sctlgpu_near_list_sizes(sctlgpu_near_list list, int64_t* n_near, int64_t* nt
 int sctlgpu_near_list_get(sctlgpu_near_list list, int64_t* near_elem_cnt, int64_t* near_elem_dsp,
                           int64_t* near_trg_idx, int64_t* near_scatter_index, int64_t* near_trg_cnt,
                           int64_t* near_trg_dsp, int64_t* near_trg_elem, void* stream);
+/* The element of every element-major entry (near_elem_idx[n_near]; the reference
+ * expands near_elem_cnt the same way when it walks the element-major list,
+ * boundary_integral.txx:1009-1032): with near_trg_idx, the (element, target)
+ * pairs sorted by element.  Host or device destination; synchronous. */
+int sctlgpu_near_list_elem_index(sctlgpu_near_list list, int64_t* near_elem_idx, void* stream);
 int sctlgpu_near_list_destroy(sctlgpu_near_list list);
 
 /*

@@ -16,13 +16,16 @@ with alpha = 2 and q = 14 (the nearest singularity of a box's integrand lies
 >= 5.6 half-sides away, so each box is exact to rounding), against alpha = 1
 and 8 points on the GPU.
 
-Parity unpinned against the reference: the reference has no runnable
-implementation of this path (the QuadElemList NearInterac stubs assert,
-quad_element.cpp:278-286) and no test or fixture for it.  The restatement is
-pinned by closed forms instead (tests/test_panel_oracle.py): on a flat square
-panel sum_ab W_ab is, for any target, the solid angle of the square over
-4 pi (double layer) or the square's 1/r potential over 4 pi (single layer),
-and far from a panel every node's weight equals one dense Gauss rule.
+Pinned to the reference: the reference's current element list cannot run
+this path (the QuadElemList NearInterac stubs assert, quad_element.cpp:278-286),
+but its legacy boundary quadrature (boundary_quadrature.hpp, built by
+oracle/legacy_quad.cpp with three interface gaps bridged) computes the same
+integrals; tests/golden/legacy_torus_dl.npz holds its near-singular potentials
+on the torus workload and tests/test_panel_oracle.py checks this restatement
+against them (<= 1e-10 + 1e-9 |U|).  Closed forms pin it further: on a flat
+square panel sum_ab W_ab is, for any target, the solid angle of the square
+over 4 pi (double layer) or the square's 1/r potential over 4 pi (single
+layer), and far from a panel every node's weight equals one dense Gauss rule.
 """
 from __future__ import annotations
 

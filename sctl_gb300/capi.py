@@ -67,7 +67,9 @@ SIGNATURES = {
     "sctlgpu_near_list_build": (_i, [ctypes.POINTER(_vp), _i64, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _u, _vp]),
     "sctlgpu_near_list_sizes": (_i, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "sctlgpu_near_list_get": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "sctlgpu_near_list_elem_index": (_i, [_vp, _vp, _vp]),
     "sctlgpu_near_list_destroy": (_i, [_vp]),
+    "sctlgpu_far_densities": (_i, [_i64, _i, _vp, _vp, _vp, _vp]),
     "sctlgpu_near_matrix_apply": (_i, [_i, _i, _i64, _vp, _i64, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp,
                                       _vp, _vp]),
     "sctlgpu_near_matrix_apply_pairs": (_i, [_i, _i, _i64, _vp, _i64, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp,

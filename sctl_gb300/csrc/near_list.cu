@@ -402,6 +402,21 @@ __global__ void widen_kernel(int64_t n, const int32_t* in, int64_t* out) {
     out[i] = in[i];
 }
 
+// Element of every element-major entry: the last element whose offset is <= the
+// entry's position (an element without entries shares its offset with the next
+// element, so the last such element is the one that owns the entry).
+__global__ void elem_index_kernel(int64_t n_near, int64_t n_elem, const int64_t* __restrict__ dsp,
+                                  int64_t* __restrict__ out) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n_near; j += (int64_t)gridDim.x * blockDim.x) {
+    int64_t lo = 0, hi = n_elem - 1;  // dsp[lo] <= j always holds (dsp[0] == 0)
+    while (lo < hi) {
+      const int64_t mid = (lo + hi + 1) >> 1;
+      if (dsp[mid] <= j) lo = mid; else hi = mid - 1;
+    }
+    out[j] = lo;
+  }
+}
+
 __global__ void trg_dsp_fix_kernel(int64_t nt, const int64_t* tcnt, int64_t* tdsp) {
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x)
     if (tcnt[t] == 0) tdsp[t] = 0;
@@ -698,6 +713,36 @@ extern "C" int sctlgpu_near_list_get(sctlgpu_near_list L, int64_t* near_elem_cnt
   cp(near_trg_cnt, L->trg_cnt, L->nt);
   cp(near_trg_dsp, L->trg_dsp, L->nt);
   cp(near_trg_elem, L->trg_elem, L->n_near);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return runtime_record(e);
+}
+
+extern "C" int sctlgpu_near_list_elem_index(sctlgpu_near_list L, int64_t* near_elem_idx, void* stream) {
+  if (!L) return SCTLGPU_ERR_NULL_POINTER;
+  if (L->n_near == 0) return SCTLGPU_OK;
+  if (!near_elem_idx) return SCTLGPU_ERR_NULL_POINTER;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != L->device) return SCTLGPU_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, L->device);
+  cudaPointerAttributes pa{};
+  cudaError_t e = cudaPointerGetAttributes(&pa, near_elem_idx);
+  const bool on_device = e == cudaSuccess && (pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged);
+  (void)cudaGetLastError();  // a plain host pointer is not an error here
+  int64_t* dst = near_elem_idx;
+  if (!on_device) {
+    e = cudaMallocAsync((void**)&dst, L->n_near * 8, st);
+    if (e != cudaSuccess) return runtime_record(e);
+  }
+  elem_index_kernel<<<grid_for(L->n_near, sms > 0 ? sms : 1), NL_T, 0, st>>>(L->n_near, L->n_elem, L->elem_dsp, dst);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  e = cudaGetLastError();
+  if (!on_device) {
+    if (e == cudaSuccess) e = cudaMemcpyAsync(near_elem_idx, dst, L->n_near * 8, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(dst, st);
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   return runtime_record(e);
 }

@@ -307,7 +307,7 @@ class LearnedCorrection:
 
 
 def learned_near_field(S, T, L: LearnedCorrection, r_trg: torch.Tensor, sigma: torch.Tensor, tol: float,
-                       kernel=1, mode="mixed", digits=10, near_factor=1.0, alpha=1.0, pairs=None, plan=None,
+                       kernel=1, mode="mixed", digits=10, near_factor=1.5, alpha=1.0, pairs=None, plan=None,
                        stats=None, h_cut=0.1):
     """Potential with learned near corrections where the pair is near-singular (the target's foot point
     inside the panel and its distance below h_cut panel sizes -- elsewhere the smooth rule is already
@@ -323,8 +323,7 @@ def learned_near_field(S, T, L: LearnedCorrection, r_trg: torch.Tensor, sigma: t
         pairs = S.near_pairs(xt, near_factor)
     if plan is None:
         plan = S.smooth_subtraction_plan(nt, pairs, kernel, mode, digits)
-    negq = (-S.Q).reshape(-1).contiguous()
-    plan.execute(xt, S.X.reshape(-1), S.N.reshape(-1), sigma.reshape(-1).contiguous(), out, w_src=negq,
+    plan.execute(xt, S.X.reshape(-1), S.N.reshape(-1), sigma.reshape(-1).contiguous(), out, w_src=S.negQ,
                  accumulate=True)
     pt, pp = pairs
     f = pair_features_device(T, xt, pt, pp)

@@ -5,13 +5,15 @@ near-singular panel corrections -- BoundaryIntegralOp::ComputePotential
 * far field: every node is a source with weight Q (ComputeFarField,
   :1248-1309: F_far = F * wts, then the direct sum), evaluated by
   `sctlgpu_eval`;
-* near field: for every (target, panel) pair closer than `near_factor` panel
-  sizes, the panel's accurate contribution minus its smooth-rule part
+* near field: for every (target, panel) pair from the GPU near list (target
+  within `near_factor` panel sizes of one of the panel's nodes, BuildNearList's
+  test, :50-522), the panel's accurate contribution minus its smooth-rule part
   (SetupNear / ComputeNearInterac, :927-1381), evaluated by
-  `sctlgpu_panel_near_correction` (adaptive refinement, FP64) or by
-  upsampled sub-panel sources through a batched near plan.
+  `sctlgpu_panel_near_correction` (adaptive refinement) or applied from stored
+  near matrices.
 
-All arrays are torch tensors on the GPU; the work runs in libsctlgpu.
+All arrays are torch tensors on the GPU used as plain device buffers; every
+kernel of an evaluation is one of libsctlgpu's.
 """
 from __future__ import annotations
 
@@ -24,57 +26,70 @@ from . import capi
 class PanelSurface:
     def __init__(self, X, N, Q, size, device="cuda"):
         """X, N: (np, p*p, 3) node coordinates and unit normals; Q: (np, p*p) smooth weights;
-        size: (np,) panel sizes (near-field radius unit)."""
+        size: (np,) panel sizes (near-field radius unit).  Host arrays; everything derived from
+        them is computed on the host and uploaded once."""
+        X, N, Q, size = (np.ascontiguousarray(a, np.float64) for a in (X, N, Q, size))
         t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=device)  # noqa: E731
         self.X, self.N, self.Q, self.size = t(X), t(N), t(Q), t(size)
-        self.np, self.nn = self.X.shape[0], self.X.shape[1]
-        self.center = self.X.mean(1)
-        self.radius = (self.X - self.center[:, None]).norm(dim=2).max(1).values
+        self.np, self.nn = X.shape[0], X.shape[1]
+        self.negQ = t(-Q.reshape(-1))  # smooth-rule weights of the subtraction plan
+        # near list inputs (BuildNearList): every node of panel P carries the radius near_factor * size_P
+        self._elem_cnt = torch.as_tensor(np.full(self.np, self.nn, np.int64), device=device)
+        self._elem_dsp = torch.as_tensor(np.arange(self.np, dtype=np.int64) * self.nn, device=device)
+        self._node_size = np.repeat(size, self.nn)
+        self._node_rad = {}
 
     # ------------------------------------------------------------ near list
-    def near_pairs(self, r_trg, near_factor=1.0, chunk=1 << 15):
-        """(target, panel) pairs with |x_t - c_P| < radius_P + near_factor * size_P (a brute-force
-        GPU form of BuildNearList, boundary_integral.txx:50-522).  Sorted by panel."""
-        xt = r_trg.reshape(-1, 3)
-        lim = self.radius + near_factor * self.size
-        tt, pp = [], []
-        for a in range(0, xt.shape[0], chunk):
-            d = torch.cdist(xt[a:a + chunk], self.center)
-            i, j = torch.nonzero(d < lim[None], as_tuple=True)
-            tt.append(i + a)
-            pp.append(j)
-        t = torch.cat(tt).to(torch.int64)
-        p = torch.cat(pp).to(torch.int64)
-        order = torch.argsort(p * xt.shape[0] + t)
-        return t[order].contiguous(), p[order].contiguous()
+    def near_pairs(self, r_trg, near_factor=1.5):
+        """(target, panel) pairs from the GPU near list (`NearList`, BuildNearList's test,
+        boundary_integral.txx:50-522): a target is near a panel when it lies within
+        near_factor * size_P of one of the panel's nodes (1.5 keeps the 10 x 10 smooth rule's error
+        below 1e-8 for every other target; at 1.0 it reaches 1.5e-8 above a panel's centre).
+        Sorted by panel, then target; both arrays int64 on the device."""
+        import ctypes
 
-    def near_pairs_grid(self, r_trg, near_factor=1.0):
-        """(target, panel) pairs from the GPU near list (`NearList`, BuildNearList's test): a
-        target is near a panel when it is within near_factor * size_P of one of the panel's
-        nodes.  Sorted by panel, then target."""
         from .nearlist import NearList
         xt = r_trg.reshape(-1).contiguous()
-        cnt = torch.full((self.np,), self.nn, dtype=torch.int64, device=xt.device)
-        dsp = torch.arange(self.np, dtype=torch.int64, device=xt.device) * self.nn
-        rad = (near_factor * self.size).repeat_interleave(self.nn).contiguous()
-        a = NearList(xt, cnt, dsp, self.X.reshape(-1).contiguous(), rad).arrays()
-        p = torch.repeat_interleave(torch.arange(self.np, device=xt.device), a["near_elem_cnt"])
-        return a["near_trg_idx"].contiguous(), p.to(torch.int64).contiguous()
+        rad = self._node_rad.get(near_factor)
+        if rad is None:
+            rad = self._node_rad[near_factor] = torch.as_tensor(near_factor * self._node_size, device=xt.device)
+        L = NearList(xt, self._elem_cnt, self._elem_dsp, self.X.reshape(-1), rad)
+        n = L.n_near
+        t = torch.empty(max(n, 1), dtype=torch.int64, device=xt.device)
+        p = torch.empty(max(n, 1), dtype=torch.int64, device=xt.device)
+        lib = capi.load()
+        stream = torch.cuda.current_stream().cuda_stream
+        capi.check(lib.sctlgpu_near_list_get(L._h, None, None, t.data_ptr(), None, None, None, None, stream),
+                   "sctlgpu_near_list_get")
+        capi.check(lib.sctlgpu_near_list_elem_index(L._h, ctypes.c_void_p(p.data_ptr()), stream),
+                   "sctlgpu_near_list_elem_index")
+        L.close()
+        return t[:n], p[:n]
+
+    # the name of the GPU near-list search before the brute-force form was retired
+    near_pairs_grid = near_pairs
 
     # ------------------------------------------------------------ far field
     def far_field(self, r_trg, sigma, kernel=1, mode="mixed", digits=10, out=None):
+        """ComputeFarField (boundary_integral.txx:1248-1309): F_far = sigma * Q on the device
+        (`sctlgpu_far_densities`), then one direct sum over every node; added into `out` when it
+        is given, else written to a new array."""
         xt = r_trg.reshape(-1)
         nt = xt.numel() // 3
         src = self.X.reshape(-1)
         nrm = self.N.reshape(-1)
-        f = (sigma.reshape(-1) * self.Q.reshape(-1)).contiguous()
-        if out is None:
-            out = torch.zeros(nt, dtype=torch.float64, device=xt.device)
-        flags = capi.DEVICE_PTRS | (capi.ACCUMULATE if out is not None else 0)
+        lib = capi.load()
         stream = torch.cuda.current_stream().cuda_stream
-        capi.check(capi.load().sctlgpu_eval(kernel, capi.MODE_IDS[mode], digits, nt, xt.data_ptr(), src.numel() // 3,
-                                            src.data_ptr(), nrm.data_ptr() if kernel in (1, 3) else None,
-                                            f.data_ptr(), out.data_ptr(), flags, stream), "far field")
+        sig = sigma.reshape(-1).contiguous()
+        f = torch.empty_like(sig)
+        capi.check(lib.sctlgpu_far_densities(self.np * self.nn, sig.numel() // (self.np * self.nn), sig.data_ptr(),
+                                             self.Q.data_ptr(), f.data_ptr(), stream), "far densities")
+        flags = capi.DEVICE_PTRS | (capi.ACCUMULATE if out is not None else 0)
+        if out is None:
+            out = torch.empty(nt, dtype=torch.float64, device=xt.device)
+        capi.check(lib.sctlgpu_eval(kernel, capi.MODE_IDS[mode], digits, nt, xt.data_ptr(), src.numel() // 3,
+                                    src.data_ptr(), nrm.data_ptr() if kernel in (1, 3) else None,
+                                    f.data_ptr(), out.data_ptr(), flags, stream), "far field")
         return out
 
     # ------------------------------------------------------------ near field
@@ -111,7 +126,7 @@ class PanelSurface:
         iterative solver): the accurate weights of every (target, panel) pair, see NearMatrix."""
         return NearMatrix(self, r_trg, pairs, kernel, alpha, max_depth, float_pairs)
 
-    def evaluate(self, r_trg, sigma, kernel=1, mode="mixed", digits=10, near_factor=1.0, alpha=1.0, pairs=None,
+    def evaluate(self, r_trg, sigma, kernel=1, mode="mixed", digits=10, near_factor=1.5, alpha=1.0, pairs=None,
                  plan=None, matrix=None):
         """Far field (smooth rule over every node) + near corrections.  The smooth part of the near
         panels is subtracted with a near plan in the far field's arithmetic, so the large
@@ -124,9 +139,8 @@ class PanelSurface:
             pairs = self.near_pairs(xt, near_factor)
         if plan is None:
             plan = self.smooth_subtraction_plan(xt.numel() // 3, pairs, kernel, mode, digits)
-        negq = (-self.Q).reshape(-1).contiguous()
-        plan.execute(xt, self.X.reshape(-1), self.N.reshape(-1), sigma.reshape(-1).contiguous(), out, w_src=negq,
-                     accumulate=True)
+        plan.execute(xt, self.X.reshape(-1), self.N.reshape(-1), sigma.reshape(-1).contiguous(), out,
+                     w_src=self.negQ, accumulate=True)
         if matrix is not None:
             matrix.apply(sigma, out)
         else:

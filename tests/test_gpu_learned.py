@@ -19,7 +19,7 @@ def trained(cuda):
     S = PanelSurface(T.X, T.N, T.Q, T.size)
     tg = T.targets(24000, seed=100)
     xt = torch.from_numpy(tg["r_trg"]).cuda().reshape(-1).contiguous()
-    pt, pp = S.near_pairs(xt, 1.0)
+    pt, pp = S.near_pairs(xt, 1.5)
     W = panel_weights(1, pt, pp, xt, S.X)
     f = pair_features_device(T, xt, pt, pp)
     L = LearnedCorrection(max_batch=8192, singular=T)

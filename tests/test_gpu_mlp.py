@@ -132,7 +132,7 @@ def test_weights_mode_equals_potential_mode(cuda):
     S = PanelSurface(T.X, T.N, T.Q, T.size)
     tg = T.targets(300, seed=21)
     xt = torch.from_numpy(tg["r_trg"]).cuda().reshape(-1).contiguous()
-    pt, pp = S.near_pairs(xt, 1.0)
+    pt, pp = S.near_pairs(xt, 1.5)
     sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()
     W = panel_weights(1, pt, pp, xt, S.X)
     pot = (W * sig.reshape(T.np, 100)[pp]).sum(1)

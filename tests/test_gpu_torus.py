@@ -87,7 +87,7 @@ def test_near_matrix_path_equals_adaptive_path(setup, float_pairs):
     torch, T, S = setup
     tg = T.targets(3000, seed=16, hmin=1e-4, hmax=1.0)
     xt = torch.from_numpy(tg["r_trg"]).cuda().reshape(-1).contiguous()
-    pairs = S.near_pairs(xt, 1.0)
+    pairs = S.near_pairs(xt, 1.5)
     plan = S.smooth_subtraction_plan(3000, pairs)
     M = S.near_matrix(xt, pairs, float_pairs=float_pairs)
     sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()
@@ -166,7 +166,7 @@ def test_double_float_panel_quadrature_matches_fp64(setup, kernel):
     lib = capi.load()
     tg = T.targets(1500, seed=18, hmin=1e-4, hmax=1.0)
     xt = torch.from_numpy(tg["r_trg"]).cuda().reshape(-1).contiguous()
-    pairs = S.near_pairs(xt, 1.0)
+    pairs = S.near_pairs(xt, 1.5)
     sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()
     res = {}
     for mode in (capi.F64, capi.MIXED):
@@ -261,8 +261,8 @@ def test_refinement_overflow_is_flagged_not_dropped(setup, oracle_pairs):
 def test_matches_the_reference_legacy_quadrature(setup):
     """The GPU near-singular evaluation (far field + smooth-rule subtraction + adaptive panel
     corrections) against SCTL's own legacy boundary quadrature on the same torus, density and
-    targets (tests/golden/legacy_torus_dl.npz; orders 24/24, whose own error against the exact
-    integral is ~1e-9 rel-l2 and up to ~1e-8 of the potential at 0.1-0.3 panel sizes)."""
+    targets (tests/golden/legacy_torus_dl.npz; orders 32/48, whose own error against the exact
+    integral is below 5e-11 on the sampled targets), in both panel arithmetics."""
     import json
     import os
     torch, T, S = setup
@@ -281,7 +281,8 @@ def test_matches_the_reference_legacy_quadrature(setup):
             v = S.evaluate(xt, sig, kernel=1, mode="mixed", digits=10).cpu().numpy()
         finally:
             lib.sctlgpu_panel_arithmetic(prev)
-        rel = np.abs(v - U) / np.maximum(np.abs(U), 1e-3)
+        err = np.abs(v - U)
         l2 = np.linalg.norm(v - U) / np.linalg.norm(U)
-        print(f"{arith}: rel-l2 {l2:.3e}, max {rel.max():.3e} at h = {tg['h'][rel.argmax()]:.2e}")
-        assert l2 < 5e-9 and rel.max() < 3e-8, (arith, l2, rel.max())
+        print(f"{arith}: rel-l2 {l2:.3e}, max abs {err.max():.3e} at h = {tg['h'][err.argmax()]:.2e}")
+        # the potentials are O(1): 1e-9 absolute
+        assert l2 < 5e-10 and err.max() < 1e-9, (arith, l2, err.max())
