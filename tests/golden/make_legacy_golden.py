@@ -16,6 +16,14 @@ log-uniform in [1e-4, 1] panel sizes, either side).  Quadrature orders
 legacy's direct part is short of points at 0.1-0.3 panel sizes and errs by up
 to 2.6e-6, with (24, 40) by 3e-10.  Only the potentials are stored; inputs are
 regenerated.
+
+The legacy rule integrates a panel adjacent to a near-edge target with its
+plain direct rule once the target is outside its near-singular radius; there
+48 points per direction are not enough (2.3e-5 at a target 0.063 panel sizes
+off the surface and 0.033 of a panel from an edge; 4.8e-7 with 64).  The
+golden therefore also holds the values with order_direct = 64: where the two
+agree to 1e-11 the legacy value is exact to its rounding, elsewhere their
+difference is its error estimate.
 """
 from __future__ import annotations
 
@@ -56,12 +64,16 @@ def main():
     T = Torus(seed=0)
     tg = T.targets(N_TRG, seed=SEED, hmin=1e-4, hmax=1.0)
     U, _ = legacy_potential(T, tg["r_trg"])
+    # the same with a denser rule for the parts it integrates directly: where the two agree the
+    # legacy value is trusted to its rounding; where not, their difference bounds its own error
+    U64, _ = legacy_potential(T, tg["r_trg"], orders=(ORDERS[0], 64))
     # the legacy test's Green's identity at cheaper orders (at the golden's orders it runs for hours)
     _, green = legacy_potential(T, tg["r_trg"][:1], orders=(16, 16), green=True)
-    np.savez_compressed(os.path.join(HERE, "legacy_torus_dl.npz"), U=U)
+    np.savez_compressed(os.path.join(HERE, "legacy_torus_dl.npz"), U=U, U_direct64=U64)
     meta = {"generator": "tests/golden/make_legacy_golden.py", "torus_seed": 0, "n_trg": N_TRG, "target_seed": SEED,
             "hmin": 1e-4, "hmax": 1.0, "orders": list(ORDERS),
-            "legacy_greens_identity_max_err_orders_16_16": green}
+            "legacy_greens_identity_max_err_orders_16_16": green,
+            "targets_where_orders_48_and_64_agree_to_1e-11": int((abs(U - U64) <= 1e-11).sum())}
     with open(os.path.join(HERE, "legacy_torus_dl.json"), "w") as fh:
         json.dump(meta, fh, indent=1, sort_keys=True)
     print(json.dumps(meta))

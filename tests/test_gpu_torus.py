@@ -261,15 +261,21 @@ def test_refinement_overflow_is_flagged_not_dropped(setup, oracle_pairs):
 def test_matches_the_reference_legacy_quadrature(setup):
     """The GPU near-singular evaluation (far field + smooth-rule subtraction + adaptive panel
     corrections) against SCTL's own legacy boundary quadrature on the same torus, density and
-    targets (tests/golden/legacy_torus_dl.npz; orders 32/48, whose own error against the exact
-    integral is below 5e-11 on the sampled targets), in both panel arithmetics."""
+    targets (tests/golden/legacy_torus_dl.npz, orders 32/48), in both panel arithmetics.  The
+    golden also holds the legacy values with a 64-point direct rule: where the two agree to 1e-11
+    the legacy value is exact to its rounding and the GPU must match it to 1e-9; elsewhere (targets
+    next to a panel edge, whose neighbour the legacy rule integrates with its plain direct rule)
+    the two values' difference bounds the legacy's own error, and the GPU must lie within it."""
     import json
     import os
     torch, T, S = setup
     here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
     meta = json.load(open(os.path.join(here, "legacy_torus_dl.json")))
-    U = np.load(os.path.join(here, "legacy_torus_dl.npz"))["U"]
-    assert meta["torus_seed"] == 0
+    g = np.load(os.path.join(here, "legacy_torus_dl.npz"))
+    U, U64 = g["U"], g["U_direct64"]
+    est = np.abs(U - U64)
+    trusted = est <= 1e-11
+    assert meta["torus_seed"] == 0 and trusted.sum() >= 180  # 193 of 256 in the golden
     tg = T.targets(meta["n_trg"], seed=meta["target_seed"], hmin=meta["hmin"], hmax=meta["hmax"])
     xt = torch.from_numpy(tg["r_trg"]).cuda()
     sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()
@@ -282,7 +288,9 @@ def test_matches_the_reference_legacy_quadrature(setup):
         finally:
             lib.sctlgpu_panel_arithmetic(prev)
         err = np.abs(v - U)
-        l2 = np.linalg.norm(v - U) / np.linalg.norm(U)
-        print(f"{arith}: rel-l2 {l2:.3e}, max abs {err.max():.3e} at h = {tg['h'][err.argmax()]:.2e}")
+        print(f"{arith}: {int(trusted.sum())} trusted targets, max abs {err[trusted].max():.3e}; others: "
+              f"max abs {err[~trusted].max() if (~trusted).any() else 0:.3e} (legacy error estimate up to "
+              f"{est.max():.3e})")
         # the potentials are O(1): 1e-9 absolute
-        assert l2 < 5e-10 and err.max() < 1e-9, (arith, l2, err.max())
+        assert err[trusted].max() < 1e-9, (arith, err[trusted].max())
+        assert np.all(err <= est + 1e-9), (arith, np.max(err - est))
