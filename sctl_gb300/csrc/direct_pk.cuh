@@ -115,46 +115,54 @@ template <> struct RecPk<KER_SDXU> {
   v2 xh, yh, zh, xl, yl, zl, fh0, fh1, fh2, fl0, fl1, fl2, nh0, nh1, nh2, nl0, nl1, nl2;
 };
 
-// One pair record per thread; an odd last source is paired with a copy of
-// itself whose densities are zero (it adds exactly 0).
+// The pair record of sources sa (lane x) and sa + 1 (lane y); without a real
+// second source (real_b false) lane y is a copy of sa with zero densities (it
+// adds exactly 0).
+template <int KER>
+__device__ __forceinline__ RecPk<KER> pair_record(const MixedFrame& fr, int64_t sa, bool real_b,
+                                                  const double* __restrict__ xs, const double* __restrict__ nrm,
+                                                  const double* __restrict__ f, const double* __restrict__ w) {
+  float v[2][18];
+#pragma unroll
+  for (int lane = 0; lane < 2; ++lane) {
+    const bool real = lane == 0 || real_b;
+    const int64_t s = real ? sa + lane : sa;
+    const double ws = real ? (w ? w[s] : 1.0) : 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) split_coord(fr, k, xs[s * 3 + k], v[lane][k], v[lane][3 + k]);
+    if constexpr (KER == KER_LFXU) {
+      split_val(f[s] * ws, v[lane][6], v[lane][7]);
+    } else if constexpr (KER == KER_LDXU) {
+      const double fs = f[s] * ws;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) split_val(fs * nrm[s * 3 + k], v[lane][6 + k], v[lane][9 + k]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) split_val(f[s * 3 + k] * ws, v[lane][6 + k], v[lane][9 + k]);
+      if constexpr (KER == KER_SDXU) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) split_val(nrm[s * 3 + k], v[lane][12 + k], v[lane][15 + k]);
+      }
+    }
+  }
+  constexpr int NF = sizeof(RecPk<KER>) / sizeof(v2);
+  RecPk<KER> r;
+  v2* rv = reinterpret_cast<v2*>(&r);
+#pragma unroll
+  for (int q = 0; q < NF; ++q) rv[q] = make_float2(v[0][q], v[1][q]);
+  return r;
+}
+
+// One pair record per thread: sources 2j and 2j + 1 of the list (`w`, when
+// given, weights every density, as in pack_sources_kernel).
 template <int KER>
 __global__ void pack_pairs_kernel(int64_t ns, const double* __restrict__ xs, const double* __restrict__ nrm,
                                   const double* __restrict__ f, RecPk<KER>* __restrict__ out, const BBox* bb,
                                   const double* __restrict__ w = nullptr) {
   const MixedFrame fr = frame_from_bbox(bb);
   const int64_t npairs = (ns + 1) / 2;
-  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < npairs; j += (int64_t)gridDim.x * blockDim.x) {
-    float v[2][18];
-#pragma unroll
-    for (int lane = 0; lane < 2; ++lane) {
-      const int64_t s0 = 2 * j + lane;
-      const bool real = s0 < ns;
-      const int64_t s = real ? s0 : ns - 1;
-      const double ws = real ? (w ? w[s] : 1.0) : 0.0;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) split_coord(fr, k, xs[s * 3 + k], v[lane][k], v[lane][3 + k]);
-      if constexpr (KER == KER_LFXU) {
-        split_val(f[s] * ws, v[lane][6], v[lane][7]);
-      } else if constexpr (KER == KER_LDXU) {
-        const double fs = f[s] * ws;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) split_val(fs * nrm[s * 3 + k], v[lane][6 + k], v[lane][9 + k]);
-      } else {
-#pragma unroll
-        for (int k = 0; k < 3; ++k) split_val(f[s * 3 + k] * ws, v[lane][6 + k], v[lane][9 + k]);
-        if constexpr (KER == KER_SDXU) {
-#pragma unroll
-          for (int k = 0; k < 3; ++k) split_val(nrm[s * 3 + k], v[lane][12 + k], v[lane][15 + k]);
-        }
-      }
-    }
-    constexpr int NF = sizeof(RecPk<KER>) / sizeof(v2);
-    RecPk<KER> r;
-    v2* rv = reinterpret_cast<v2*>(&r);
-#pragma unroll
-    for (int q = 0; q < NF; ++q) rv[q] = make_float2(v[0][q], v[1][q]);
-    out[j] = r;
-  }
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < npairs; j += (int64_t)gridDim.x * blockDim.x)
+    out[j] = pair_record<KER>(fr, 2 * j, 2 * j + 1 < ns, xs, nrm, f, w);
 }
 
 // ------------------------------------------------------------ pair kernel
@@ -191,6 +199,7 @@ struct PairPk {
     }
   }
   __device__ static double result(const Trg& t, int k) { return t.tot[k]; }
+  __device__ static void add_partial(Trg& t, int k, double v) { t.tot[k] += v; }
 
   __device__ __forceinline__ static void apply(Trg& t, const RecPk<KER>& s) {
     // r = x_t - y_s = D + d: exact hi and lo differences (common grids), Fast2Sum.

@@ -75,6 +75,7 @@ cudaError_t compute_bbox(cudaStream_t s, int64_t nt, const double* r_trg, int64_
 namespace sctlgpu {
 
 struct NearParams;
+struct NearBlock;
 
 // Per (kernel, arithmetic, Newton) entry points of the batched near-field path.
 struct NearOps {
@@ -82,8 +83,15 @@ struct NearOps {
   int T = 1;             // targets per thread
   int occ = 1;           // resident CTAs per SM
   size_t smem = 0;       // dynamic shared memory of the persistent kernel
+  // Records of two sources each (the packed double-float arithmetic): `pack` pairs the whole
+  // list (source 2j with 2j + 1), `pack_blocks` pairs every block's sources separately, and the
+  // kernel's block table counts pair records.
+  bool paired = false;
   cudaError_t (*pack)(cudaStream_t, int64_t ns, const void* xs, const void* nrm, const void* f, const void* w,
                       void* recs, const BBox* bb, int sms) = nullptr;
+  cudaError_t (*pack_blocks)(cudaStream_t, int64_t nblk, const NearBlock* pair_blocks, const NearBlock* src_blocks,
+                             int64_t n_pairs, const void* xs, const void* nrm, const void* f, const void* w,
+                             void* recs, const BBox* bb, int sms) = nullptr;
   cudaError_t (*launch)(cudaStream_t, unsigned ctas, const NearParams& p) = nullptr;
 };
 

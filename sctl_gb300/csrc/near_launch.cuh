@@ -3,6 +3,7 @@
 
 #include "launch_direct.cuh"
 #include "near.cuh"
+#include "near_pk.cuh"
 
 namespace sctlgpu {
 
@@ -41,6 +42,63 @@ NearOps make_near_ops() {
     return cudaGetLastError();
   };
   return o;
+}
+
+// The packed double-float variant (mixed, 8..11 digits).
+template <int KER>
+NearOps make_near_ops_pk() {
+  using RecT = RecPk<KER>;
+  using Cfg = NearCfgPk<KER>;
+  NearOps o;
+  o.rec_bytes = sizeof(RecT);
+  o.T = Cfg::T;
+  o.paired = true;
+  o.smem = 2 * Cfg::S * sizeof(RecT) + (size_t)NEAR_THREADS * Cfg::T * KDims<KER>::K1 * sizeof(double) +
+           2 * sizeof(uint64_t);
+  static int occ = [&] {
+    int v = 0;
+    if (o.smem > 48 * 1024)
+      cudaFuncSetAttribute(near_batch_pk_kernel<KER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)o.smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, near_batch_pk_kernel<KER>, NEAR_THREADS, o.smem);
+    return v > 0 ? v : 1;
+  }();
+  o.occ = occ;
+  o.pack = [](cudaStream_t st, int64_t ns, const void* xs, const void* nrm, const void* f, const void* w, void* recs,
+              const BBox* bb, int sms) -> cudaError_t {
+    if (ns <= 0) return cudaSuccess;
+    const int64_t np = (ns + 1) / 2;
+    pack_pairs_kernel<KER><<<grid_for(np, 256, sms), 256, 0, st>>>(ns, (const double*)xs, (const double*)nrm,
+                                                                  (const double*)f, (RecT*)recs, bb, (const double*)w);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+  };
+  o.pack_blocks = [](cudaStream_t st, int64_t nblk, const NearBlock* pblk, const NearBlock* sblk, int64_t n_pairs,
+                     const void* xs, const void* nrm, const void* f, const void* w, void* recs, const BBox* bb,
+                     int sms) -> cudaError_t {
+    if (n_pairs <= 0 || nblk <= 0) return cudaSuccess;
+    pack_block_pairs_kernel<KER><<<grid_for(n_pairs, 256, sms), 256, 0, st>>>(
+        nblk, pblk, sblk, n_pairs, (const double*)xs, (const double*)nrm, (const double*)f, (const double*)w,
+        (RecT*)recs, bb);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+  };
+  o.launch = [](cudaStream_t st, unsigned ctas, const NearParams& p) -> cudaError_t {
+    const size_t smem = 2 * Cfg::S * sizeof(RecT) + (size_t)NEAR_THREADS * Cfg::T * KDims<KER>::K1 * sizeof(double) +
+                        2 * sizeof(uint64_t);
+    near_batch_pk_kernel<KER><<<ctas, NEAR_THREADS, smem, st>>>(p);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+  };
+  return o;
+}
+
+inline NearOps near_ops_pk(int kernel) {
+  switch (kernel) {
+    case KER_LFXU: return make_near_ops_pk<KER_LFXU>();
+    case KER_LDXU: return make_near_ops_pk<KER_LDXU>();
+    case KER_SFXU: return make_near_ops_pk<KER_SFXU>();
+    default: return make_near_ops_pk<KER_SDXU>();
+  }
 }
 
 template <int MODE, int NEWTON>

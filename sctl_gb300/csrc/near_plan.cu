@@ -23,7 +23,9 @@ struct sctlgpu_near_plan_s {
   bool has_map = false;
   int device = 0, sms = 1;
   NearItem* d_items = nullptr;
-  NearBlock* d_blocks = nullptr;
+  NearBlock* d_blocks = nullptr;      // the kernel's table (pair records when ops.paired)
+  NearBlock* d_src_blocks = nullptr;  // paired plans: every block's source range, for the per-block pack
+  int64_t n_pairs = 0;                // paired plans: pair records of all blocks
   int64_t* d_map = nullptr;
   int64_t* d_tidx = nullptr;
   int64_t n_index = 0;
@@ -204,9 +206,13 @@ int autotune(int kernel, int imode, int newton, const NearOps& ops, int sms, int
         static const int64_t rep_nt[5] = {16, 36, 72, 144, 384};
         const int64_t cnt_t = rep_nt[c / 2], cnt_s = (c % 2) ? 2048 : 256;
         const int64_t nb = std::max<int64_t>(sms, std::min<int64_t>(nb_max, (int64_t)5e7 / (cnt_t * cnt_s)));
-        std::vector<NearBlock> blocks(nb);
-        for (int64_t b = 0; b < nb; ++b) blocks[b] = {b * max_ns, cnt_s, b * max_nt, cnt_t};
-        e = cudaMemcpyAsync(buf + o_b, blocks.data(), nb * sizeof(NearBlock), cudaMemcpyHostToDevice, st);
+        std::vector<NearBlock> blocks(nb), kblocks(nb);
+        for (int64_t b = 0; b < nb; ++b) {
+          blocks[b] = {b * max_ns, cnt_s, b * max_nt, cnt_t};
+          // paired records: every block starts at an even source, so pairing the whole list pairs each block
+          kblocks[b] = ops.paired ? NearBlock{b * max_ns / 2, cnt_s / 2, b * max_nt, cnt_t} : blocks[b];
+        }
+        e = cudaMemcpyAsync(buf + o_b, kblocks.data(), nb * sizeof(NearBlock), cudaMemcpyHostToDevice, st);
         float best_ms = 1e30f;
         int best = table[c];
         for (int split = 1; split <= 8 && e == cudaSuccess; split *= 2) {
@@ -246,7 +252,11 @@ cudaError_t enqueue(sctlgpu_near_plan_s* P, const void* const* k, unsigned flags
     e = compute_bbox(s, P->nt, (const double*)r_trg, P->ns, (const double*)r_src, P->d_bbox);
     if (e != cudaSuccess) return e;
   }
-  e = P->ops.pack(s, P->ns, r_src, P->ND ? n_src : nullptr, v_src, w_src, P->d_recs, P->d_bbox, P->sms);
+  if (P->ops.paired)
+    e = P->ops.pack_blocks(s, P->nblk, P->d_blocks, P->d_src_blocks, P->n_pairs, r_src, P->ND ? n_src : nullptr,
+                           v_src, w_src, P->d_recs, P->d_bbox, P->sms);
+  else
+    e = P->ops.pack(s, P->ns, r_src, P->ND ? n_src : nullptr, v_src, w_src, P->d_recs, P->d_bbox, P->sms);
   if (e != cudaSuccess) return e;
   const bool accumulate = flags & SCTLGPU_ACCUMULATE;
   if ((P->has_map || P->d_tidx) && !accumulate) {
@@ -277,6 +287,7 @@ void free_plan(sctlgpu_near_plan_s* P) {
   if (P->cap) cudaStreamDestroy(P->cap);
   cudaFree(P->d_items);
   cudaFree(P->d_blocks);
+  cudaFree(P->d_src_blocks);
   cudaFree(P->d_map);
   cudaFree(P->d_tidx);
   cudaFree(P->d_scratch);
@@ -377,11 +388,21 @@ int sctlgpu_near_plan_create_indexed(sctlgpu_near_plan* out, int kernel, int mod
     return rc;
   }
   std::vector<NearItem> items;
-  build_items(hb, table, P->ops.T, items);
+  build_items(hb, table, P->ops.T, items);  // size classes and costs by source counts
   P->n_items = (int64_t)items.size();
+  std::vector<NearBlock> hk = hb;  // the kernel's table
+  if (P->ops.paired) {
+    int64_t off = 0;
+    for (size_t b = 0; b < hb.size(); ++b) {
+      const int64_t np = (hb[b].ns + 1) / 2;
+      hk[b] = {off, np, hb[b].t0, hb[b].nt};
+      off += np;
+    }
+    P->n_pairs = off;
+  }
 
   cudaError_t e = cudaSuccess;
-  const size_t rec_bytes = ((size_t)ns * P->ops.rec_bytes + 255) / 256 * 256;
+  const size_t rec_bytes = ((size_t)(P->ops.paired ? P->n_pairs : ns) * P->ops.rec_bytes + 255) / 256 * 256;
   do {
     if ((e = cudaStreamCreateWithFlags(&P->cap, cudaStreamNonBlocking))) break;
     if ((e = cudaMalloc(&P->d_items, std::max<size_t>(1, items.size()) * sizeof(NearItem)))) break;
@@ -394,8 +415,14 @@ int sctlgpu_near_plan_create_indexed(sctlgpu_near_plan* out, int kernel, int mod
     if (!items.empty() &&
         (e = cudaMemcpy(P->d_items, items.data(), items.size() * sizeof(NearItem), cudaMemcpyHostToDevice)))
       break;
-    if (!hb.empty() && (e = cudaMemcpy(P->d_blocks, hb.data(), hb.size() * sizeof(NearBlock), cudaMemcpyHostToDevice)))
+    if (!hk.empty() && (e = cudaMemcpy(P->d_blocks, hk.data(), hk.size() * sizeof(NearBlock), cudaMemcpyHostToDevice)))
       break;
+    if (P->ops.paired) {
+      if ((e = cudaMalloc(&P->d_src_blocks, std::max<size_t>(1, hb.size()) * sizeof(NearBlock)))) break;
+      if (!hb.empty() &&
+          (e = cudaMemcpy(P->d_src_blocks, hb.data(), hb.size() * sizeof(NearBlock), cudaMemcpyHostToDevice)))
+        break;
+    }
     if ((e = cudaMemset(P->d_status, 0, sizeof(unsigned)))) break;
     if (trg_map) {
       if ((e = cudaMalloc(&P->d_map, std::max<int64_t>(1, nlist) * sizeof(int64_t)))) break;

@@ -265,7 +265,8 @@ def test_matches_the_reference_legacy_quadrature(setup):
     golden also holds the legacy values with a 64-point direct rule: where the two agree to 1e-11
     the legacy value is exact to its rounding and the GPU must match it to 1e-9; elsewhere (targets
     next to a panel edge, whose neighbour the legacy rule integrates with its plain direct rule)
-    the two values' difference bounds the legacy's own error, and the GPU must lie within it."""
+    twice the two values' difference bounds the legacy's own error (the denser rule at least
+    halves it), and the GPU must lie within that."""
     import json
     import os
     torch, T, S = setup
@@ -293,4 +294,5 @@ def test_matches_the_reference_legacy_quadrature(setup):
               f"{est.max():.3e})")
         # the potentials are O(1): 1e-9 absolute
         assert err[trusted].max() < 1e-9, (arith, err[trusted].max())
-        assert np.all(err <= est + 1e-9), (arith, np.max(err - est))
+        # elsewhere the denser rule at least halves the legacy's error, so |U - exact| <= 2 |U - U64|
+        assert np.all(err <= 2 * est + 1e-9), (arith, np.max(err - 2 * est))
