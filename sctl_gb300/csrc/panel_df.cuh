@@ -81,6 +81,62 @@ __device__ __forceinline__ f2 rsqrt(f2 R, float* rho_out, float* y0_out) {
 
 }  // namespace dfq
 
+// Packed forms of the dfq operations (fma/add/mul.rn.f32x2): two quadrature
+// nodes per lane, lane x and lane y, each with exactly the scalar sequence of
+// roundings.  GB300 runs the double-float quadrature issue-bound on the FP32
+// pipe; one f32x2 instruction per two nodes halves the issue slots.
+namespace pdfq {
+
+using v2 = float2;
+struct d2 {
+  v2 h, l;
+};
+__device__ __forceinline__ v2 dup(float a) { return make_float2(a, a); }
+__device__ __forceinline__ v2 vneg(v2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ v2 vadd(v2 a, v2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ v2 vsub(v2 a, v2 b) { return __fadd2_rn(a, vneg(b)); }
+__device__ __forceinline__ v2 vmul(v2 a, v2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ v2 vfma(v2 a, v2 b, v2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ d2 dupf2(sctlgpu::f2 x) { return {dup(x.h), dup(x.l)}; }
+__device__ __forceinline__ d2 pair(sctlgpu::f2 x, sctlgpu::f2 y) { return {make_float2(x.h, y.h), make_float2(x.l, y.l)}; }
+__device__ __forceinline__ d2 two_prod(v2 a, v2 b) {
+  const v2 p = vmul(a, b);
+  return {p, vfma(a, b, vneg(p))};
+}
+__device__ __forceinline__ d2 two_sum(v2 a, v2 b) {
+  const v2 s = vadd(a, b);
+  const v2 bb = vsub(s, a);
+  return {s, vadd(vsub(a, vsub(s, bb)), vsub(b, bb))};
+}
+__device__ __forceinline__ d2 norm(d2 x) {
+  const v2 s = vadd(x.h, x.l);
+  return {s, vsub(x.l, vsub(s, x.h))};
+}
+__device__ __forceinline__ d2 neg(d2 x) { return {vneg(x.h), vneg(x.l)}; }
+__device__ __forceinline__ d2 mul(d2 a, d2 b) {
+  const v2 p = vmul(a.h, b.h);
+  v2 e = vfma(a.h, b.h, vneg(p));
+  e = vfma(a.h, b.l, e);
+  e = vfma(a.l, b.h, e);
+  return {p, e};
+}
+__device__ __forceinline__ d2 mulf(d2 a, v2 b) {
+  const v2 p = vmul(a.h, b);
+  return {p, vfma(a.l, b, vfma(a.h, b, vneg(p)))};
+}
+__device__ __forceinline__ d2 add(d2 a, d2 b) {
+  const d2 s = two_sum(a.h, b.h);
+  return norm({s.h, vadd(vadd(s.l, a.l), b.l)});
+}
+__device__ __forceinline__ d2 sub(d2 a, d2 b) { return add(a, neg(b)); }
+__device__ __forceinline__ void fma_acc(d2& acc, d2 a, d2 b) {
+  const d2 p = mul(a, b);
+  const d2 s = two_sum(acc.h, p.h);
+  acc = {s.h, vadd(acc.l, vadd(s.l, p.l))};
+}
+
+}  // namespace pdfq
+
 // Per-warp shared state of the double-float kernel.  All boxes of one round
 // have the same size (2^-depth), so only their corners are queued; the
 // weights-mode arrays exist only in the weights-mode layout (smaller footprint
@@ -97,8 +153,20 @@ struct PanelWarpSmemDFW : PanelWarpSmemDF {
   f2 T[PQ_GL][PQ_P];
   f2 W[PQ_NODES];
 };
+// Potential-mode layout: Gauss rows i and i + 4 side by side (lane x, lane y)
+// so that one lane integrates two nodes with f32x2 arithmetic and one 16-byte
+// shared load per operand pair.  Same footprint as PanelWarpSmemDF.
+struct PanelWarpSmemDFP {
+  f2 F[4][PQ_NODES];
+  pdfq::d2 LsP[PQ_GL / 2][PQ_P], LdsP[PQ_GL / 2][PQ_P];
+  f2 Lt[PQ_GL][PQ_P], Ldt[PQ_GL][PQ_P];
+  pdfq::d2 AP[7][PQ_GL / 2][PQ_P];
+  float box[2][PQ_QUEUE][2];
+  float leaf[PQ_QUEUE][2];
+};
+static_assert(sizeof(PanelWarpSmemDFP) == sizeof(PanelWarpSmemDF), "packed layout keeps the footprint");
 template <bool WEIGHTS>
-using DFSmem = typename std::conditional<WEIGHTS, PanelWarpSmemDFW, PanelWarpSmemDF>::type;
+using DFSmem = typename std::conditional<WEIGHTS, PanelWarpSmemDFW, PanelWarpSmemDFP>::type;
 
 __constant__ float c_gl_xh[PQ_GL], c_gl_xl[PQ_GL];        // Gauss-Legendre nodes, double-float
 __constant__ float c_gl_wh[PQ_GL], c_gl_wl[PQ_GL];        // and weights
@@ -146,6 +214,106 @@ __device__ __forceinline__ void basis_df(f2 s, f2 (&l)[PQ_P], f2 (&d)[PQ_P]) {
   }
 }
 
+// One accepted box of size bz at (bs, bt), potential mode: basis values as
+// above, then L_s F and the 64 Gauss nodes with two nodes per lane -- rows r
+// and r + 4 of the box's 8 x 8 rule in lanes x and y of f32x2 operations, each
+// lane with the same roundings as the scalar form.  acc gathers the lane's
+// two node sums.
+template <int KER>
+__device__ __forceinline__ void leaf_potential_pk(PanelWarpSmemDFP& sm, int lane, float bs, float bt, float bz,
+                                                  pdfq::d2& acc) {
+  constexpr int H = PQ_GL / 2;
+  if (lane < 2 * PQ_GL) {
+    const int i = lane % PQ_GL;
+    const f2 g = {c_gl_xh[i], c_gl_xl[i]};
+    const f2 s = dfq::add({lane < PQ_GL ? bs : bt, 0.f}, dfq::mulf(g, bz));
+    f2 l[PQ_P], d[PQ_P];
+    basis_df(s, l, d);
+    const int r = i % H;
+    const int y = i >= H ? 1 : 0;
+#pragma unroll
+    for (int a = 0; a < PQ_P; ++a) {
+      if (lane < PQ_GL) {
+        // d2 = {h.x, h.y, l.x, l.y}: row i's words sit at offsets y and 2 + y
+        float* ls = reinterpret_cast<float*>(&sm.LsP[r][a]) + y;
+        float* ld = reinterpret_cast<float*>(&sm.LdsP[r][a]) + y;
+        ls[0] = l[a].h;
+        ls[2] = l[a].l;
+        ld[0] = d[a].h;
+        ld[2] = d[a].l;
+      } else {
+        sm.Lt[i][a] = l[a];
+        sm.Ldt[i][a] = d[a];
+      }
+    }
+  }
+  __syncwarp();
+  for (int e = lane; e < 7 * H * PQ_P; e += 32) {
+    const int m = e / (H * PQ_P), r = (e / PQ_P) % H, b = e % PQ_P;
+    const int c = m < 4 ? m : m - 4;
+    const pdfq::d2* L = m < 4 ? sm.LsP[r] : sm.LdsP[r];
+    pdfq::d2 v = {};
+#pragma unroll
+    for (int a = 0; a < PQ_P; ++a) pdfq::fma_acc(v, L[a], pdfq::dupf2(sm.F[c][a * PQ_P + b]));
+    sm.AP[m][r][b] = pdfq::norm(v);
+  }
+  __syncwarp();
+  const int r = lane / PQ_GL, j = lane % PQ_GL;  // nodes (r, j) and (r + 4, j)
+  pdfq::d2 X[3] = {}, Xs[3] = {}, Xt[3] = {}, sg = {};
+#pragma unroll 2
+  for (int b = 0; b < PQ_P; ++b) {
+    const pdfq::d2 lt = pdfq::dupf2(sm.Lt[j][b]), ldt = pdfq::dupf2(sm.Ldt[j][b]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const pdfq::d2 ac = sm.AP[c][r][b];
+      pdfq::fma_acc(X[c], ac, lt);
+      pdfq::fma_acc(Xt[c], ac, ldt);
+      pdfq::fma_acc(Xs[c], sm.AP[4 + c][r][b], lt);
+    }
+    pdfq::fma_acc(sg, sm.AP[3][r][b], lt);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    X[c] = pdfq::norm(X[c]);  // X = x_s - x_t = -r
+    Xs[c] = pdfq::norm(Xs[c]);
+    Xt[c] = pdfq::norm(Xt[c]);
+  }
+  using pdfq::add;
+  using pdfq::mul;
+  using pdfq::sub;
+  const pdfq::d2 n0 = sub(mul(Xs[1], Xt[2]), mul(Xs[2], Xt[1]));
+  const pdfq::d2 n1 = sub(mul(Xs[2], Xt[0]), mul(Xs[0], Xt[2]));
+  const pdfq::d2 n2 = sub(mul(Xs[0], Xt[1]), mul(Xs[1], Xt[0]));
+  const pdfq::d2 R = add(add(mul(X[0], X[0]), mul(X[1], X[1])), mul(X[2], X[2]));
+  // 1/sqrt(R): hardware estimate per lane, one Newton step on the exact residual (dfq::rsqrt)
+  float2 y0 = make_float2(sctlgpu::rsqrt_seed(R.h.x), sctlgpu::rsqrt_seed(R.h.y));
+  y0.x = R.h.x > 0.f ? y0.x : 0.f;
+  y0.y = R.h.y > 0.f ? y0.y : 0.f;
+  const pdfq::d2 q = pdfq::two_prod(y0, y0);
+  float2 rho = pdfq::vfma(pdfq::vneg(q.h), R.h, pdfq::dup(1.f));
+  rho = pdfq::vfma(pdfq::vneg(q.l), R.h, rho);
+  rho = pdfq::vfma(pdfq::vneg(q.h), R.l, rho);
+  const pdfq::d2 yv = {y0, pdfq::vmul(pdfq::vmul(pdfq::dup(0.5f), y0), rho)};
+  const pdfq::d2 wi = pdfq::pair({c_gl_wh[r], c_gl_wl[r]}, {c_gl_wh[r + H], c_gl_wl[r + H]});
+  const pdfq::d2 w = pdfq::mulf(mul(wi, pdfq::dupf2({c_gl_wh[j], c_gl_wl[j]})), pdfq::dup(bz * bz));
+  pdfq::d2 kda;
+  if (KER == 0) {  // single layer: |n| / r
+    const pdfq::d2 J2 = add(add(mul(n0, n0), mul(n1, n1)), mul(n2, n2));
+    const float2 jh = make_float2(sqrtf(J2.h.x), sqrtf(J2.h.y));
+    const pdfq::d2 jp = pdfq::two_prod(jh, jh);
+    const float2 jl = make_float2(jh.x > 0.f ? ((J2.h.x - jp.h.x - jp.l.x) + J2.l.x) / (2.f * jh.x) : 0.f,
+                                  jh.y > 0.f ? ((J2.h.y - jp.h.y - jp.l.y) + J2.l.y) / (2.f * jh.y) : 0.f);
+    kda = mul(mul(pdfq::norm({jh, jl}), yv), w);
+  } else {  // double layer: (r . n) / r^3 with r = -X
+    const pdfq::d2 rn = pdfq::neg(add(add(mul(X[0], n0), mul(X[1], n1)), mul(X[2], n2)));
+    pdfq::d2 y3 = pdfq::mulf(pdfq::two_prod(y0, y0), y0);  // y0^3 (1 + 3 rho / 2)
+    y3.l = pdfq::vfma(y3.h, pdfq::vmul(pdfq::dup(1.5f), rho), y3.l);
+    kda = mul(mul(rn, y3), w);
+  }
+  pdfq::fma_acc(acc, kda, pdfq::norm(sg));
+  acc = pdfq::norm(acc);
+}
+
 template <int KER, bool WEIGHTS>
 __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParams p) {
   extern __shared__ __align__(16) unsigned char pq_smem_df[];
@@ -181,7 +349,7 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
       }
     }
     __syncwarp();
-    f2 acc = {0.f, 0.f};
+    pdfq::d2 acc = {};  // potential mode: the lane's two node sums
     int cur = 0, ncur = 1, nleaf = 0;
     if (lane == 0) {
       sm.box[0][0][0] = 0.0f;
@@ -196,86 +364,85 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
       auto integrate_leaves = [&]() {
         for (int lf = 0; lf < nleaf; ++lf) {
           const float bs = sm.leaf[lf][0], bt = sm.leaf[lf][1];
-          if (lane < 2 * PQ_GL) {
-            const int i = lane % PQ_GL;
-            // s = b0 + bz * g_i (b0, bz dyadic: exact floats)
-            const f2 g = {c_gl_xh[i], c_gl_xl[i]};
-            const f2 s = dfq::add({lane < PQ_GL ? bs : bt, 0.f}, dfq::mulf(g, bz));
-            f2 l[PQ_P], d[PQ_P];
-            basis_df(s, l, d);
-  #pragma unroll
-            for (int a = 0; a < PQ_P; ++a) {
-              if (lane < PQ_GL) {
-                sm.Ls[i][a] = l[a];
-                sm.Lds[i][a] = d[a];
-              } else {
-                sm.Lt[i][a] = l[a];
-                sm.Ldt[i][a] = d[a];
+          if constexpr (!WEIGHTS) {
+            leaf_potential_pk<KER>(sm, lane, bs, bt, bz, acc);
+            __syncwarp();
+          } else {
+            if (lane < 2 * PQ_GL) {
+              const int i = lane % PQ_GL;
+              // s = b0 + bz * g_i (b0, bz dyadic: exact floats)
+              const f2 g = {c_gl_xh[i], c_gl_xl[i]};
+              const f2 s = dfq::add({lane < PQ_GL ? bs : bt, 0.f}, dfq::mulf(g, bz));
+              f2 l[PQ_P], d[PQ_P];
+              basis_df(s, l, d);
+    #pragma unroll
+              for (int a = 0; a < PQ_P; ++a) {
+                if (lane < PQ_GL) {
+                  sm.Ls[i][a] = l[a];
+                  sm.Lds[i][a] = d[a];
+                } else {
+                  sm.Lt[i][a] = l[a];
+                  sm.Ldt[i][a] = d[a];
+                }
               }
             }
-          }
-          __syncwarp();
-          for (int e = lane; e < 7 * PQ_GL * PQ_P; e += 32) {
-            const int m = e / (PQ_GL * PQ_P), i = (e / PQ_P) % PQ_GL, b = e % PQ_P;
-            if (WEIGHTS && m == 3) continue;  // no density in weights mode
-            const int c = m < 4 ? m : m - 4;
-            const f2* L = m < 4 ? sm.Ls[i] : sm.Lds[i];
-            f2 v = {0.f, 0.f};
-  #pragma unroll
-            for (int a = 0; a < PQ_P; ++a) dfq::fma_acc(v, L[a], sm.F[c][a * PQ_P + b]);
-            sm.A[m][i][b] = dfq::norm(v);
-          }
-          __syncwarp();
-          const float bz2 = bz * bz;
-          for (int gq = lane; gq < PQ_GL * PQ_GL; gq += 32) {
-            const int i = gq / PQ_GL, j = gq % PQ_GL;
-            f2 X[3] = {}, Xs[3] = {}, Xt[3] = {}, sg = {0.f, 0.f};
-  #pragma unroll 2
-            for (int b = 0; b < PQ_P; ++b) {
-              const f2 lt = sm.Lt[j][b], ldt = sm.Ldt[j][b];
-  #pragma unroll
+            __syncwarp();
+            for (int e = lane; e < 7 * PQ_GL * PQ_P; e += 32) {
+              const int m = e / (PQ_GL * PQ_P), i = (e / PQ_P) % PQ_GL, b = e % PQ_P;
+              if (m == 3) continue;  // no density in weights mode
+              const int c = m < 4 ? m : m - 4;
+              const f2* L = m < 4 ? sm.Ls[i] : sm.Lds[i];
+              f2 v = {0.f, 0.f};
+    #pragma unroll
+              for (int a = 0; a < PQ_P; ++a) dfq::fma_acc(v, L[a], sm.F[c][a * PQ_P + b]);
+              sm.A[m][i][b] = dfq::norm(v);
+            }
+            __syncwarp();
+            const float bz2 = bz * bz;
+            for (int gq = lane; gq < PQ_GL * PQ_GL; gq += 32) {
+              const int i = gq / PQ_GL, j = gq % PQ_GL;
+              f2 X[3] = {}, Xs[3] = {}, Xt[3] = {};
+    #pragma unroll 2
+              for (int b = 0; b < PQ_P; ++b) {
+                const f2 lt = sm.Lt[j][b], ldt = sm.Ldt[j][b];
+    #pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                  dfq::fma_acc(X[c], sm.A[c][i][b], lt);
+                  dfq::fma_acc(Xt[c], sm.A[c][i][b], ldt);
+                  dfq::fma_acc(Xs[c], sm.A[4 + c][i][b], lt);
+                }
+              }
+    #pragma unroll
               for (int c = 0; c < 3; ++c) {
-                dfq::fma_acc(X[c], sm.A[c][i][b], lt);
-                dfq::fma_acc(Xt[c], sm.A[c][i][b], ldt);
-                dfq::fma_acc(Xs[c], sm.A[4 + c][i][b], lt);
+                X[c] = dfq::norm(X[c]);  // X = x_s - x_t = -r
+                Xs[c] = dfq::norm(Xs[c]);
+                Xt[c] = dfq::norm(Xt[c]);
               }
-              if (!WEIGHTS) dfq::fma_acc(sg, sm.A[3][i][b], lt);
-            }
-  #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              X[c] = dfq::norm(X[c]);  // X = x_s - x_t = -r
-              Xs[c] = dfq::norm(Xs[c]);
-              Xt[c] = dfq::norm(Xt[c]);
-            }
-            // unnormalised normal n = Xs x Xt (|n| = area element of the parameter square)
-            const f2 n0 = dfq::sub(dfq::mul(Xs[1], Xt[2]), dfq::mul(Xs[2], Xt[1]));
-            const f2 n1 = dfq::sub(dfq::mul(Xs[2], Xt[0]), dfq::mul(Xs[0], Xt[2]));
-            const f2 n2 = dfq::sub(dfq::mul(Xs[0], Xt[1]), dfq::mul(Xs[1], Xt[0]));
-            f2 R = dfq::add(dfq::add(dfq::mul(X[0], X[0]), dfq::mul(X[1], X[1])), dfq::mul(X[2], X[2]));
-            float rho, y0;
-            const f2 y = dfq::rsqrt(R, &rho, &y0);
-            const f2 w = dfq::mulf(dfq::mul({c_gl_wh[i], c_gl_wl[i]}, {c_gl_wh[j], c_gl_wl[j]}), bz2);
-            f2 kda;
-            if (KER == 0) {  // single layer: |n| / r
-              const f2 J2 = dfq::add(dfq::add(dfq::mul(n0, n0), dfq::mul(n1, n1)), dfq::mul(n2, n2));
-              const float jh = sqrtf(J2.h);
-              const f2 jp = two_prod(jh, jh);
-              const f2 J = dfq::norm({jh, jh > 0.f ? ((J2.h - jp.h - jp.l) + J2.l) / (2.f * jh) : 0.f});
-              kda = dfq::mul(dfq::mul(J, y), w);
-            } else {  // double layer: (r . n) / r^3 with r = -X
-              const f2 rn = dfq::neg(
-                  dfq::add(dfq::add(dfq::mul(X[0], n0), dfq::mul(X[1], n1)), dfq::mul(X[2], n2)));
-              f2 y3 = dfq::mulf(two_prod(y0, y0), y0);  // y0^3 (1 + 3 rho / 2)
-              y3.l = fmaf(y3.h, 1.5f * rho, y3.l);
-              kda = dfq::mul(dfq::mul(rn, y3), w);
-            }
-            if constexpr (WEIGHTS)
+              // unnormalised normal n = Xs x Xt (|n| = area element of the parameter square)
+              const f2 n0 = dfq::sub(dfq::mul(Xs[1], Xt[2]), dfq::mul(Xs[2], Xt[1]));
+              const f2 n1 = dfq::sub(dfq::mul(Xs[2], Xt[0]), dfq::mul(Xs[0], Xt[2]));
+              const f2 n2 = dfq::sub(dfq::mul(Xs[0], Xt[1]), dfq::mul(Xs[1], Xt[0]));
+              f2 R = dfq::add(dfq::add(dfq::mul(X[0], X[0]), dfq::mul(X[1], X[1])), dfq::mul(X[2], X[2]));
+              float rho, y0;
+              const f2 y = dfq::rsqrt(R, &rho, &y0);
+              const f2 w = dfq::mulf(dfq::mul({c_gl_wh[i], c_gl_wl[i]}, {c_gl_wh[j], c_gl_wl[j]}), bz2);
+              f2 kda;
+              if (KER == 0) {  // single layer: |n| / r
+                const f2 J2 = dfq::add(dfq::add(dfq::mul(n0, n0), dfq::mul(n1, n1)), dfq::mul(n2, n2));
+                const float jh = sqrtf(J2.h);
+                const f2 jp = two_prod(jh, jh);
+                const f2 J = dfq::norm({jh, jh > 0.f ? ((J2.h - jp.h - jp.l) + J2.l) / (2.f * jh) : 0.f});
+                kda = dfq::mul(dfq::mul(J, y), w);
+              } else {  // double layer: (r . n) / r^3 with r = -X
+                const f2 rn = dfq::neg(
+                    dfq::add(dfq::add(dfq::mul(X[0], n0), dfq::mul(X[1], n1)), dfq::mul(X[2], n2)));
+                f2 y3 = dfq::mulf(two_prod(y0, y0), y0);  // y0^3 (1 + 3 rho / 2)
+                y3.l = fmaf(y3.h, 1.5f * rho, y3.l);
+                kda = dfq::mul(dfq::mul(rn, y3), w);
+              }
               sm.Kd[i][j] = dfq::norm(kda);
-            else
-              dfq::fma_acc(acc, kda, dfq::norm(sg));
-          }
-          __syncwarp();
-          if constexpr (WEIGHTS) {
+            }
+            __syncwarp();
             for (int e = lane; e < PQ_GL * PQ_P; e += 32) {
               const int i = e / PQ_P, b = e % PQ_P;
               f2 v = {0.f, 0.f};
@@ -293,7 +460,6 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
             }
             __syncwarp();
           }
-          acc = dfq::norm(acc);
         }
         nleaf = 0;
       };
@@ -350,7 +516,7 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
       __syncwarp();
       for (int q = lane; q < PQ_NODES; q += 32) p.out[pr * PQ_NODES + q] = dfq::to_double(sm.W[q]) * p.scale;
     } else {
-      double v = dfq::to_double(acc) + acc_smooth;
+      double v = ((double)acc.h.x + (double)acc.l.x) + ((double)acc.h.y + (double)acc.l.y) + acc_smooth;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
       if (lane == 0) atomicAdd(&p.out[oix], v * p.scale);
