@@ -508,6 +508,56 @@ def torus_section(torch, n_eval=1 << 20, n_train=440000, steps=4000, learned=Tru
     return res
 
 
+def treecode_section(torch, n=1 << 20):
+    """ParticleFMM::Eval's fast path (the treecode, sctlgpu_treecode_*) against the direct sum:
+    the sphere/ball workload at n x n (Laplace DxU, Stokes DxU) and the torus far field (204,800
+    panel nodes, densities sigma * Q, n near-surface targets), mixed arithmetic at digits 6 and
+    10.  Accuracy: relative l2 on a 512-target sample against the FP64 oracle."""
+    import sctl_gb300 as S
+    from oracle import oracle as O
+    from sctl_gb300 import capi
+    from sctl_gb300 import treecode as TC
+    from sctl_gb300 import workloads as W
+    from sctl_gb300.torus import Torus
+    cases = []
+    for k in (1, 3):
+        d = W.sphere_ball(n, n, k, seed=500 + k)
+        cases.append((f"sphere_ball_{NAMES[k]}", k, d["r_src"], d["n_src"], d["r_trg"], d["v_src"]))
+    T = Torus(seed=0)
+    X, N, Q, sig = T.nodes()
+    cases.append(("torus_far_field_Laplace3D_DxU", 1, X, N, T.targets(n, seed=7)["r_trg"], sig * Q))
+    res = {"workload": f"n = {n} targets; sphere/ball sources n on the unit sphere; torus 204,800 nodes"}
+    stream = torch.cuda.current_stream().cuda_stream
+    for name, k, xs, xn, xt, f in cases:
+        td = 3 if k >= 2 else 1
+        nt, ns = xt.shape[0], xs.shape[0]
+        dv = {a: torch.from_numpy(np.ascontiguousarray(v, np.float64).reshape(-1)).cuda()
+              for a, v in (("xs", xs), ("xn", xn), ("xt", xt), ("f", f))}
+        out = torch.empty(nt * td, dtype=torch.float64, device="cuda")
+        sub = np.arange(0, nt, max(1, nt // 512))
+        ref = O.eval(k, xt[sub], xs, xn, f)
+        r = {"n_src": ns, "n_trg": nt}
+        for digits in (6, 10):
+            direct = lambda: S.eval_device(k, capi.MIXED, digits, nt, dv["xt"].data_ptr(), ns, dv["xs"].data_ptr(),  # noqa: E731
+                                           dv["xn"].data_ptr(), dv["f"].data_ptr(), out.data_ptr(), False, stream)
+            t_direct = _ev_ms(torch, direct, reps=1)
+            err_direct = O.rel_l2(out.cpu().numpy().reshape(nt, td)[sub].reshape(-1), ref)
+            t0 = time.perf_counter()
+            tc = TC.Treecode(k, xs, xt, n_src=xn, digits=digits)
+            setup_s = time.perf_counter() - t0
+            t_tc = _ev_ms(torch, lambda: tc.eval(dv["f"], out=out), reps=2)
+            err = O.rel_l2(out.cpu().numpy().reshape(nt, td)[sub].reshape(-1), ref)
+            info = tc.info()
+            tc.close()
+            r[f"digits{digits}"] = {
+                "direct_ms": t_direct, "direct_rel_l2": err_direct, "treecode_ms": t_tc, "treecode_rel_l2": err,
+                "speedup": t_direct / t_tc, "setup_s": setup_s, "order": info["order"], "theta": info["theta"],
+                "interactions_vs_direct": (info["direct_interactions"] + info["proxy_interactions"])
+                / info["direct_sum_interactions"], "clusters": info["clusters"], "blocks": info["blocks"]}
+        res[name] = r
+    return res
+
+
 def learning_curve_section(torch, n_train=220000, steps_list=(2000, 8000, 32000, 96000), batch=1 << 14):
     """Held-out accuracy of the correction network against training length: one network (the
     15 -> 256 -> 256 -> 256 -> 100 GELU MLP on the tcgen05 kernels, singular part subtracted, basis
@@ -557,7 +607,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="timed region only (for profiler runs)")
     ap.add_argument("--skip-torus", action="store_true", help="omit the near-singular torus section")
     ap.add_argument("--section", choices=["near", "near_panel", "clusters", "cube", "torus", "torus_plain", "mlp",
-                                          "ext", "kmat", "ref_full", "learning_curve"],
+                                          "ext", "kmat", "ref_full", "learning_curve", "treecode"],
                     help="run only this secondary workload and print its JSON (profiling of one kernel family)")
     ap.add_argument("--torus-n", type=int, default=1 << 20, help="targets of the torus section")
     args = ap.parse_args()
@@ -579,7 +629,8 @@ def main():
               "ext": lambda: ext_section(torch, stream), "kmat": lambda: kmat_section(torch, stream),
               "torus": lambda: torus_section(torch, n_eval=args.torus_n),
               "torus_plain": lambda: torus_section(torch, n_eval=args.torus_n, learned=False),
-              "learning_curve": lambda: learning_curve_section(torch)}[args.section]
+              "learning_curve": lambda: learning_curve_section(torch),
+              "treecode": lambda: treecode_section(torch)}[args.section]
         print(json.dumps({"section": args.section, **fn()}), flush=True)
         return
 

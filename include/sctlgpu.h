@@ -268,6 +268,53 @@ int sctlgpu_near_list_elem_index(sctlgpu_near_list list, int64_t* near_elem_idx,
 int sctlgpu_near_list_destroy(sctlgpu_near_list list);
 
 /*
+ * Far field by a barycentric Lagrange treecode.  Replaces ParticleFMM::Eval's
+ * fast path, EvalPVFMM (fmm-wrapper.txx:854-1038; Eval at :542-549 takes it for
+ * 40,000 targets or more): v_out = scale * sum_s K(x_t - y_s, n_s) . f_s for
+ * the four hot-path kernels, with work below the direct sum's Ns * Nt.  The
+ * algorithm differs from PVFMM's (a particle-cluster treecode: clusters seen
+ * from far enough are replaced by proxy sources at (order+1)^3 Chebyshev points
+ * carrying interpolated moments; everything else is summed directly); every
+ * interaction runs in the batched near-field kernels with `mode` / `digits`
+ * arithmetic (SCTLGPU_F64 or SCTLGPU_MIXED).
+ *
+ * create: the geometry (host arrays; the reference's SetSrcCoord / SetTrgCoord,
+ * fmm-wrapper.txx:505-540): source coordinates and normals (double-layer
+ * kernels), target coordinates; builds both trees, the interaction blocks and
+ * the device-side plan.  params may be NULL: order and theta then follow
+ * `digits`, leaf_max = 1.5 proxy slots per cluster ((order+1)^3, three times
+ * that for the Stokes double layer), batch_max = 512.
+ * execute: v_src (device, ns * SrcDim, source order as given; SetDensitySL /
+ * DL) -> v_out (device, nt * TrgDim, target order as given); flags may hold
+ * SCTLGPU_ACCUMULATE; asynchronous on `stream`.
+ * info / layout: sizes[7] = {blocks, source slots (leaves padded to even
+ * counts), all slots (with proxies), approximated clusters, direct
+ * interactions, proxy interactions, order}, and the acceptance parameter.
+ * layout is the host-only part of create (no device needed): the blocks
+ * (sources indexing slots), the source of every slot (-1 padding, -2 proxy),
+ * the target order of the blocks' target ranges, and per approximated cluster
+ * {source slot begin, end, proxy slot begin, end}; any output may be NULL.
+ */
+typedef struct sctlgpu_treecode_params {
+  double theta;  /* a cluster is approximated when (r_batch + r_cluster) < theta * distance; <= 0: from digits */
+  int order;     /* interpolation degree per dimension, 1..15; <= 0: from digits */
+  int leaf_max;  /* sources per leaf; <= 0: 1.5 proxy slots */
+  int batch_max; /* targets per batch; <= 0: 512 */
+} sctlgpu_treecode_params;
+typedef struct sctlgpu_treecode_s* sctlgpu_treecode;
+int sctlgpu_treecode_create(sctlgpu_treecode* tc, int kernel, int mode, int digits, int64_t ns, const double* r_src,
+                            const double* n_src, int64_t nt, const double* r_trg,
+                            const sctlgpu_treecode_params* params);
+int sctlgpu_treecode_execute(sctlgpu_treecode tc, const double* v_src, double* v_out, unsigned flags, void* stream);
+int sctlgpu_treecode_info(sctlgpu_treecode tc, int64_t* sizes, double* theta);
+/* Synchronises `stream`; SCTLGPU_ERR_DEVICE_TIMEOUT if a bounded device wait gave up. */
+int sctlgpu_treecode_status(sctlgpu_treecode tc, void* stream);
+int sctlgpu_treecode_destroy(sctlgpu_treecode tc);
+int sctlgpu_treecode_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, const double* r_trg,
+                            const sctlgpu_treecode_params* params, int digits, int64_t* sizes, double* theta,
+                            sctlgpu_block* blocks, int64_t* slot_src, int64_t* trg_order, int64_t* clusters);
+
+/*
  * Applies precomputed near-interaction matrices and sums them per target:
  * replaces BoundaryIntegralOp::ComputeNearInterac's per-block GEMV, ScatterForward
  * and per-target accumulation (boundary_integral.txx:1311-1381) with one pass.

@@ -26,6 +26,7 @@ struct sctlgpu_near_plan_s {
   NearBlock* d_blocks = nullptr;      // the kernel's table (pair records when ops.paired)
   NearBlock* d_src_blocks = nullptr;  // paired plans: every block's source range, for the per-block pack
   int64_t n_pairs = 0;                // paired plans: pair records of all blocks
+  bool shared_pairs = false;          // paired plans whose blocks all start and end on pair boundaries
   int64_t* d_map = nullptr;
   int64_t* d_tidx = nullptr;
   int64_t n_index = 0;
@@ -252,7 +253,7 @@ cudaError_t enqueue(sctlgpu_near_plan_s* P, const void* const* k, unsigned flags
     e = compute_bbox(s, P->nt, (const double*)r_trg, P->ns, (const double*)r_src, P->d_bbox);
     if (e != cudaSuccess) return e;
   }
-  if (P->ops.paired)
+  if (P->ops.paired && !P->shared_pairs)
     e = P->ops.pack_blocks(s, P->nblk, P->d_blocks, P->d_src_blocks, P->n_pairs, r_src, P->ND ? n_src : nullptr,
                            v_src, w_src, P->d_recs, P->d_bbox, P->sms);
   else
@@ -392,13 +393,19 @@ int sctlgpu_near_plan_create_indexed(sctlgpu_near_plan* out, int kernel, int mod
   P->n_items = (int64_t)items.size();
   std::vector<NearBlock> hk = hb;  // the kernel's table
   if (P->ops.paired) {
+    // Blocks that all start on an even source and end on an even one (or at the
+    // list's end) share one pairing of the whole list (source 2j with 2j + 1),
+    // packed once; otherwise every block's sources are paired on their own.
+    bool aligned = true;
+    for (const NearBlock& b : hb) aligned = aligned && b.s0 % 2 == 0 && (b.ns % 2 == 0 || b.s0 + b.ns == ns);
+    P->shared_pairs = aligned;
     int64_t off = 0;
     for (size_t b = 0; b < hb.size(); ++b) {
       const int64_t np = (hb[b].ns + 1) / 2;
-      hk[b] = {off, np, hb[b].t0, hb[b].nt};
+      hk[b] = {aligned ? hb[b].s0 / 2 : off, np, hb[b].t0, hb[b].nt};
       off += np;
     }
-    P->n_pairs = off;
+    P->n_pairs = aligned ? (ns + 1) / 2 : off;
   }
 
   cudaError_t e = cudaSuccess;
@@ -417,7 +424,7 @@ int sctlgpu_near_plan_create_indexed(sctlgpu_near_plan* out, int kernel, int mod
       break;
     if (!hk.empty() && (e = cudaMemcpy(P->d_blocks, hk.data(), hk.size() * sizeof(NearBlock), cudaMemcpyHostToDevice)))
       break;
-    if (P->ops.paired) {
+    if (P->ops.paired && !P->shared_pairs) {
       if ((e = cudaMalloc(&P->d_src_blocks, std::max<size_t>(1, hb.size()) * sizeof(NearBlock)))) break;
       if (!hb.empty() &&
           (e = cudaMemcpy(P->d_src_blocks, hb.data(), hb.size() * sizeof(NearBlock), cudaMemcpyHostToDevice)))

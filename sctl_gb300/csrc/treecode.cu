@@ -1,0 +1,688 @@
+// Far field by a barycentric Lagrange treecode: the role ParticleFMM::Eval
+// (fmm-wrapper.txx:542-549) gives EvalPVFMM (fmm-wrapper.txx:854-1038) for
+// 40,000 targets or more -- U(x_t) = sum_s K(x_t, y_s) q_s to `digits`, with
+// work below the O(N M) of the direct sum.  The algorithm is not PVFMM's (an
+// FMM with equivalent densities and M2L translations): it is a particle-cluster
+// treecode whose cluster approximations are themselves direct sums, so every
+// interaction runs in the batched near-field kernels of near_plan.cu with the
+// arithmetic `digits` selects there.
+//
+//  * host: an octree over the sources (tight boxes split at their centres,
+//    leaves of <= leaf_max sources) and one over the targets whose leaves are
+//    the target batches (<= batch_max).  Sources are laid out leaf by leaf and
+//    every leaf is padded to an even count with zero-charge slots, so every
+//    cluster's slot range starts and ends on a pair boundary: the plan pairs
+//    the whole slot list once (packed double-float records) for all blocks.
+//  * traversal per batch from the root: a cluster is approximated when
+//    (r_batch + r_cluster) < theta |c_batch - c_cluster| and it holds more
+//    sources than proxy slots, a leaf is summed directly, anything else descends.
+//  * an approximated cluster carries (order + 1)^3 proxy sources at the
+//    tensor-product Chebyshev points (second kind) of its box; with the
+//    Lagrange basis L_k, K(x, y) ~ sum_k L_k(y) K(x, z_k) for y in the box, so
+//    the proxies carry the moments M_k = sum_s L_k(y_s) q_s of the cluster's
+//    source charges q_s: the density (single layers), the density times the
+//    normal (Laplace double layer: the moment is the proxy's normal), or
+//    normal (x) density (Stokes double layer: three proxies per point with
+//    unit normals e_c and densities M_k[c][:]).
+//  * device, per evaluation: densities gathered into slot order, moments in
+//    FP64 per (cluster, 256-slot chunk), reduced per cluster in chunk order
+//    (deterministic), then one execution of the near-field plan over the
+//    (batch, leaf range) and (batch, proxy range) blocks.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sctlgpu.h"
+#include "launch.h"
+
+namespace sctlgpu {
+namespace {
+
+constexpr int TC_MAX_NP = 16;   // Chebyshev points per dimension (order + 1)
+constexpr int TC_CHUNK = 256;   // source slots per moment work item
+constexpr int TC_THREADS = 256;
+
+struct TcNode {
+  int64_t b = 0, e = 0;    // points [b, e) of the tree's permutation
+  int64_t sb = 0, se = 0;  // slots [sb, se) (sources: leaves padded to even counts)
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0}, c[3] = {0, 0, 0}, r = 0;
+  int32_t child0 = -1, nchild = 0;  // children are consecutive nodes
+  int64_t proxy = -1;               // first proxy slot of an approximated cluster
+};
+
+void set_box(const double* X, const std::vector<int64_t>& perm, TcNode& nd) {
+  for (int d = 0; d < 3; ++d) {
+    nd.lo[d] = INFINITY;
+    nd.hi[d] = -INFINITY;
+  }
+  for (int64_t i = nd.b; i < nd.e; ++i)
+    for (int d = 0; d < 3; ++d) {
+      const double v = X[perm[i] * 3 + d];
+      nd.lo[d] = std::min(nd.lo[d], v);
+      nd.hi[d] = std::max(nd.hi[d], v);
+    }
+  double r2 = 0;
+  for (int d = 0; d < 3; ++d) {
+    nd.c[d] = 0.5 * (nd.lo[d] + nd.hi[d]);
+    r2 += 0.25 * (nd.hi[d] - nd.lo[d]) * (nd.hi[d] - nd.lo[d]);
+  }
+  nd.r = std::sqrt(r2);
+}
+
+// Octree on tight boxes: a node with more than `leaf_max` points is split at
+// its box centre into its non-empty octants (children consecutive, in octant
+// order, which is also their order in `perm`).
+void build_octree(const double* X, int64_t n, int64_t leaf_max, std::vector<int64_t>& perm,
+                  std::vector<TcNode>& nodes) {
+  perm.resize((size_t)n);
+  std::iota(perm.begin(), perm.end(), (int64_t)0);
+  nodes.assign(1, TcNode{});
+  nodes[0].b = 0;
+  nodes[0].e = n;
+  if (n == 0) return;
+  set_box(X, perm, nodes[0]);
+  std::vector<int64_t> tmp((size_t)n);
+  std::vector<std::pair<int32_t, int>> stack{{0, 0}};
+  while (!stack.empty()) {
+    const auto [id, depth] = stack.back();
+    stack.pop_back();
+    const TcNode nd = nodes[id];
+    if (nd.e - nd.b <= leaf_max || depth >= 60) continue;
+    if (nd.hi[0] == nd.lo[0] && nd.hi[1] == nd.lo[1] && nd.hi[2] == nd.lo[2]) continue;  // coincident points
+    int64_t cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0}, off[8];
+    auto octant = [&](int64_t p) {
+      const double* x = X + p * 3;
+      return (x[0] > nd.c[0] ? 1 : 0) | (x[1] > nd.c[1] ? 2 : 0) | (x[2] > nd.c[2] ? 4 : 0);
+    };
+    for (int64_t i = nd.b; i < nd.e; ++i) ++cnt[octant(perm[i])];
+    off[0] = nd.b;
+    for (int o = 1; o < 8; ++o) off[o] = off[o - 1] + cnt[o - 1];
+    int64_t pos[8];
+    std::copy(off, off + 8, pos);
+    for (int64_t i = nd.b; i < nd.e; ++i) tmp[pos[octant(perm[i])]++] = perm[i];
+    std::copy(tmp.begin() + nd.b, tmp.begin() + nd.e, perm.begin() + nd.b);
+    nodes[id].child0 = (int32_t)nodes.size();
+    for (int o = 0; o < 8; ++o) {
+      if (!cnt[o]) continue;
+      TcNode ch;
+      ch.b = off[o];
+      ch.e = off[o] + cnt[o];
+      set_box(X, perm, ch);
+      nodes.push_back(ch);
+      ++nodes[id].nchild;
+    }
+    for (int k = nodes[id].nchild - 1; k >= 0; --k) stack.push_back({nodes[id].child0 + k, depth + 1});
+  }
+}
+
+// Interpolation box of a cluster: its tight box, every side at least 1e-3 of
+// the longest one (a flat cluster keeps a well-posed tensor grid), centred.
+void interp_box(const TcNode& C, double lo[3], double ext[3]) {
+  double emax = 0;
+  for (int d = 0; d < 3; ++d) emax = std::max(emax, C.hi[d] - C.lo[d]);
+  if (emax <= 0) emax = 1e-3 * std::max(1.0, std::fabs(C.c[0]) + std::fabs(C.c[1]) + std::fabs(C.c[2]));
+  for (int d = 0; d < 3; ++d) {
+    ext[d] = std::max(C.hi[d] - C.lo[d], 1e-3 * emax);
+    lo[d] = C.c[d] - 0.5 * ext[d];
+  }
+}
+
+struct TcLayout {
+  int order = 0, np = 0, npts = 0, per_point = 1, proxy_slots = 0;  // proxy_slots: per cluster, even
+  double theta = 0;
+  std::vector<TcNode> src, trg;
+  std::vector<int64_t> sperm, tperm;
+  std::vector<int64_t> slot_src;  // source slot -> source index, -1 = padding
+  int64_t n_src_slots = 0, n_slots = 0;
+  std::vector<int32_t> clusters;  // approximated clusters (node ids) in proxy order
+  std::vector<sctlgpu_block> blocks;
+  int64_t pp = 0, pc = 0;         // interactions (target x slot) of the direct and proxy blocks
+  double xcheb[TC_MAX_NP], wcheb[TC_MAX_NP];
+};
+
+// Default (order, theta) per digits: Chebyshev interpolation of K(x, .) on a box
+// seen from distance >= r / theta converges like rho^-order with
+// rho = s + sqrt(s^2 - 1), s ~ sqrt(3) / theta per dimension.
+void tc_defaults(int digits, int* order, double* theta) {
+  static const int ord[16] = {3, 3, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 15};
+  static const double th[16] = {0.7, 0.7, 0.7, 0.7, 0.65, 0.6, 0.6, 0.55, 0.55, 0.5, 0.5, 0.5, 0.45, 0.45, 0.4, 0.4};
+  const int d = std::min(15, std::max(0, digits < 0 ? 15 : digits));
+  if (*order <= 0) *order = ord[d];
+  if (*theta <= 0) *theta = th[d];
+}
+
+int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, const double* r_trg, int order,
+                    double theta, int64_t leaf_max, int64_t batch_max, TcLayout& L) {
+  if (order < 1 || order >= TC_MAX_NP || !(theta > 0) || theta >= 1.0) return SCTLGPU_ERR_INVALID_ARGUMENT;
+  L.order = order;
+  L.np = order + 1;
+  L.npts = L.np * L.np * L.np;
+  L.per_point = kernel == SCTLGPU_STOKES3D_DXU ? 3 : 1;
+  L.proxy_slots = (L.npts * L.per_point + 1) / 2 * 2;
+  L.theta = theta;
+  if (leaf_max <= 0) leaf_max = std::max<int64_t>(64, (3 * (int64_t)L.npts * L.per_point) / 2);
+  if (batch_max <= 0) batch_max = 512;
+  for (int m = 0; m <= order; ++m) {  // Chebyshev points of the second kind and their barycentric weights
+    L.xcheb[m] = std::cos(M_PI * m / order);
+    L.wcheb[m] = (m % 2 ? -1.0 : 1.0) * ((m == 0 || m == order) ? 0.5 : 1.0);
+  }
+  build_octree(r_src, ns, leaf_max, L.sperm, L.src);
+  build_octree(r_trg, nt, batch_max, L.tperm, L.trg);
+  // source slots: leaves in permutation order, each padded to an even count
+  std::vector<int32_t> leaves;
+  for (int32_t i = 0; i < (int32_t)L.src.size(); ++i)
+    if (L.src[i].nchild == 0 && L.src[i].e > L.src[i].b) leaves.push_back(i);
+  std::sort(leaves.begin(), leaves.end(), [&](int32_t a, int32_t b) { return L.src[a].b < L.src[b].b; });
+  int64_t cur = 0;
+  L.slot_src.clear();
+  for (int32_t id : leaves) {
+    TcNode& nd = L.src[id];
+    nd.sb = cur;
+    for (int64_t i = nd.b; i < nd.e; ++i) L.slot_src.push_back(L.sperm[i]);
+    if ((nd.e - nd.b) % 2) L.slot_src.push_back(-1);
+    cur = (int64_t)L.slot_src.size();
+    nd.se = cur;
+  }
+  for (int32_t i = (int32_t)L.src.size() - 1; i >= 0; --i) {  // children come after their parent
+    TcNode& nd = L.src[i];
+    if (nd.nchild) {
+      nd.sb = L.src[nd.child0].sb;
+      nd.se = L.src[nd.child0 + nd.nchild - 1].se;
+    }
+  }
+  L.n_src_slots = cur;
+  // traversal: per batch the approximated clusters and the directly summed leaves
+  std::vector<int32_t> batches;
+  for (int32_t i = 0; i < (int32_t)L.trg.size(); ++i)
+    if (L.trg[i].nchild == 0 && L.trg[i].e > L.trg[i].b) batches.push_back(i);
+  std::sort(batches.begin(), batches.end(), [&](int32_t a, int32_t b) { return L.trg[a].b < L.trg[b].b; });
+  std::vector<std::vector<int32_t>> pcl(batches.size()), ppl(batches.size());
+  std::vector<char> used(L.src.size(), 0);
+  std::vector<int32_t> stack;
+  for (size_t bi = 0; bi < batches.size() && ns > 0; ++bi) {
+    const TcNode& B = L.trg[batches[bi]];
+    stack.assign(1, 0);
+    while (!stack.empty()) {
+      const int32_t id = stack.back();
+      stack.pop_back();
+      const TcNode& C = L.src[id];
+      if (C.e == C.b) continue;
+      const double dx = B.c[0] - C.c[0], dy = B.c[1] - C.c[1], dz = B.c[2] - C.c[2];
+      const double dist = std::sqrt(dx * dx + dy * dy + dz * dz);
+      if (B.r + C.r < theta * dist && C.e - C.b > (int64_t)L.npts * L.per_point) {
+        pcl[bi].push_back(id);
+        used[id] = 1;
+      } else if (C.nchild == 0) {
+        ppl[bi].push_back(id);
+      } else {
+        for (int k = C.nchild - 1; k >= 0; --k) stack.push_back(C.child0 + k);
+      }
+    }
+  }
+  // proxies of the approximated clusters, in node order (siblings adjacent)
+  L.clusters.clear();
+  int64_t pcur = L.n_src_slots;
+  for (int32_t i = 0; i < (int32_t)L.src.size(); ++i)
+    if (used[i]) {
+      L.src[i].proxy = pcur;
+      pcur += L.proxy_slots;
+      L.clusters.push_back(i);
+    }
+  L.n_slots = pcur;
+  // blocks: contiguous slot ranges merged per batch
+  L.blocks.clear();
+  L.pp = L.pc = 0;
+  for (size_t bi = 0; bi < batches.size(); ++bi) {
+    const TcNode& B = L.trg[batches[bi]];
+    const int64_t t0 = B.b, tn = B.e - B.b;
+    auto emit = [&](std::vector<std::pair<int64_t, int64_t>>& r, int64_t& count) {
+      std::sort(r.begin(), r.end());
+      size_t k = 0;
+      while (k < r.size()) {
+        int64_t s0 = r[k].first, s1 = r[k].second;
+        size_t j = k + 1;
+        while (j < r.size() && r[j].first == s1) s1 = r[j++].second;
+        L.blocks.push_back({s0, s1 - s0, t0, tn});
+        count += (s1 - s0) * tn;
+        k = j;
+      }
+    };
+    std::vector<std::pair<int64_t, int64_t>> r;
+    for (int32_t id : ppl[bi]) r.push_back({L.src[id].sb, L.src[id].se});
+    emit(r, L.pp);
+    r.clear();
+    for (int32_t id : pcl[bi]) r.push_back({L.src[id].proxy, L.src[id].proxy + L.proxy_slots});
+    emit(r, L.pc);
+  }
+  return SCTLGPU_OK;
+}
+
+// ------------------------------------------------------------------ device
+
+struct TcCluster {
+  double lo[3], inv[3];  // interpolation box: t = (y - lo) * inv - 1 in [-1, 1]
+  int64_t proxy;         // first proxy slot
+  int32_t item0, item1;  // moment work items [item0, item1)
+};
+struct TcItem {
+  int32_t cluster;
+  int32_t n;   // slots of the chunk
+  int64_t s0;  // first slot
+};
+struct TcMomParams {
+  const TcCluster* clusters;
+  const TcItem* items;
+  const double* r;  // slot coordinates
+  const double* n;  // slot normals (double-layer kernels)
+  const double* v;  // slot densities
+  double* part;     // per item: npts x Q partial moments
+  double* pn;       // proxy normals (Laplace double layer)
+  double* pv;       // proxy densities
+  int np;
+  double x[TC_MAX_NP], w[TC_MAX_NP];
+};
+
+template <int KER>
+struct TcCharge;
+template <>
+struct TcCharge<SCTLGPU_LAPLACE3D_FXU> {
+  static constexpr int Q = 1;
+};
+template <>
+struct TcCharge<SCTLGPU_LAPLACE3D_DXU> {
+  static constexpr int Q = 3;
+};
+template <>
+struct TcCharge<SCTLGPU_STOKES3D_FXU> {
+  static constexpr int Q = 3;
+};
+template <>
+struct TcCharge<SCTLGPU_STOKES3D_DXU> {
+  static constexpr int Q = 9;
+};
+
+__global__ void tc_gather_kernel(int64_t n_slots, int sd, const int64_t* slot_src, const double* v_src, double* v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_slots * sd;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = slot_src[i / sd];
+    v[i] = s >= 0 ? v_src[s * sd + i % sd] : 0.0;
+  }
+}
+
+// Barycentric Lagrange basis at t (second-kind Chebyshev points x, weights w).
+__device__ __forceinline__ void tc_lagrange(double t, int np, const double* x, const double* w, double* L) {
+  int hit = -1;
+  double sum = 0;
+  for (int m = 0; m < np; ++m) {
+    const double d = t - x[m];
+    if (d == 0.0) hit = m;
+    const double q = d != 0.0 ? w[m] / d : 0.0;
+    L[m] = q;
+    sum += q;
+  }
+  if (hit >= 0) {
+    for (int m = 0; m < np; ++m) L[m] = m == hit ? 1.0 : 0.0;
+  } else {
+    const double inv = 1.0 / sum;
+    for (int m = 0; m < np; ++m) L[m] *= inv;
+  }
+}
+
+// Partial moments of one chunk: M_k = sum_s L_k(y_s) q_s over <= 256 slots.
+template <int KER>
+__global__ void __launch_bounds__(TC_THREADS) tc_moments_kernel(TcMomParams p) {
+  constexpr int Q = TcCharge<KER>::Q;
+  extern __shared__ double tc_sm[];
+  const int np = p.np, npts = np * np * np;
+  double* Ls = tc_sm;                          // [TC_CHUNK][3][np]
+  double* qs = tc_sm + TC_CHUNK * 3 * np;      // [TC_CHUNK][Q]
+  const TcItem it = p.items[blockIdx.x];
+  const TcCluster C = p.clusters[it.cluster];
+  for (int s = threadIdx.x; s < TC_CHUNK; s += blockDim.x) {
+    const bool valid = s < it.n;
+    const int64_t slot = it.s0 + s;
+    for (int d = 0; d < 3; ++d) {
+      double t = valid ? (p.r[slot * 3 + d] - C.lo[d]) * C.inv[d] - 1.0 : 0.0;
+      t = fmin(1.0, fmax(-1.0, t));
+      tc_lagrange(t, np, p.x, p.w, Ls + (s * 3 + d) * np);
+    }
+    double q[Q];
+    for (int c = 0; c < Q; ++c) q[c] = 0.0;
+    if (valid) {
+      if constexpr (KER == SCTLGPU_LAPLACE3D_FXU) {
+        q[0] = p.v[slot];
+      } else if constexpr (KER == SCTLGPU_LAPLACE3D_DXU) {
+        for (int c = 0; c < 3; ++c) q[c] = p.n[slot * 3 + c] * p.v[slot];
+      } else if constexpr (KER == SCTLGPU_STOKES3D_FXU) {
+        for (int c = 0; c < 3; ++c) q[c] = p.v[slot * 3 + c];
+      } else {  // normal (x) density
+        for (int c = 0; c < 3; ++c)
+          for (int d = 0; d < 3; ++d) q[c * 3 + d] = p.n[slot * 3 + c] * p.v[slot * 3 + d];
+      }
+    }
+    for (int c = 0; c < Q; ++c) qs[s * Q + c] = q[c];
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < npts; k += blockDim.x) {
+    const int i = k / (np * np), j = (k / np) % np, l = k % np;
+    double acc[Q];
+    for (int c = 0; c < Q; ++c) acc[c] = 0.0;
+    for (int s = 0; s < it.n; ++s) {
+      const double wgt = Ls[(s * 3) * np + i] * Ls[(s * 3 + 1) * np + j] * Ls[(s * 3 + 2) * np + l];
+#pragma unroll
+      for (int c = 0; c < Q; ++c) acc[c] = fma(wgt, qs[s * Q + c], acc[c]);
+    }
+    double* out = p.part + ((int64_t)blockIdx.x * npts + k) * Q;
+#pragma unroll
+    for (int c = 0; c < Q; ++c) out[c] = acc[c];
+  }
+}
+
+// Moments of every approximated cluster (its chunks in order) into the proxy slots.
+template <int KER>
+__global__ void tc_reduce_kernel(TcMomParams p, int n_clusters) {
+  constexpr int Q = TcCharge<KER>::Q;
+  const int npts = p.np * p.np * p.np;
+  const int c = blockIdx.y;
+  if (c >= n_clusters) return;
+  const TcCluster C = p.clusters[c];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < npts; k += gridDim.x * blockDim.x) {
+    double m[Q];
+    for (int q = 0; q < Q; ++q) m[q] = 0.0;
+    for (int it = C.item0; it < C.item1; ++it) {
+      const double* src = p.part + ((int64_t)it * npts + k) * Q;
+#pragma unroll
+      for (int q = 0; q < Q; ++q) m[q] += src[q];
+    }
+    if constexpr (KER == SCTLGPU_LAPLACE3D_FXU) {
+      p.pv[C.proxy + k] = m[0];
+    } else if constexpr (KER == SCTLGPU_LAPLACE3D_DXU) {
+      for (int q = 0; q < 3; ++q) p.pn[(C.proxy + k) * 3 + q] = m[q];
+    } else if constexpr (KER == SCTLGPU_STOKES3D_FXU) {
+      for (int q = 0; q < 3; ++q) p.pv[(C.proxy + k) * 3 + q] = m[q];
+    } else {  // proxy (k, c): normal e_c, density M_k[c][:]
+      for (int q = 0; q < Q; ++q) p.pv[(C.proxy + 3 * k + q / 3) * 3 + q % 3] = m[q];
+    }
+  }
+}
+
+template <int KER>
+cudaError_t tc_launch_moments(const TcMomParams& p, int n_items, int n_clusters, cudaStream_t st) {
+  constexpr int Q = TcCharge<KER>::Q;
+  if (n_items == 0) return cudaSuccess;
+  const size_t smem = (size_t)TC_CHUNK * (3 * p.np + Q) * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(tc_moments_kernel<KER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  tc_moments_kernel<KER><<<n_items, TC_THREADS, smem, st>>>(p);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  const int npts = p.np * p.np * p.np;
+  tc_reduce_kernel<KER><<<dim3((npts + 255) / 256, n_clusters), 256, 0, st>>>(p, n_clusters);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  return cudaGetLastError();
+}
+
+}  // namespace
+}  // namespace sctlgpu
+
+using namespace sctlgpu;
+
+struct sctlgpu_treecode_s {
+  int kernel = 0, mode = 0, digits = 0, ND = 0, SD = 0, TD = 0;
+  int device = 0;
+  TcLayout L;
+  int64_t ns = 0, nt = 0, n_items = 0;
+  double *d_trg = nullptr, *d_r = nullptr, *d_n = nullptr, *d_v = nullptr, *d_part = nullptr;
+  int64_t* d_slot_src = nullptr;
+  TcCluster* d_clusters = nullptr;
+  TcItem* d_items = nullptr;
+  sctlgpu_near_plan plan = nullptr;
+};
+
+namespace {
+
+void tc_free(sctlgpu_treecode_s* T) {
+  if (T->plan) sctlgpu_near_plan_destroy(T->plan);
+  cudaFree(T->d_trg);
+  cudaFree(T->d_r);
+  cudaFree(T->d_n);
+  cudaFree(T->d_v);
+  cudaFree(T->d_part);
+  cudaFree(T->d_slot_src);
+  cudaFree(T->d_clusters);
+  cudaFree(T->d_items);
+  delete T;
+}
+
+int tc_check_common(int kernel, int64_t ns, const double* r_src, int64_t nt, const double* r_trg) {
+  if (kernel < 0 || kernel > SCTLGPU_STOKES3D_DXU) return SCTLGPU_ERR_INVALID_KERNEL;
+  if (ns < 0 || nt < 0 || ns > (INT64_C(1) << 40) || nt > (INT64_C(1) << 40)) return SCTLGPU_ERR_INVALID_SIZE;
+  if ((ns && !r_src) || (nt && !r_trg)) return SCTLGPU_ERR_NULL_POINTER;
+  for (int64_t i = 0; i < 3 * ns; ++i)
+    if (!std::isfinite(r_src[i])) return SCTLGPU_ERR_INVALID_ARGUMENT;
+  for (int64_t i = 0; i < 3 * nt; ++i)
+    if (!std::isfinite(r_trg[i])) return SCTLGPU_ERR_INVALID_ARGUMENT;
+  return SCTLGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sctlgpu_treecode_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, const double* r_trg,
+                            const sctlgpu_treecode_params* prm, int digits, int64_t* sizes, double* theta_out,
+                            sctlgpu_block* blocks, int64_t* slot_src, int64_t* trg_order, int64_t* clusters) {
+  int rc = tc_check_common(kernel, ns, r_src, nt, r_trg);
+  if (rc) return rc;
+  if (!sizes) return SCTLGPU_ERR_NULL_POINTER;
+  int order = prm ? prm->order : 0;
+  double theta = prm ? prm->theta : 0.0;
+  tc_defaults(digits, &order, &theta);
+  TcLayout L;
+  rc = tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, prm ? prm->leaf_max : 0, prm ? prm->batch_max : 0,
+                       L);
+  if (rc) return rc;
+  sizes[0] = (int64_t)L.blocks.size();
+  sizes[1] = L.n_src_slots;
+  sizes[2] = L.n_slots;
+  sizes[3] = (int64_t)L.clusters.size();
+  sizes[4] = L.pp;
+  sizes[5] = L.pc;
+  sizes[6] = L.order;
+  if (theta_out) *theta_out = L.theta;
+  if (blocks) std::copy(L.blocks.begin(), L.blocks.end(), blocks);
+  if (slot_src) {
+    std::copy(L.slot_src.begin(), L.slot_src.end(), slot_src);
+    for (int64_t i = L.n_src_slots; i < L.n_slots; ++i) slot_src[i] = -2;  // proxy slots
+  }
+  if (trg_order) std::copy(L.tperm.begin(), L.tperm.end(), trg_order);
+  if (clusters)
+    for (size_t k = 0; k < L.clusters.size(); ++k) {
+      const TcNode& C = L.src[L.clusters[k]];
+      clusters[4 * k + 0] = C.sb;
+      clusters[4 * k + 1] = C.se;
+      clusters[4 * k + 2] = C.proxy;
+      clusters[4 * k + 3] = C.proxy + L.proxy_slots;
+    }
+  return SCTLGPU_OK;
+}
+
+int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int digits, int64_t ns, const double* r_src,
+                            const double* n_src, int64_t nt, const double* r_trg, const sctlgpu_treecode_params* prm) {
+  if (!out) return SCTLGPU_ERR_NULL_POINTER;
+  *out = nullptr;
+  int rc = tc_check_common(kernel, ns, r_src, nt, r_trg);
+  if (rc) return rc;
+  if (mode != SCTLGPU_F64 && mode != SCTLGPU_MIXED) return SCTLGPU_ERR_INVALID_MODE;  // FP64 results, scattered
+  int nd, sd, td;
+  if (sctlgpu_kernel_dims(kernel, nullptr, &nd, &sd, &td) != SCTLGPU_OK) return SCTLGPU_ERR_INVALID_KERNEL;
+  if (nd && ns && !n_src) return SCTLGPU_ERR_NULL_POINTER;
+  int dev;
+  unsigned* status;
+  int sms;
+  if ((rc = runtime_device(&dev, &status, &sms))) return rc;
+  auto* T = new sctlgpu_treecode_s();
+  T->kernel = kernel;
+  T->mode = mode;
+  T->digits = digits;
+  T->ND = nd;
+  T->SD = sd;
+  T->TD = td;
+  T->device = dev;
+  T->ns = ns;
+  T->nt = nt;
+  int order = prm ? prm->order : 0;
+  double theta = prm ? prm->theta : 0.0;
+  tc_defaults(digits, &order, &theta);
+  TcLayout& L = T->L;
+  rc = tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, prm ? prm->leaf_max : 0, prm ? prm->batch_max : 0,
+                       L);
+  if (rc) {
+    delete T;
+    return rc;
+  }
+  // slot arrays: sources (sorted, padded), then proxies
+  const int64_t S = L.n_slots;
+  std::vector<double> hr((size_t)S * 3, 0.0), hn(nd ? (size_t)S * 3 : 0, 0.0), hv((size_t)S * sd, 0.0);
+  for (int64_t i = 0; i < L.n_src_slots; ++i) {
+    int64_t s = L.slot_src[i];
+    const bool pad = s < 0;
+    if (pad) s = L.slot_src[i - 1];  // padding sits on its leaf's last source, with zero charge
+    for (int d = 0; d < 3; ++d) hr[i * 3 + d] = r_src[s * 3 + d];
+    if (nd && !pad)
+      for (int d = 0; d < 3; ++d) hn[i * 3 + d] = n_src[s * 3 + d];
+  }
+  std::vector<TcCluster> hc;
+  std::vector<TcItem> hi;
+  for (int32_t id : L.clusters) {
+    const TcNode& C = L.src[id];
+    TcCluster tc{};
+    double ext[3];
+    interp_box(C, tc.lo, ext);
+    for (int d = 0; d < 3; ++d) tc.inv[d] = 2.0 / ext[d];
+    tc.proxy = C.proxy;
+    tc.item0 = (int32_t)hi.size();
+    for (int64_t s0 = C.sb; s0 < C.se; s0 += TC_CHUNK)
+      hi.push_back({(int32_t)hc.size(), (int32_t)std::min<int64_t>(TC_CHUNK, C.se - s0), s0});
+    tc.item1 = (int32_t)hi.size();
+    for (int k = 0; k < L.proxy_slots; ++k) {
+      const int pt = std::min(k / L.per_point, L.npts - 1);  // the padding slot repeats the last point
+      const int i = pt / (L.np * L.np), j = (pt / L.np) % L.np, l = pt % L.np;
+      const int64_t slot = C.proxy + k;
+      const double g[3] = {L.xcheb[i], L.xcheb[j], L.xcheb[l]};
+      for (int d = 0; d < 3; ++d) hr[slot * 3 + d] = tc.lo[d] + 0.5 * (g[d] + 1.0) * ext[d];
+      const bool real = k < L.npts * L.per_point;
+      if (kernel == SCTLGPU_LAPLACE3D_DXU && real) hv[slot] = 1.0;  // the moment is the proxy's normal
+      if (kernel == SCTLGPU_STOKES3D_DXU && real) hn[slot * 3 + k % 3] = 1.0;  // normal e_c
+    }
+    hc.push_back(tc);
+  }
+  T->n_items = (int64_t)hi.size();
+  const int64_t npts = L.npts, Q = kernel == SCTLGPU_STOKES3D_DXU ? 9 : (kernel == SCTLGPU_LAPLACE3D_FXU ? 1 : 3);
+  std::vector<double> htrg((size_t)nt * 3);
+  for (int64_t k = 0; k < nt; ++k)
+    for (int d = 0; d < 3; ++d) htrg[k * 3 + d] = r_trg[L.tperm[k] * 3 + d];
+  cudaError_t e = cudaSuccess;
+  auto up = [&](void** dst, const void* src, size_t bytes) {
+    if (e != cudaSuccess) return;
+    e = cudaMalloc(dst, std::max<size_t>(bytes, 16));
+    if (e == cudaSuccess && bytes) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+  };
+  up((void**)&T->d_trg, htrg.data(), htrg.size() * sizeof(double));
+  up((void**)&T->d_r, hr.data(), hr.size() * sizeof(double));
+  if (nd) up((void**)&T->d_n, hn.data(), hn.size() * sizeof(double));
+  up((void**)&T->d_v, hv.data(), hv.size() * sizeof(double));
+  up((void**)&T->d_slot_src, L.slot_src.data(), L.slot_src.size() * sizeof(int64_t));
+  up((void**)&T->d_clusters, hc.data(), hc.size() * sizeof(TcCluster));
+  up((void**)&T->d_items, hi.data(), hi.size() * sizeof(TcItem));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&T->d_part, std::max<size_t>(16, (size_t)T->n_items * npts * Q * sizeof(double)));
+  if (e != cudaSuccess) {
+    tc_free(T);
+    return runtime_record(e);
+  }
+  std::vector<int64_t> tmap(L.tperm.begin(), L.tperm.end());
+  rc = sctlgpu_near_plan_create(&T->plan, kernel, mode, digits, (int64_t)L.blocks.size(), L.blocks.data(), S, nt,
+                                nt ? tmap.data() : nullptr, nt);
+  if (rc) {
+    T->plan = nullptr;
+    tc_free(T);
+    return rc;
+  }
+  *out = T;
+  return SCTLGPU_OK;
+}
+
+int sctlgpu_treecode_execute(sctlgpu_treecode T, const double* v_src, double* v_out, unsigned flags, void* stream) {
+  if (!T) return SCTLGPU_ERR_NULL_POINTER;
+  if (flags & ~(unsigned)(SCTLGPU_ACCUMULATE | SCTLGPU_DEVICE_PTRS)) return SCTLGPU_ERR_INVALID_ARGUMENT;
+  if ((T->ns && !v_src) || (T->nt && !v_out)) return SCTLGPU_ERR_NULL_POINTER;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev != T->device) return SCTLGPU_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  const TcLayout& L = T->L;
+  cudaError_t e = cudaSuccess;
+  if (L.n_src_slots) {
+    const int64_t work = L.n_src_slots * T->SD;
+    tc_gather_kernel<<<(unsigned)std::min<int64_t>((work + 255) / 256, 152 * 16), 256, 0, st>>>(
+        L.n_src_slots, T->SD, T->d_slot_src, v_src, T->d_v);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    if ((e = cudaGetLastError()) != cudaSuccess) return runtime_record(e);
+  }
+  TcMomParams p{};
+  p.clusters = T->d_clusters;
+  p.items = T->d_items;
+  p.r = T->d_r;
+  p.n = T->d_n;
+  p.v = T->d_v;
+  p.part = T->d_part;
+  p.pn = T->d_n;
+  p.pv = T->d_v;
+  p.np = L.np;
+  for (int m = 0; m < L.np; ++m) {
+    p.x[m] = L.xcheb[m];
+    p.w[m] = L.wcheb[m];
+  }
+  const int nc = (int)L.clusters.size(), ni = (int)T->n_items;
+  switch (T->kernel) {
+    case SCTLGPU_LAPLACE3D_FXU: e = tc_launch_moments<SCTLGPU_LAPLACE3D_FXU>(p, ni, nc, st); break;
+    case SCTLGPU_LAPLACE3D_DXU: e = tc_launch_moments<SCTLGPU_LAPLACE3D_DXU>(p, ni, nc, st); break;
+    case SCTLGPU_STOKES3D_FXU: e = tc_launch_moments<SCTLGPU_STOKES3D_FXU>(p, ni, nc, st); break;
+    default: e = tc_launch_moments<SCTLGPU_STOKES3D_DXU>(p, ni, nc, st); break;
+  }
+  if (e != cudaSuccess) return runtime_record(e);
+  return sctlgpu_near_plan_execute(T->plan, T->d_trg, T->d_r, T->d_n, T->d_v, nullptr, v_out,
+                                   (flags & SCTLGPU_ACCUMULATE) | SCTLGPU_DEVICE_PTRS, stream);
+}
+
+int sctlgpu_treecode_info(sctlgpu_treecode T, int64_t* stats, double* theta) {
+  if (!T || !stats) return SCTLGPU_ERR_NULL_POINTER;
+  const TcLayout& L = T->L;
+  stats[0] = (int64_t)L.blocks.size();
+  stats[1] = L.n_src_slots;
+  stats[2] = L.n_slots;
+  stats[3] = (int64_t)L.clusters.size();
+  stats[4] = L.pp;
+  stats[5] = L.pc;
+  stats[6] = L.order;
+  if (theta) *theta = L.theta;
+  return SCTLGPU_OK;
+}
+
+int sctlgpu_treecode_status(sctlgpu_treecode T, void* stream) {
+  if (!T) return SCTLGPU_ERR_NULL_POINTER;
+  return sctlgpu_near_plan_status(T->plan, stream);
+}
+
+int sctlgpu_treecode_destroy(sctlgpu_treecode T) {
+  if (!T) return SCTLGPU_OK;
+  cudaDeviceSynchronize();
+  tc_free(T);
+  return SCTLGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,114 @@
+"""The GPU treecode (sctlgpu_treecode_*, the fast path of ParticleFMM::Eval) against the direct
+sum: the FP64 oracle (the reference's Eval restated, pinned to the reference's own outputs) on
+a target sample, and the GPU direct sum on whole target sets.
+
+Tolerance: relative l2 of the potentials within 10^-digits (the accuracy `digits` asks of
+ParticleFMM, SetAccuracy fmm-wrapper.txx:270-281) for digits 6 and 10, on the sphere/ball
+workload, clustered sources and the torus far field; plus the accumulate flag, an all-direct
+tree (one leaf) that must agree with the direct sum to rounding, and repeated evaluations
+with new densities.
+"""
+import numpy as np
+import pytest
+
+import sctl_gb300 as S
+from oracle import oracle as O
+from sctl_gb300 import capi, workloads as W
+from sctl_gb300 import treecode as TC
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a, np.float64).reshape(-1)).cuda()
+
+
+def nrm(k, d):
+    return d["n_src"] if k in (1, 3) else None
+
+
+@pytest.mark.parametrize("k", [0, 1, 2, 3])
+@pytest.mark.parametrize("digits", [6, 10])
+def test_treecode_vs_oracle_sphere_ball(cuda, k, digits):
+    torch = cuda
+    nt = 1 << 16
+    d = W.sphere_ball(1 << 18, nt, k, seed=40 + k)
+    tc = TC.Treecode(k, d["r_src"], d["r_trg"], n_src=nrm(k, d), digits=digits)
+    info = tc.info()
+    assert info["proxy_interactions"] > 0
+    u = tc.eval(dev(torch, d["v_src"])).cpu().numpy()
+    assert tc.status() == capi.OK
+    sub = np.arange(0, nt, 128)
+    ref = O.eval(k, d["r_trg"][sub], d["r_src"], d["n_src"], d["v_src"])
+    got = u.reshape(nt, -1)[sub].reshape(-1)
+    err = O.rel_l2(got, ref)
+    saved = 1 - (info["direct_interactions"] + info["proxy_interactions"]) / info["direct_sum_interactions"]
+    print(f"k{k} digits {digits}: rel_l2 {err:.2e}, order {info['order']} theta {info['theta']}, "
+          f"interactions saved {saved:.2f}")
+    assert err < 10.0 ** -digits
+
+
+@pytest.mark.parametrize("digits", [6, 10])
+def test_treecode_clusters_f64_and_mixed(cuda, digits):
+    torch = cuda
+    k = 1
+    d = W.clusters(1 << 17, 1 << 14, k, seed=3, n_clusters=16, sigma=3e-2)
+    ref = None
+    for mode in ("f64", "mixed"):
+        tc = TC.Treecode(k, d["r_src"], d["r_trg"], n_src=d["n_src"], digits=digits, mode=mode)
+        assert tc.info()["proxy_interactions"] > 0
+        u = tc.eval(dev(torch, d["v_src"])).cpu().numpy()
+        sub = np.arange(0, 1 << 14, 64)
+        if ref is None:
+            ref = O.eval(k, d["r_trg"][sub], d["r_src"], d["n_src"], d["v_src"])
+        assert O.rel_l2(u[sub], ref) < 10.0 ** -digits, mode
+
+
+def test_treecode_accumulate_and_new_densities(cuda):
+    torch = cuda
+    k = 2
+    d = W.sphere_ball(1 << 16, 1 << 13, k, seed=9)
+    tc = TC.Treecode(k, d["r_src"], d["r_trg"], digits=8)
+    v1 = dev(torch, d["v_src"])
+    v2 = dev(torch, np.random.default_rng(1).standard_normal(d["v_src"].size))
+    u1 = tc.eval(v1).clone()
+    u2 = tc.eval(v2).clone()
+    out = u1.clone()
+    tc.eval(v2, out=out, accumulate=True)
+    assert torch.allclose(out, u1 + u2, rtol=0, atol=1e-13 * float(out.abs().max()))
+    # linearity of the whole pipeline (moments, proxies, direct blocks)
+    u3 = tc.eval(2.0 * v1 - v2)
+    assert float((u3 - (2 * u1 - u2)).norm() / u3.norm()) < 1e-12
+
+
+def test_treecode_single_leaf_is_the_direct_sum(cuda):
+    """One leaf, FP64 arithmetic: the treecode is the direct sum up to summation order."""
+    torch = cuda
+    k = 3
+    d = W.sphere_ball(3001, 1531, k, seed=7)
+    tc = TC.Treecode(k, d["r_src"], d["r_trg"], n_src=d["n_src"], digits=-1, mode="f64", leaf_max=4096)
+    assert tc.info()["proxy_interactions"] == 0
+    u = tc.eval(dev(torch, d["v_src"])).cpu().numpy()
+    ref = O.eval(k, d["r_trg"], d["r_src"], d["n_src"], d["v_src"])
+    assert O.rel_l2(u, ref) < 1e-14
+
+
+def test_treecode_torus_far_field(cuda):
+    """C5's far field (204,800 panel nodes, densities sigma * Q) at 65,536 near-surface targets,
+    Laplace double layer, digits 10: against the GPU direct sum (mixed, digits 10)."""
+    torch = cuda
+    from sctl_gb300.torus import Torus
+    T = Torus(seed=0)
+    X, N, Q, sig = T.nodes()
+    xt = T.targets(1 << 16, seed=7)["r_trg"]
+    f = sig * Q
+    ref = S.Laplace3D_DxU.Eval(None, xt, X, N, f, digits=10, mode="mixed")
+    for digits in (6, 10):
+        tc = TC.Treecode(1, X, xt, n_src=N, digits=digits)
+        u = tc.eval(dev(torch, f)).cpu().numpy()
+        err = O.rel_l2(u, ref)
+        info = tc.info()
+        print(f"torus digits {digits}: rel_l2 {err:.2e}, interactions "
+              f"{(info['direct_interactions'] + info['proxy_interactions']) / info['direct_sum_interactions']:.3f}"
+              " of the direct sum")
+        assert err < 10.0 ** -digits
