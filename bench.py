@@ -817,6 +817,7 @@ def main():
         extras["tensor_core_mlp"] = mlp_section(torch, stream)
         extras["other_micro_kernels"] = ext_section(torch, stream)
         extras["kernel_matrix"] = kmat_section(torch, stream)
+        extras["far_field_treecode"] = treecode_section(torch)
         if not args.skip_torus:
             extras["torus_near_singular"] = torus_section(torch)
 

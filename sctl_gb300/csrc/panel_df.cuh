@@ -146,7 +146,6 @@ struct PanelWarpSmemDF {
   f2 Ls[PQ_GL][PQ_P], Lds[PQ_GL][PQ_P], Lt[PQ_GL][PQ_P], Ldt[PQ_GL][PQ_P];
   f2 A[7][PQ_GL][PQ_P];
   float box[2][PQ_QUEUE][2];  // (s0, t0) of the boxes of this and the next round (dyadic: exact)
-  float leaf[PQ_QUEUE][2];
 };
 struct PanelWarpSmemDFW : PanelWarpSmemDF {
   f2 Kd[PQ_GL][PQ_GL];
@@ -162,7 +161,6 @@ struct PanelWarpSmemDFP {
   f2 Lt[PQ_GL][PQ_P], Ldt[PQ_GL][PQ_P];
   pdfq::d2 AP[7][PQ_GL / 2][PQ_P];
   float box[2][PQ_QUEUE][2];
-  float leaf[PQ_QUEUE][2];
 };
 static_assert(sizeof(PanelWarpSmemDFP) == sizeof(PanelWarpSmemDF), "packed layout keeps the footprint");
 template <bool WEIGHTS>
@@ -350,7 +348,7 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
     }
     __syncwarp();
     pdfq::d2 acc = {};  // potential mode: the lane's two node sums
-    int cur = 0, ncur = 1, nleaf = 0;
+    int cur = 0, ncur = 1;
     if (lane == 0) {
       sm.box[0][0][0] = 0.0f;
       sm.box[0][0][1] = 0.0f;
@@ -358,12 +356,13 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
     __syncwarp();
     for (int depth = 0; depth <= p.max_depth && ncur > 0; ++depth) {
       int nnext = 0;
-      nleaf = 0;
       const float bz = ldexpf(1.0f, -depth);  // every box of this round has this size
-      // Integrates the queued leaves of this round and empties the leaf buffer.
-      auto integrate_leaves = [&]() {
-        for (int lf = 0; lf < nleaf; ++lf) {
-          const float bs = sm.leaf[lf][0], bt = sm.leaf[lf][1];
+      // Integrates the accepted boxes of one group of 32 (acc_mask over the lanes holding them),
+      // in lane order, as soon as the group is classified: no leaf queue in shared memory.
+      auto integrate_leaves = [&](unsigned acc_mask, float lbs, float lbt) {
+        for (unsigned mk = acc_mask; mk; mk &= mk - 1u) {
+          const int src = __ffs(mk) - 1;
+          const float bs = __shfl_sync(0xffffffffu, lbs, src), bt = __shfl_sync(0xffffffffu, lbt, src);
           if constexpr (!WEIGHTS) {
             leaf_potential_pk<KER>(sm, lane, bs, bt, bz, acc);
             __syncwarp();
@@ -461,15 +460,8 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
             __syncwarp();
           }
         }
-        nleaf = 0;
       };
       for (int base = 0; base < ncur; base += 32) {
-        // a batch adds at most 32 leaves: flush the leaves when they might not fit
-        if (nleaf + 32 > PQ_QUEUE) {
-          __syncwarp();
-          integrate_leaves();
-          __syncwarp();
-        }
         const int i = base + lane;
         bool accept = false, far = true, valid = i < ncur;
         float bs = 0, bt = 0;
@@ -488,13 +480,6 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
         const unsigned acc_mask = __ballot_sync(0xffffffffu, valid && accept);
         const unsigned ref_mask = __ballot_sync(0xffffffffu, valid && !accept);
         const unsigned lt_mask = (1u << lane) - 1u;
-        if (valid && accept) {
-          const int slot = nleaf + __popc(acc_mask & lt_mask);
-          if (slot < PQ_QUEUE) {
-            sm.leaf[slot][0] = bs;
-            sm.leaf[slot][1] = bt;
-          }
-        }
         if (valid && !accept) {
           const int slot = nnext + 4 * __popc(ref_mask & lt_mask);
           const float h = 0.5f * bz;
@@ -504,11 +489,11 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
               sm.box[cur ^ 1][slot + c][1] = bt + (c >> 1) * h;
             }
         }
-        nleaf += __popc(acc_mask);  // <= PQ_QUEUE by the flush above
         nnext += 4 * __popc(ref_mask);  // <= PQ_QUEUE by the room check
+        __syncwarp();
+        integrate_leaves(acc_mask, bs, bt);
       }
       __syncwarp();
-      integrate_leaves();
       cur ^= 1;
       ncur = nnext;
     }
