@@ -70,10 +70,12 @@ class PanelSurface:
     near_pairs_grid = near_pairs
 
     # ------------------------------------------------------------ far field
-    def far_field(self, r_trg, sigma, kernel=1, mode="mixed", digits=10, out=None):
+    def far_field(self, r_trg, sigma, kernel=1, mode="mixed", digits=10, out=None, method="direct"):
         """ComputeFarField (boundary_integral.txx:1248-1309): F_far = sigma * Q on the device
-        (`sctlgpu_far_densities`), then one direct sum over every node; added into `out` when it
-        is given, else written to a new array."""
+        (`sctlgpu_far_densities`), then the sum over every node -- one direct sum
+        (method="direct", ParticleFMM::EvalDirect) or the treecode (method="treecode", the fast
+        path ParticleFMM::Eval takes for 40,000 targets or more; its trees are kept per target
+        array); added into `out` when it is given, else written to a new array."""
         xt = r_trg.reshape(-1)
         nt = xt.numel() // 3
         src = self.X.reshape(-1)
@@ -84,13 +86,32 @@ class PanelSurface:
         f = torch.empty_like(sig)
         capi.check(lib.sctlgpu_far_densities(self.np * self.nn, sig.numel() // (self.np * self.nn), sig.data_ptr(),
                                              self.Q.data_ptr(), f.data_ptr(), stream), "far densities")
-        flags = capi.DEVICE_PTRS | (capi.ACCUMULATE if out is not None else 0)
+        accumulate = out is not None
         if out is None:
-            out = torch.empty(nt, dtype=torch.float64, device=xt.device)
+            out = torch.empty(nt * (3 if kernel >= 2 else 1), dtype=torch.float64, device=xt.device)
+        if method == "treecode":
+            return self.treecode(xt, kernel, mode, digits).eval(f, out=out, accumulate=accumulate)
+        if method != "direct":
+            raise ValueError(f"unknown far-field method {method!r}")
+        flags = capi.DEVICE_PTRS | (capi.ACCUMULATE if accumulate else 0)
         capi.check(lib.sctlgpu_eval(kernel, capi.MODE_IDS[mode], digits, nt, xt.data_ptr(), src.numel() // 3,
                                     src.data_ptr(), nrm.data_ptr() if kernel in (1, 3) else None,
                                     f.data_ptr(), out.data_ptr(), flags, stream), "far field")
         return out
+
+    def treecode(self, r_trg, kernel=1, mode="mixed", digits=10):
+        """The far-field treecode of these nodes and targets (built on first use; the geometry
+        calls of ParticleFMM, SetSrcCoord / SetTrgCoord, fmm-wrapper.txx:505-540)."""
+        from .treecode import Treecode
+        xt = r_trg.reshape(-1)
+        # the cached trees hold a reference to their target array (its storage cannot be reused
+        # while cached) and are rebuilt when the array is written in place (its version changes)
+        key = (xt.data_ptr(), xt.numel(), xt._version, kernel, mode, digits)
+        if getattr(self, "_tc_key", None) != key:
+            self._tc = Treecode(kernel, self.X.reshape(-1), xt, n_src=self.N.reshape(-1) if kernel in (1, 3) else None,
+                                digits=digits, mode=mode)
+            self._tc_key, self._tc_trg = key, xt
+        return self._tc
 
     # ------------------------------------------------------------ near field
     def near_correction(self, r_trg, sigma, pairs, kernel=1, alpha=1.0, max_depth=22, out=None,
@@ -127,14 +148,15 @@ class PanelSurface:
         return NearMatrix(self, r_trg, pairs, kernel, alpha, max_depth, float_pairs)
 
     def evaluate(self, r_trg, sigma, kernel=1, mode="mixed", digits=10, near_factor=1.5, alpha=1.0, pairs=None,
-                 plan=None, matrix=None):
+                 plan=None, matrix=None, far="direct"):
         """Far field (smooth rule over every node) + near corrections.  The smooth part of the near
         panels is subtracted with a near plan in the far field's arithmetic, so the large
         near-singular smooth terms cancel exactly as in the reference's FP64 flow.  With `matrix`
         (a NearMatrix of the same pairs) the accurate near part is applied from the stored
-        weights instead of being integrated again."""
+        weights instead of being integrated again.  `far` selects the far-field summation
+        ("direct" or "treecode")."""
         xt = r_trg.reshape(-1).contiguous()
-        out = self.far_field(xt, sigma, kernel, mode, digits)
+        out = self.far_field(xt, sigma, kernel, mode, digits, method=far)
         if pairs is None:
             pairs = self.near_pairs(xt, near_factor)
         if plan is None:

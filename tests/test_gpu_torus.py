@@ -34,6 +34,24 @@ def test_gauss_law_double_layer(setup):
     assert capi.load().sctlgpu_device_status(None) == capi.OK  # no queue overflow / bad index
 
 
+def test_gauss_law_with_treecode_far_field(setup):
+    """The whole evaluation with the far field by the treecode (ParticleFMM::Eval's fast path):
+    Gauss's law as above at 65,536 targets, and within 1e-9 of the direct-far-field evaluation."""
+    torch, T, S = setup
+    tg = T.targets(1 << 16, seed=15, hmin=1e-4, hmax=1.0)
+    xt = torch.from_numpy(tg["r_trg"]).cuda()
+    one = torch.ones(T.np * T.p * T.p, dtype=torch.float64, device="cuda")
+    pairs = S.near_pairs(xt)
+    v = S.evaluate(xt, one, pairs=pairs, far="treecode").cpu().numpy()
+    assert S.treecode(xt).info()["proxy_interactions"] > 0
+    exact = np.where(tg["side"] < 0, -1.0, 0.0)
+    assert np.abs(v - exact).max() < 1e-8
+    sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()
+    a = S.evaluate(xt, sig, pairs=pairs, far="treecode").cpu().numpy()
+    b = S.evaluate(xt, sig, pairs=pairs).cpu().numpy()
+    assert np.abs(a - b).max() < 1e-9 * max(1.0, np.abs(b).max())
+
+
 def test_smooth_rule_alone_is_wrong_near_and_right_far(setup):
     torch, T, S = setup
     far = T.targets(500, seed=12, hmin=2.0, hmax=3.0)
