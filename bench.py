@@ -621,6 +621,7 @@ def main():
                                           "ext", "kmat", "ref_full", "learning_curve", "treecode"],
                     help="run only this secondary workload and print its JSON (profiling of one kernel family)")
     ap.add_argument("--torus-n", type=int, default=1 << 20, help="targets of the torus section")
+    ap.add_argument("--tc-n", type=int, default=1 << 20, help="targets (and sphere sources) of the treecode section")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -641,7 +642,7 @@ def main():
               "torus": lambda: torus_section(torch, n_eval=args.torus_n),
               "torus_plain": lambda: torus_section(torch, n_eval=args.torus_n, learned=False),
               "learning_curve": lambda: learning_curve_section(torch),
-              "treecode": lambda: treecode_section(torch)}[args.section]
+              "treecode": lambda: treecode_section(torch, n=args.tc_n)}[args.section]
         print(json.dumps({"section": args.section, **fn()}), flush=True)
         return
 

@@ -24,10 +24,12 @@
 //    normal (Laplace double layer: the moment is the proxy's normal), or
 //    normal (x) density (Stokes double layer: three proxies per point with
 //    unit normals e_c and densities M_k[c][:]).
-//  * device, per evaluation: densities gathered into slot order, moments in
-//    FP64 per (cluster, 256-slot chunk), reduced per cluster in chunk order
-//    (deterministic), then one execution of the near-field plan over the
-//    (batch, leaf range) and (batch, proxy range) blocks.
+//  * device, per evaluation: densities gathered into slot order, moments per
+//    (cluster, 256-slot chunk) -- in double-float on the FP32 pipe when the
+//    plan's arithmetic is FP32 or double-float, else in FP64 -- reduced per
+//    cluster in chunk order (deterministic), then one execution of the
+//    near-field plan over the (batch, leaf range) and (batch, proxy range)
+//    blocks.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -38,6 +40,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/sctlgpu.h"
+#include "common.cuh"
 #include "launch.h"
 
 namespace sctlgpu {
@@ -285,6 +288,7 @@ struct TcMomParams {
   double* pv;       // proxy densities
   int np;
   double x[TC_MAX_NP], w[TC_MAX_NP];
+  float xh[TC_MAX_NP], xl[TC_MAX_NP], wf[TC_MAX_NP];  // the points as double-float pairs; weights exact
 };
 
 template <int KER>
@@ -383,6 +387,87 @@ __global__ void __launch_bounds__(TC_THREADS) tc_moments_kernel(TcMomParams p) {
   }
 }
 
+// The same in double-float on the FP32 pipe (GB300's FP64 pipe is ~1/64 of it): for plans
+// whose arithmetic is FP32 or double-float, whose own per-interaction error is far above the
+// ~2^-44 of these moments.
+__device__ __forceinline__ f2 tc_rcp(f2 d) {  // 1 / d: FP32 estimate, one Newton step on the exact residual
+  const float y = 1.0f / d.h;
+  float t = fmaf(-d.h, y, 1.0f);
+  t = fmaf(-d.l, y, t);
+  return fast_two_sum(y, y * t);
+}
+__device__ __forceinline__ f2 tc_split(double v) {
+  const float h = (float)v;
+  return {h, (float)(v - (double)h)};
+}
+__device__ __forceinline__ void tc_lagrange_df(double tt, int np, const TcMomParams& p, f2* L) {
+  const f2 t = tc_split(tt);
+  int hit = -1;
+  f2 sum = {0.f, 0.f};
+  for (int m = 0; m < np; ++m) {
+    const f2 d = df_norm(df_add(t, {-p.xh[m], -p.xl[m]}));
+    if (d.h == 0.f) hit = m;
+    const f2 q = d.h != 0.f ? df_mulf(tc_rcp(d), p.wf[m]) : f2{0.f, 0.f};
+    L[m] = q;
+    df_acc(sum, q);
+  }
+  if (hit >= 0) {
+    for (int m = 0; m < np; ++m) L[m] = {m == hit ? 1.f : 0.f, 0.f};
+  } else {
+    const f2 inv = tc_rcp(df_norm(sum));
+    for (int m = 0; m < np; ++m) L[m] = df_norm(df_mul(L[m], inv));
+  }
+}
+
+template <int KER>
+__global__ void __launch_bounds__(TC_THREADS) tc_moments_df_kernel(TcMomParams p) {
+  constexpr int Q = TcCharge<KER>::Q;
+  extern __shared__ double tc_sm[];
+  const int np = p.np, npts = np * np * np;
+  f2* Ls = reinterpret_cast<f2*>(tc_sm);  // [TC_CHUNK][3][np]
+  f2* qs = Ls + TC_CHUNK * 3 * np;        // [TC_CHUNK][Q]
+  const TcItem it = p.items[blockIdx.x];
+  const TcCluster C = p.clusters[it.cluster];
+  for (int s = threadIdx.x; s < TC_CHUNK; s += blockDim.x) {
+    const bool valid = s < it.n;
+    const int64_t slot = it.s0 + s;
+    for (int d = 0; d < 3; ++d) {
+      double t = valid ? (p.r[slot * 3 + d] - C.lo[d]) * C.inv[d] - 1.0 : 0.0;
+      t = fmin(1.0, fmax(-1.0, t));
+      tc_lagrange_df(t, np, p, Ls + (s * 3 + d) * np);
+    }
+    double q[Q];
+    for (int c = 0; c < Q; ++c) q[c] = 0.0;
+    if (valid) {
+      if constexpr (KER == SCTLGPU_LAPLACE3D_FXU) {
+        q[0] = p.v[slot];
+      } else if constexpr (KER == SCTLGPU_LAPLACE3D_DXU) {
+        for (int c = 0; c < 3; ++c) q[c] = p.n[slot * 3 + c] * p.v[slot];
+      } else if constexpr (KER == SCTLGPU_STOKES3D_FXU) {
+        for (int c = 0; c < 3; ++c) q[c] = p.v[slot * 3 + c];
+      } else {
+        for (int c = 0; c < 3; ++c)
+          for (int d = 0; d < 3; ++d) q[c * 3 + d] = p.n[slot * 3 + c] * p.v[slot * 3 + d];
+      }
+    }
+    for (int c = 0; c < Q; ++c) qs[s * Q + c] = tc_split(q[c]);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < npts; k += blockDim.x) {
+    const int i = k / (np * np), j = (k / np) % np, l = k % np;
+    f2 acc[Q];
+    for (int c = 0; c < Q; ++c) acc[c] = {0.f, 0.f};
+    for (int s = 0; s < it.n; ++s) {
+      const f2 wgt = df_mul(df_mul(Ls[(s * 3) * np + i], Ls[(s * 3 + 1) * np + j]), Ls[(s * 3 + 2) * np + l]);
+#pragma unroll
+      for (int c = 0; c < Q; ++c) df_acc(acc[c], df_mul(wgt, qs[s * Q + c]));
+    }
+    double* out = p.part + ((int64_t)blockIdx.x * npts + k) * Q;
+#pragma unroll
+    for (int c = 0; c < Q; ++c) out[c] = (double)acc[c].h + (double)acc[c].l;
+  }
+}
+
 // Moments of every approximated cluster (its chunks in order) into the proxy slots.
 template <int KER>
 __global__ void tc_reduce_kernel(TcMomParams p, int n_clusters) {
@@ -412,13 +497,15 @@ __global__ void tc_reduce_kernel(TcMomParams p, int n_clusters) {
 }
 
 template <int KER>
-cudaError_t tc_launch_moments(const TcMomParams& p, int n_items, int n_clusters, cudaStream_t st) {
+cudaError_t tc_launch_moments(const TcMomParams& p, int n_items, int n_clusters, bool df, cudaStream_t st) {
   constexpr int Q = TcCharge<KER>::Q;
   if (n_items == 0) return cudaSuccess;
+  // f2 and double tiles: both fit the same byte count (8 bytes per value)
   const size_t smem = (size_t)TC_CHUNK * (3 * p.np + Q) * sizeof(double);
-  cudaError_t e = cudaFuncSetAttribute(tc_moments_kernel<KER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  auto kern = df ? tc_moments_df_kernel<KER> : tc_moments_kernel<KER>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  tc_moments_kernel<KER><<<n_items, TC_THREADS, smem, st>>>(p);
+  kern<<<n_items, TC_THREADS, smem, st>>>(p);
   g_launches.fetch_add(1, std::memory_order_relaxed);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const int npts = p.np * p.np * p.np;
@@ -434,6 +521,7 @@ using namespace sctlgpu;
 
 struct sctlgpu_treecode_s {
   int kernel = 0, mode = 0, digits = 0, ND = 0, SD = 0, TD = 0;
+  bool df_moments = false;  // moments in double-float (plans in FP32 or double-float arithmetic)
   int device = 0;
   TcLayout L;
   int64_t ns = 0, nt = 0, n_items = 0;
@@ -536,6 +624,8 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   T->device = dev;
   T->ns = ns;
   T->nt = nt;
+  T->df_moments =
+      mode == SCTLGPU_MIXED && runtime_mixed_arith(runtime_effective_digits(mode, digits)) != MIXED_ARITH_F64;
   int order = prm ? prm->order : 0;
   double theta = prm ? prm->theta : 0.0;
   tc_defaults(digits, &order, &theta);
@@ -646,13 +736,17 @@ int sctlgpu_treecode_execute(sctlgpu_treecode T, const double* v_src, double* v_
   for (int m = 0; m < L.np; ++m) {
     p.x[m] = L.xcheb[m];
     p.w[m] = L.wcheb[m];
+    p.xh[m] = (float)L.xcheb[m];
+    p.xl[m] = (float)(L.xcheb[m] - (double)p.xh[m]);
+    p.wf[m] = (float)L.wcheb[m];  // +-1 or +-1/2: exact
   }
   const int nc = (int)L.clusters.size(), ni = (int)T->n_items;
+  const bool df = T->df_moments;
   switch (T->kernel) {
-    case SCTLGPU_LAPLACE3D_FXU: e = tc_launch_moments<SCTLGPU_LAPLACE3D_FXU>(p, ni, nc, st); break;
-    case SCTLGPU_LAPLACE3D_DXU: e = tc_launch_moments<SCTLGPU_LAPLACE3D_DXU>(p, ni, nc, st); break;
-    case SCTLGPU_STOKES3D_FXU: e = tc_launch_moments<SCTLGPU_STOKES3D_FXU>(p, ni, nc, st); break;
-    default: e = tc_launch_moments<SCTLGPU_STOKES3D_DXU>(p, ni, nc, st); break;
+    case SCTLGPU_LAPLACE3D_FXU: e = tc_launch_moments<SCTLGPU_LAPLACE3D_FXU>(p, ni, nc, df, st); break;
+    case SCTLGPU_LAPLACE3D_DXU: e = tc_launch_moments<SCTLGPU_LAPLACE3D_DXU>(p, ni, nc, df, st); break;
+    case SCTLGPU_STOKES3D_FXU: e = tc_launch_moments<SCTLGPU_STOKES3D_FXU>(p, ni, nc, df, st); break;
+    default: e = tc_launch_moments<SCTLGPU_STOKES3D_DXU>(p, ni, nc, df, st); break;
   }
   if (e != cudaSuccess) return runtime_record(e);
   return sctlgpu_near_plan_execute(T->plan, T->d_trg, T->d_r, T->d_n, T->d_v, nullptr, v_out,
