@@ -272,9 +272,11 @@ int sctlgpu_near_list_destroy(sctlgpu_near_list list);
  * fast path, EvalPVFMM (fmm-wrapper.txx:854-1038; Eval at :542-549 takes it for
  * 40,000 targets or more): v_out = scale * sum_s K(x_t - y_s, n_s) . f_s for
  * the four hot-path kernels, with work below the direct sum's Ns * Nt.  The
- * algorithm differs from PVFMM's (a particle-cluster treecode: clusters seen
- * from far enough are replaced by proxy sources at (order+1)^3 Chebyshev points
- * carrying interpolated moments; everything else is summed directly); every
+ * algorithm differs from PVFMM's (a barycentric Lagrange treecode over a
+ * source and a target tree: separated clusters are replaced by proxies at
+ * (order+1)^3 Chebyshev points -- source proxies carry interpolated moments,
+ * target proxies collect potentials that a downward pass interpolates to the
+ * targets -- and everything else is summed directly); every
  * interaction runs in the batched near-field kernels with `mode` / `digits`
  * arithmetic (SCTLGPU_F64 or SCTLGPU_MIXED).
  *
@@ -287,19 +289,24 @@ int sctlgpu_near_list_destroy(sctlgpu_near_list list);
  * execute: v_src (device, ns * SrcDim, source order as given; SetDensitySL /
  * DL) -> v_out (device, nt * TrgDim, target order as given); flags may hold
  * SCTLGPU_ACCUMULATE; asynchronous on `stream`.
- * info / layout: sizes[7] = {blocks, source slots (leaves padded to even
- * counts), all slots (with proxies), approximated clusters, direct
- * interactions, proxy interactions, order}, and the acceptance parameter.
- * layout is the host-only part of create (no device needed): the blocks
- * (sources indexing slots), the source of every slot (-1 padding, -2 proxy),
- * the target order of the blocks' target ranges, and per approximated cluster
- * {source slot begin, end, proxy slot begin, end}; any output may be NULL.
+ * info / layout: sizes[9] = {blocks, source slots (leaves padded to even
+ * counts), all source slots (with proxies), source clusters with proxies,
+ * direct interactions, interactions through proxies, order, target list
+ * (targets, then target proxies), target clusters with proxies}, and the
+ * acceptance parameter.  layout is the host-only part of create (no device
+ * needed): the blocks (sources index the source slots, targets the target
+ * list), the source of every slot (-1 padding, -2 proxy), the target order,
+ * per source cluster with proxies {slot begin, end, proxy slot begin, end}
+ * and per target cluster with proxies {target begin, end, proxy begin, end};
+ * any output may be NULL.
  */
 typedef struct sctlgpu_treecode_params {
-  double theta;  /* a cluster is approximated when (r_batch + r_cluster) < theta * distance; <= 0: from digits */
+  double theta;  /* a pair of clusters is separated when (r_trg + r_src) < theta * distance; <= 0: from digits */
   int order;     /* interpolation degree per dimension, 1..15; <= 0: from digits */
   int leaf_max;  /* sources per leaf; <= 0: 1.5 proxy slots */
-  int batch_max; /* targets per batch; <= 0: 512 */
+  int batch_max; /* targets per batch, <= 2048; <= 0: 512 */
+  int dual;      /* nonzero: target clusters interpolate too (cluster-cluster interactions, a downward pass);
+                    0: particle-cluster only */
 } sctlgpu_treecode_params;
 typedef struct sctlgpu_treecode_s* sctlgpu_treecode;
 int sctlgpu_treecode_create(sctlgpu_treecode* tc, int kernel, int mode, int digits, int64_t ns, const double* r_src,
@@ -312,7 +319,8 @@ int sctlgpu_treecode_status(sctlgpu_treecode tc, void* stream);
 int sctlgpu_treecode_destroy(sctlgpu_treecode tc);
 int sctlgpu_treecode_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, const double* r_trg,
                             const sctlgpu_treecode_params* params, int digits, int64_t* sizes, double* theta,
-                            sctlgpu_block* blocks, int64_t* slot_src, int64_t* trg_order, int64_t* clusters);
+                            sctlgpu_block* blocks, int64_t* slot_src, int64_t* trg_order, int64_t* clusters,
+                            int64_t* trg_clusters);
 
 /*
  * Applies precomputed near-interaction matrices and sums them per target:

@@ -85,14 +85,15 @@ SIGNATURES = {
     "sctlgpu_treecode_info": (_i, [_vp, _vp, ctypes.POINTER(_d)]),
     "sctlgpu_treecode_status": (_i, [_vp, _vp]),
     "sctlgpu_treecode_destroy": (_i, [_vp]),
-    "sctlgpu_treecode_layout": (_i, [_i, _i64, _vp, _i64, _vp, _vp, _i, _vp, ctypes.POINTER(_d), _vp, _vp, _vp, _vp]),
+    "sctlgpu_treecode_layout": (_i, [_i, _i64, _vp, _i64, _vp, _vp, _i, _vp, ctypes.POINTER(_d), _vp, _vp, _vp, _vp,
+                                     _vp]),
 }
 
 
 class TreecodeParams(ctypes.Structure):
     """sctlgpu_treecode_params."""
     _fields_ = [("theta", ctypes.c_double), ("order", ctypes.c_int), ("leaf_max", ctypes.c_int),
-                ("batch_max", ctypes.c_int)]
+                ("batch_max", ctypes.c_int), ("dual", ctypes.c_int)]
 NEAR_CLASSES = 10
 NOALLOC_SCRATCH_BYTES = 64 << 20
 

@@ -35,6 +35,7 @@
 #include <cstdint>
 #include <cstring>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -49,13 +50,15 @@ namespace {
 constexpr int TC_MAX_NP = 16;   // Chebyshev points per dimension (order + 1)
 constexpr int TC_CHUNK = 256;   // source slots per moment work item
 constexpr int TC_THREADS = 256;
+constexpr int TC_MAX_BATCH = 2048;  // targets per batch (the downward pass keeps a batch's sums in shared memory)
 
 struct TcNode {
   int64_t b = 0, e = 0;    // points [b, e) of the tree's permutation
   int64_t sb = 0, se = 0;  // slots [sb, se) (sources: leaves padded to even counts)
   double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0}, c[3] = {0, 0, 0}, r = 0;
   int32_t child0 = -1, nchild = 0;  // children are consecutive nodes
-  int64_t proxy = -1;               // first proxy slot of an approximated cluster
+  int32_t parent = -1;
+  int64_t proxy = -1;  // sources: first proxy slot; targets: first proxy entry of the target list
 };
 
 void set_box(const double* X, const std::vector<int64_t>& perm, TcNode& nd) {
@@ -113,6 +116,7 @@ void build_octree(const double* X, int64_t n, int64_t leaf_max, std::vector<int6
     for (int o = 0; o < 8; ++o) {
       if (!cnt[o]) continue;
       TcNode ch;
+      ch.parent = id;
       ch.b = off[o];
       ch.e = off[o] + cnt[o];
       set_box(X, perm, ch);
@@ -142,9 +146,14 @@ struct TcLayout {
   std::vector<int64_t> sperm, tperm;
   std::vector<int64_t> slot_src;  // source slot -> source index, -1 = padding
   int64_t n_src_slots = 0, n_slots = 0;
-  std::vector<int32_t> clusters;  // approximated clusters (node ids) in proxy order
+  std::vector<int32_t> clusters;  // approximated source clusters (node ids) in proxy order
+  std::vector<int32_t> tclusters; // target clusters with proxies (node ids) in proxy order
+  int64_t n_trg_slots = 0;        // sorted targets, then the target clusters' proxies
+  std::vector<int32_t> batches;   // target leaves in target order
+  std::vector<int32_t> anc_ptr, anc;  // per batch: its target clusters with proxies (indices of tclusters)
   std::vector<sctlgpu_block> blocks;
-  int64_t pp = 0, pc = 0;         // interactions (target x slot) of the direct and proxy blocks
+  int64_t pp = 0, approx = 0;     // interactions of the direct blocks and of the proxy blocks
+  bool dual = true;
   double xcheb[TC_MAX_NP], wcheb[TC_MAX_NP];
 };
 
@@ -160,8 +169,10 @@ void tc_defaults(int digits, int* order, double* theta) {
 }
 
 int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, const double* r_trg, int order,
-                    double theta, int64_t leaf_max, int64_t batch_max, TcLayout& L) {
+                    double theta, int64_t leaf_max, int64_t batch_max, bool dual, TcLayout& L) {
   if (order < 1 || order >= TC_MAX_NP || !(theta > 0) || theta >= 1.0) return SCTLGPU_ERR_INVALID_ARGUMENT;
+  if (batch_max > TC_MAX_BATCH) return SCTLGPU_ERR_INVALID_ARGUMENT;
+  L.dual = dual;
   L.order = order;
   L.np = order + 1;
   L.npts = L.np * L.np * L.np;
@@ -199,68 +210,114 @@ int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, con
     }
   }
   L.n_src_slots = cur;
-  // traversal: per batch the approximated clusters and the directly summed leaves
-  std::vector<int32_t> batches;
+  // Traversal over (target node, source node) pairs.  With `dual`, from the two roots; a pair
+  // that passes the acceptance test takes the cheapest of: direct (targets x sources),
+  // targets x source proxies, target proxies x sources, target proxies x source proxies, where
+  // a side may use its proxies only when it holds more points than proxies; otherwise the
+  // larger node (by radius) is split, and two leaves are summed directly.  Without `dual`,
+  // every batch starts from the source root and only the source side is ever approximated.
+  const int64_t Ps = (int64_t)L.npts * L.per_point, Pt = L.npts;
+  struct Rec {
+    int32_t t, s;
+    char kind;  // 0 direct, 1 source proxies, 2 target proxies, 3 both
+  };
+  std::vector<Rec> recs;
+  std::vector<char> sused(L.src.size(), 0), tused(L.trg.size(), 0);
+  std::vector<std::pair<int32_t, int32_t>> st;
+  L.batches.clear();
   for (int32_t i = 0; i < (int32_t)L.trg.size(); ++i)
-    if (L.trg[i].nchild == 0 && L.trg[i].e > L.trg[i].b) batches.push_back(i);
-  std::sort(batches.begin(), batches.end(), [&](int32_t a, int32_t b) { return L.trg[a].b < L.trg[b].b; });
-  std::vector<std::vector<int32_t>> pcl(batches.size()), ppl(batches.size());
-  std::vector<char> used(L.src.size(), 0);
-  std::vector<int32_t> stack;
-  for (size_t bi = 0; bi < batches.size() && ns > 0; ++bi) {
-    const TcNode& B = L.trg[batches[bi]];
-    stack.assign(1, 0);
-    while (!stack.empty()) {
-      const int32_t id = stack.back();
-      stack.pop_back();
-      const TcNode& C = L.src[id];
-      if (C.e == C.b) continue;
-      const double dx = B.c[0] - C.c[0], dy = B.c[1] - C.c[1], dz = B.c[2] - C.c[2];
-      const double dist = std::sqrt(dx * dx + dy * dy + dz * dz);
-      if (B.r + C.r < theta * dist && C.e - C.b > (int64_t)L.npts * L.per_point) {
-        pcl[bi].push_back(id);
-        used[id] = 1;
-      } else if (C.nchild == 0) {
-        ppl[bi].push_back(id);
-      } else {
-        for (int k = C.nchild - 1; k >= 0; --k) stack.push_back(C.child0 + k);
-      }
+    if (L.trg[i].nchild == 0 && L.trg[i].e > L.trg[i].b) L.batches.push_back(i);
+  std::sort(L.batches.begin(), L.batches.end(), [&](int32_t a, int32_t b) { return L.trg[a].b < L.trg[b].b; });
+  if (ns > 0 && nt > 0) {
+    if (L.dual)
+      st.push_back({0, 0});
+    else
+      for (auto it = L.batches.rbegin(); it != L.batches.rend(); ++it) st.push_back({*it, 0});
+  }
+  while (!st.empty()) {
+    const auto [ti, si] = st.back();
+    st.pop_back();
+    const TcNode &T = L.trg[ti], &S = L.src[si];
+    if (T.e == T.b || S.e == S.b) continue;
+    const double dx = T.c[0] - S.c[0], dy = T.c[1] - S.c[1], dz = T.c[2] - S.c[2];
+    const double dist = std::sqrt(dx * dx + dy * dy + dz * dz);
+    const int64_t nT = T.e - T.b, nS = S.e - S.b, sS = S.se - S.sb;
+    if (T.r + S.r < theta * dist) {
+      const bool src_ok = nS > Ps, trg_ok = L.dual && nT > Pt;
+      double best = (double)nT * sS;
+      char kind = 0;
+      if (src_ok && (double)nT * Ps < best) best = (double)nT * Ps, kind = 1;
+      if (trg_ok && (double)Pt * sS < best) best = (double)Pt * sS, kind = 2;
+      if (src_ok && trg_ok && (double)Pt * Ps < best) best = (double)Pt * Ps, kind = 3;
+      recs.push_back({ti, si, kind});
+      if (kind & 1) sused[si] = 1;
+      if (kind & 2) tused[ti] = 1;
+      continue;
+    }
+    const bool tl = T.nchild == 0 || !L.dual, sl = S.nchild == 0;
+    if (tl && sl) {
+      recs.push_back({ti, si, 0});
+    } else if (sl || (!tl && T.r >= S.r)) {
+      for (int k = T.nchild - 1; k >= 0; --k) st.push_back({T.child0 + k, si});
+    } else {
+      for (int k = S.nchild - 1; k >= 0; --k) st.push_back({ti, S.child0 + k});
     }
   }
-  // proxies of the approximated clusters, in node order (siblings adjacent)
+  // proxies: source clusters in node order (siblings adjacent), then target clusters
   L.clusters.clear();
   int64_t pcur = L.n_src_slots;
   for (int32_t i = 0; i < (int32_t)L.src.size(); ++i)
-    if (used[i]) {
+    if (sused[i]) {
       L.src[i].proxy = pcur;
       pcur += L.proxy_slots;
       L.clusters.push_back(i);
     }
   L.n_slots = pcur;
-  // blocks: contiguous slot ranges merged per batch
+  L.tclusters.clear();
+  std::vector<int32_t> tindex(L.trg.size(), -1);
+  int64_t tcur = nt;
+  for (int32_t i = 0; i < (int32_t)L.trg.size(); ++i)
+    if (tused[i]) {
+      L.trg[i].proxy = tcur;
+      tcur += Pt;
+      tindex[i] = (int32_t)L.tclusters.size();
+      L.tclusters.push_back(i);
+    }
+  L.n_trg_slots = tcur;
+  // per batch, its ancestors (and itself) that carry target proxies
+  L.anc_ptr.assign(1, 0);
+  L.anc.clear();
+  for (int32_t b : L.batches) {
+    for (int32_t a = b; a >= 0; a = L.trg[a].parent)
+      if (tindex[a] >= 0) L.anc.push_back(tindex[a]);
+    L.anc_ptr.push_back((int32_t)L.anc.size());
+  }
+  // blocks: per target range, contiguous source ranges merged
+  struct Blk {
+    int64_t t0, tn, s0, s1;
+  };
+  std::vector<Blk> bl;
+  bl.reserve(recs.size());
+  for (const Rec& r : recs) {
+    const TcNode &T = L.trg[r.t], &S = L.src[r.s];
+    const bool tp = r.kind & 2, sp = r.kind & 1;
+    bl.push_back({tp ? T.proxy : T.b, tp ? Pt : T.e - T.b, sp ? S.proxy : S.sb, sp ? S.proxy + Ps : S.se});
+  }
+  std::sort(bl.begin(), bl.end(), [](const Blk& a, const Blk& b) {
+    return a.t0 != b.t0 ? a.t0 < b.t0 : (a.tn != b.tn ? a.tn < b.tn : a.s0 < b.s0);
+  });
   L.blocks.clear();
-  L.pp = L.pc = 0;
-  for (size_t bi = 0; bi < batches.size(); ++bi) {
-    const TcNode& B = L.trg[batches[bi]];
-    const int64_t t0 = B.b, tn = B.e - B.b;
-    auto emit = [&](std::vector<std::pair<int64_t, int64_t>>& r, int64_t& count) {
-      std::sort(r.begin(), r.end());
-      size_t k = 0;
-      while (k < r.size()) {
-        int64_t s0 = r[k].first, s1 = r[k].second;
-        size_t j = k + 1;
-        while (j < r.size() && r[j].first == s1) s1 = r[j++].second;
-        L.blocks.push_back({s0, s1 - s0, t0, tn});
-        count += (s1 - s0) * tn;
-        k = j;
-      }
-    };
-    std::vector<std::pair<int64_t, int64_t>> r;
-    for (int32_t id : ppl[bi]) r.push_back({L.src[id].sb, L.src[id].se});
-    emit(r, L.pp);
-    r.clear();
-    for (int32_t id : pcl[bi]) r.push_back({L.src[id].proxy, L.src[id].proxy + L.proxy_slots});
-    emit(r, L.pc);
+  L.pp = L.approx = 0;
+  for (size_t k = 0; k < bl.size();) {
+    Blk cur = bl[k];
+    size_t j = k + 1;
+    const bool direct = cur.t0 < nt && cur.s0 < L.n_src_slots;
+    while (j < bl.size() && bl[j].t0 == cur.t0 && bl[j].tn == cur.tn && bl[j].s0 == cur.s1 &&
+           (bl[j].s0 < L.n_src_slots) == (cur.s0 < L.n_src_slots))
+      cur.s1 = bl[j++].s1;
+    L.blocks.push_back({cur.s0, cur.s1 - cur.s0, cur.t0, cur.tn});
+    (direct ? L.pp : L.approx) += (cur.s1 - cur.s0) * cur.tn;
+    k = j;
   }
   return SCTLGPU_OK;
 }
@@ -514,6 +571,143 @@ cudaError_t tc_launch_moments(const TcMomParams& p, int n_items, int n_clusters,
   return cudaGetLastError();
 }
 
+// Downward pass and output: every sorted target k gets its plan sum u[k] plus, for each of
+// its target clusters A with proxies (its batch and the batch's ancestors),
+// sum_k L_k(x) u[A's proxy k] -- the interpolation of the potentials the plan accumulated at
+// A's Chebyshev points -- and is written (or added) to out[perm[k]].  One CTA per batch, one
+// warp per target: the lanes split the (order+1)^3 terms, in double-float (DF) or FP64.
+struct TcTrgBox {
+  double lo[3], inv[3];
+  int64_t proxy;  // first proxy entry of the target list
+};
+struct TcL2PParams {
+  const TcTrgBox* boxes;
+  const int64_t* bt0;  // per batch: first sorted target
+  const int32_t* btn;  // per batch: targets
+  const int32_t* anc_ptr;
+  const int32_t* anc;
+  const double* r;      // sorted target coordinates
+  const double* u;      // plan results over the target list (targets, then proxies)
+  const int64_t* perm;  // sorted target -> output index
+  double* out;
+  int accumulate;
+  int np;
+  double x[TC_MAX_NP], w[TC_MAX_NP];
+  float xh[TC_MAX_NP], xl[TC_MAX_NP], wf[TC_MAX_NP];
+};
+
+__device__ __forceinline__ void tc_lagrange_df2(double tt, int np, const TcL2PParams& p, f2* L) {
+  const f2 t = tc_split(tt);
+  int hit = -1;
+  f2 sum = {0.f, 0.f};
+  for (int m = 0; m < np; ++m) {
+    const f2 d = df_norm(df_add(t, {-p.xh[m], -p.xl[m]}));
+    if (d.h == 0.f) hit = m;
+    const f2 q = d.h != 0.f ? df_mulf(tc_rcp(d), p.wf[m]) : f2{0.f, 0.f};
+    L[m] = q;
+    df_acc(sum, q);
+  }
+  if (hit >= 0) {
+    for (int m = 0; m < np; ++m) L[m] = {m == hit ? 1.f : 0.f, 0.f};
+  } else {
+    const f2 inv = tc_rcp(df_norm(sum));
+    for (int m = 0; m < np; ++m) L[m] = df_norm(df_mul(L[m], inv));
+  }
+}
+
+template <int TD, bool DF>
+__global__ void __launch_bounds__(TC_THREADS) tc_l2p_kernel(TcL2PParams p) {
+  using V = typename std::conditional<DF, f2, double>::type;
+  extern __shared__ double tc_sm[];
+  const int np = p.np, npts = np * np * np;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  V* P = reinterpret_cast<V*>(tc_sm);                         // [npts][TD] proxy potentials of one cluster
+  V* Lw = P + (size_t)npts * TD + warp * 3 * TC_MAX_NP;       // per warp: [3][np] basis values
+  double* acc_t = tc_sm + (size_t)npts * TD + nwarps * 3 * TC_MAX_NP;  // [batch_max][TD] target sums
+  const int b = blockIdx.x;
+  const int64_t t0 = p.bt0[b];
+  const int tn = p.btn[b];
+  for (int e = threadIdx.x; e < tn * TD; e += blockDim.x) acc_t[e] = p.u[t0 * TD + e];
+  for (int a = p.anc_ptr[b]; a < p.anc_ptr[b + 1]; ++a) {
+    const TcTrgBox A = p.boxes[p.anc[a]];
+    __syncthreads();
+    for (int e = threadIdx.x; e < npts * TD; e += blockDim.x) {
+      const double v = p.u[A.proxy * TD + e];
+      if constexpr (DF)
+        P[e] = tc_split(v);
+      else
+        P[e] = v;
+    }
+    __syncthreads();
+    for (int t = warp; t < tn; t += nwarps) {  // one warp per target
+      const int64_t k = t0 + t;
+      if (lane < 3) {
+        double tt = (p.r[k * 3 + lane] - A.lo[lane]) * A.inv[lane] - 1.0;
+        tt = fmin(1.0, fmax(-1.0, tt));
+        if constexpr (DF) {
+          tc_lagrange_df2(tt, np, p, Lw + lane * TC_MAX_NP);
+        } else {
+          double* L = Lw + lane * TC_MAX_NP;
+          int hit = -1;
+          double sum = 0.0;
+          for (int m = 0; m < np; ++m) {
+            const double d = tt - p.x[m];
+            if (d == 0.0) hit = m;
+            L[m] = d != 0.0 ? p.w[m] / d : 0.0;
+            sum += L[m];
+          }
+          for (int m = 0; m < np; ++m) L[m] = hit >= 0 ? (m == hit ? 1.0 : 0.0) : L[m] / sum;
+        }
+      }
+      __syncwarp();
+      V acc[TD];
+      for (int c = 0; c < TD; ++c) acc[c] = V{};
+      for (int kk = lane; kk < npts; kk += 32) {
+        const int i = kk / (np * np), j = (kk / np) % np, l = kk % np;
+        if constexpr (DF) {
+          const f2 wgt = df_mul(df_mul(Lw[i], Lw[TC_MAX_NP + j]), Lw[2 * TC_MAX_NP + l]);
+#pragma unroll
+          for (int c = 0; c < TD; ++c) df_acc(acc[c], df_mul(wgt, P[kk * TD + c]));
+        } else {
+          const double wgt = Lw[i] * Lw[TC_MAX_NP + j] * Lw[2 * TC_MAX_NP + l];
+#pragma unroll
+          for (int c = 0; c < TD; ++c) acc[c] = fma(wgt, P[kk * TD + c], acc[c]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < TD; ++c) {
+        double v;
+        if constexpr (DF)
+          v = (double)acc[c].h + (double)acc[c].l;
+        else
+          v = acc[c];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) acc_t[t * TD + c] += v;
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < tn * TD; e += blockDim.x) {
+    const int t = e / TD, c = e % TD;
+    double* o = p.out + p.perm[t0 + t] * TD + c;
+    *o = p.accumulate ? *o + acc_t[e] : acc_t[e];
+  }
+}
+
+cudaError_t tc_launch_l2p(const TcL2PParams& p, int td, bool df, int n_batches, int batch_max, cudaStream_t st) {
+  if (n_batches == 0) return cudaSuccess;
+  const size_t smem =
+      ((size_t)p.np * p.np * p.np * td + (TC_THREADS / 32) * 3 * TC_MAX_NP + (size_t)batch_max * td) * sizeof(double);
+  auto kern = td == 3 ? (df ? tc_l2p_kernel<3, true> : tc_l2p_kernel<3, false>)
+                      : (df ? tc_l2p_kernel<1, true> : tc_l2p_kernel<1, false>);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  kern<<<n_batches, TC_THREADS, smem, st>>>(p);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  return cudaGetLastError();
+}
+
 }  // namespace
 }  // namespace sctlgpu
 
@@ -521,14 +715,16 @@ using namespace sctlgpu;
 
 struct sctlgpu_treecode_s {
   int kernel = 0, mode = 0, digits = 0, ND = 0, SD = 0, TD = 0;
-  bool df_moments = false;  // moments in double-float (plans in FP32 or double-float arithmetic)
-  int device = 0;
+  bool df = false;  // moments and downward pass in double-float (plans in FP32 or double-float arithmetic)
+  int device = 0, batch_max = 0;
   TcLayout L;
   int64_t ns = 0, nt = 0, n_items = 0;
-  double *d_trg = nullptr, *d_r = nullptr, *d_n = nullptr, *d_v = nullptr, *d_part = nullptr;
-  int64_t* d_slot_src = nullptr;
+  double *d_trg = nullptr, *d_r = nullptr, *d_n = nullptr, *d_v = nullptr, *d_part = nullptr, *d_u = nullptr;
+  int64_t *d_slot_src = nullptr, *d_tperm = nullptr, *d_bt0 = nullptr;
+  int32_t *d_btn = nullptr, *d_anc_ptr = nullptr, *d_anc = nullptr;
   TcCluster* d_clusters = nullptr;
   TcItem* d_items = nullptr;
+  TcTrgBox* d_boxes = nullptr;
   sctlgpu_near_plan plan = nullptr;
 };
 
@@ -536,14 +732,10 @@ namespace {
 
 void tc_free(sctlgpu_treecode_s* T) {
   if (T->plan) sctlgpu_near_plan_destroy(T->plan);
-  cudaFree(T->d_trg);
-  cudaFree(T->d_r);
-  cudaFree(T->d_n);
-  cudaFree(T->d_v);
-  cudaFree(T->d_part);
-  cudaFree(T->d_slot_src);
-  cudaFree(T->d_clusters);
-  cudaFree(T->d_items);
+  for (void* q : {(void*)T->d_trg, (void*)T->d_r, (void*)T->d_n, (void*)T->d_v, (void*)T->d_part, (void*)T->d_u,
+                  (void*)T->d_slot_src, (void*)T->d_tperm, (void*)T->d_bt0, (void*)T->d_btn, (void*)T->d_anc_ptr,
+                  (void*)T->d_anc, (void*)T->d_clusters, (void*)T->d_items, (void*)T->d_boxes})
+    cudaFree(q);
   delete T;
 }
 
@@ -558,30 +750,43 @@ int tc_check_common(int kernel, int64_t ns, const double* r_src, int64_t nt, con
   return SCTLGPU_OK;
 }
 
+int tc_layout_from(int kernel, int digits, int64_t ns, const double* r_src, int64_t nt, const double* r_trg,
+                   const sctlgpu_treecode_params* prm, TcLayout& L, int* batch_max) {
+  int order = prm ? prm->order : 0;
+  double theta = prm ? prm->theta : 0.0;
+  tc_defaults(digits, &order, &theta);
+  const int bm = prm && prm->batch_max > 0 ? prm->batch_max : 512;
+  if (batch_max) *batch_max = bm;
+  return tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, prm ? prm->leaf_max : 0, bm,
+                         !prm || prm->dual != 0, L);
+}
+
+void tc_sizes(const TcLayout& L, int64_t* sizes) {
+  sizes[0] = (int64_t)L.blocks.size();
+  sizes[1] = L.n_src_slots;
+  sizes[2] = L.n_slots;
+  sizes[3] = (int64_t)L.clusters.size();
+  sizes[4] = L.pp;
+  sizes[5] = L.approx;
+  sizes[6] = L.order;
+  sizes[7] = L.n_trg_slots;
+  sizes[8] = (int64_t)L.tclusters.size();
+}
+
 }  // namespace
 
 extern "C" {
 
 int sctlgpu_treecode_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, const double* r_trg,
                             const sctlgpu_treecode_params* prm, int digits, int64_t* sizes, double* theta_out,
-                            sctlgpu_block* blocks, int64_t* slot_src, int64_t* trg_order, int64_t* clusters) {
+                            sctlgpu_block* blocks, int64_t* slot_src, int64_t* trg_order, int64_t* clusters,
+                            int64_t* trg_clusters) {
   int rc = tc_check_common(kernel, ns, r_src, nt, r_trg);
   if (rc) return rc;
   if (!sizes) return SCTLGPU_ERR_NULL_POINTER;
-  int order = prm ? prm->order : 0;
-  double theta = prm ? prm->theta : 0.0;
-  tc_defaults(digits, &order, &theta);
   TcLayout L;
-  rc = tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, prm ? prm->leaf_max : 0, prm ? prm->batch_max : 0,
-                       L);
-  if (rc) return rc;
-  sizes[0] = (int64_t)L.blocks.size();
-  sizes[1] = L.n_src_slots;
-  sizes[2] = L.n_slots;
-  sizes[3] = (int64_t)L.clusters.size();
-  sizes[4] = L.pp;
-  sizes[5] = L.pc;
-  sizes[6] = L.order;
+  if ((rc = tc_layout_from(kernel, digits, ns, r_src, nt, r_trg, prm, L, nullptr))) return rc;
+  tc_sizes(L, sizes);
   if (theta_out) *theta_out = L.theta;
   if (blocks) std::copy(L.blocks.begin(), L.blocks.end(), blocks);
   if (slot_src) {
@@ -596,6 +801,14 @@ int sctlgpu_treecode_layout(int kernel, int64_t ns, const double* r_src, int64_t
       clusters[4 * k + 1] = C.se;
       clusters[4 * k + 2] = C.proxy;
       clusters[4 * k + 3] = C.proxy + L.proxy_slots;
+    }
+  if (trg_clusters)
+    for (size_t k = 0; k < L.tclusters.size(); ++k) {
+      const TcNode& C = L.trg[L.tclusters[k]];
+      trg_clusters[4 * k + 0] = C.b;
+      trg_clusters[4 * k + 1] = C.e;
+      trg_clusters[4 * k + 2] = C.proxy;
+      trg_clusters[4 * k + 3] = C.proxy + L.npts;
     }
   return SCTLGPU_OK;
 }
@@ -624,19 +837,13 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   T->device = dev;
   T->ns = ns;
   T->nt = nt;
-  T->df_moments =
-      mode == SCTLGPU_MIXED && runtime_mixed_arith(runtime_effective_digits(mode, digits)) != MIXED_ARITH_F64;
-  int order = prm ? prm->order : 0;
-  double theta = prm ? prm->theta : 0.0;
-  tc_defaults(digits, &order, &theta);
+  T->df = mode == SCTLGPU_MIXED && runtime_mixed_arith(runtime_effective_digits(mode, digits)) != MIXED_ARITH_F64;
   TcLayout& L = T->L;
-  rc = tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, prm ? prm->leaf_max : 0, prm ? prm->batch_max : 0,
-                       L);
-  if (rc) {
+  if ((rc = tc_layout_from(kernel, digits, ns, r_src, nt, r_trg, prm, L, &T->batch_max))) {
     delete T;
     return rc;
   }
-  // slot arrays: sources (sorted, padded), then proxies
+  // source slots: sources (sorted, padded), then the source proxies
   const int64_t S = L.n_slots;
   std::vector<double> hr((size_t)S * 3, 0.0), hn(nd ? (size_t)S * 3 : 0, 0.0), hv((size_t)S * sd, 0.0);
   for (int64_t i = 0; i < L.n_src_slots; ++i) {
@@ -674,9 +881,32 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   }
   T->n_items = (int64_t)hi.size();
   const int64_t npts = L.npts, Q = kernel == SCTLGPU_STOKES3D_DXU ? 9 : (kernel == SCTLGPU_LAPLACE3D_FXU ? 1 : 3);
-  std::vector<double> htrg((size_t)nt * 3);
+  // target list: sorted targets, then the target clusters' proxies (their Chebyshev points)
+  const int64_t NT = L.n_trg_slots;
+  std::vector<double> htrg((size_t)NT * 3);
   for (int64_t k = 0; k < nt; ++k)
     for (int d = 0; d < 3; ++d) htrg[k * 3 + d] = r_trg[L.tperm[k] * 3 + d];
+  std::vector<TcTrgBox> hb;
+  for (int32_t id : L.tclusters) {
+    const TcNode& C = L.trg[id];
+    TcTrgBox tb{};
+    double ext[3];
+    interp_box(C, tb.lo, ext);
+    for (int d = 0; d < 3; ++d) tb.inv[d] = 2.0 / ext[d];
+    tb.proxy = C.proxy;
+    for (int k = 0; k < L.npts; ++k) {
+      const int i = k / (L.np * L.np), j = (k / L.np) % L.np, l = k % L.np;
+      const double g[3] = {L.xcheb[i], L.xcheb[j], L.xcheb[l]};
+      for (int d = 0; d < 3; ++d) htrg[(C.proxy + k) * 3 + d] = tb.lo[d] + 0.5 * (g[d] + 1.0) * ext[d];
+    }
+    hb.push_back(tb);
+  }
+  std::vector<int64_t> hbt0;
+  std::vector<int32_t> hbtn;
+  for (int32_t b : L.batches) {
+    hbt0.push_back(L.trg[b].b);
+    hbtn.push_back((int32_t)(L.trg[b].e - L.trg[b].b));
+  }
   cudaError_t e = cudaSuccess;
   auto up = [&](void** dst, const void* src, size_t bytes) {
     if (e != cudaSuccess) return;
@@ -690,14 +920,25 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   up((void**)&T->d_slot_src, L.slot_src.data(), L.slot_src.size() * sizeof(int64_t));
   up((void**)&T->d_clusters, hc.data(), hc.size() * sizeof(TcCluster));
   up((void**)&T->d_items, hi.data(), hi.size() * sizeof(TcItem));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&T->d_part, std::max<size_t>(16, (size_t)T->n_items * npts * Q * sizeof(double)));
+  up((void**)&T->d_tperm, L.tperm.data(), L.tperm.size() * sizeof(int64_t));
+  up((void**)&T->d_boxes, hb.data(), hb.size() * sizeof(TcTrgBox));
+  up((void**)&T->d_bt0, hbt0.data(), hbt0.size() * sizeof(int64_t));
+  up((void**)&T->d_btn, hbtn.data(), hbtn.size() * sizeof(int32_t));
+  up((void**)&T->d_anc_ptr, L.anc_ptr.data(), L.anc_ptr.size() * sizeof(int32_t));
+  up((void**)&T->d_anc, L.anc.data(), L.anc.size() * sizeof(int32_t));
+  if (e == cudaSuccess)
+    e = cudaMalloc((void**)&T->d_part, std::max<size_t>(16, (size_t)T->n_items * npts * Q * sizeof(double)));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&T->d_u, std::max<size_t>(16, (size_t)NT * td * sizeof(double)));
   if (e != cudaSuccess) {
     tc_free(T);
     return runtime_record(e);
   }
-  std::vector<int64_t> tmap(L.tperm.begin(), L.tperm.end());
-  rc = sctlgpu_near_plan_create(&T->plan, kernel, mode, digits, (int64_t)L.blocks.size(), L.blocks.data(), S, nt,
-                                nt ? tmap.data() : nullptr, nt);
+  // the plan accumulates into d_u over the whole target list (identity map: the scattered,
+  // zero-initialised form of the plan)
+  std::vector<int64_t> ident((size_t)NT);
+  std::iota(ident.begin(), ident.end(), (int64_t)0);
+  rc = sctlgpu_near_plan_create(&T->plan, kernel, mode, digits, (int64_t)L.blocks.size(), L.blocks.data(), S, NT,
+                                NT ? ident.data() : nullptr, NT);
   if (rc) {
     T->plan = nullptr;
     tc_free(T);
@@ -716,6 +957,7 @@ int sctlgpu_treecode_execute(sctlgpu_treecode T, const double* v_src, double* v_
   cudaStream_t st = (cudaStream_t)stream;
   const TcLayout& L = T->L;
   cudaError_t e = cudaSuccess;
+  if (T->nt == 0) return SCTLGPU_OK;
   if (L.n_src_slots) {
     const int64_t work = L.n_src_slots * T->SD;
     tc_gather_kernel<<<(unsigned)std::min<int64_t>((work + 255) / 256, 152 * 16), 256, 0, st>>>(
@@ -733,37 +975,44 @@ int sctlgpu_treecode_execute(sctlgpu_treecode T, const double* v_src, double* v_
   p.pn = T->d_n;
   p.pv = T->d_v;
   p.np = L.np;
+  TcL2PParams q{};
+  q.boxes = T->d_boxes;
+  q.bt0 = T->d_bt0;
+  q.btn = T->d_btn;
+  q.anc_ptr = T->d_anc_ptr;
+  q.anc = T->d_anc;
+  q.r = T->d_trg;
+  q.u = T->d_u;
+  q.perm = T->d_tperm;
+  q.out = v_out;
+  q.accumulate = (flags & SCTLGPU_ACCUMULATE) ? 1 : 0;
+  q.np = L.np;
   for (int m = 0; m < L.np; ++m) {
-    p.x[m] = L.xcheb[m];
-    p.w[m] = L.wcheb[m];
-    p.xh[m] = (float)L.xcheb[m];
-    p.xl[m] = (float)(L.xcheb[m] - (double)p.xh[m]);
-    p.wf[m] = (float)L.wcheb[m];  // +-1 or +-1/2: exact
+    p.x[m] = q.x[m] = L.xcheb[m];
+    p.w[m] = q.w[m] = L.wcheb[m];
+    p.xh[m] = q.xh[m] = (float)L.xcheb[m];
+    p.xl[m] = q.xl[m] = (float)(L.xcheb[m] - (double)p.xh[m]);
+    p.wf[m] = q.wf[m] = (float)L.wcheb[m];  // +-1 or +-1/2: exact
   }
   const int nc = (int)L.clusters.size(), ni = (int)T->n_items;
-  const bool df = T->df_moments;
   switch (T->kernel) {
-    case SCTLGPU_LAPLACE3D_FXU: e = tc_launch_moments<SCTLGPU_LAPLACE3D_FXU>(p, ni, nc, df, st); break;
-    case SCTLGPU_LAPLACE3D_DXU: e = tc_launch_moments<SCTLGPU_LAPLACE3D_DXU>(p, ni, nc, df, st); break;
-    case SCTLGPU_STOKES3D_FXU: e = tc_launch_moments<SCTLGPU_STOKES3D_FXU>(p, ni, nc, df, st); break;
-    default: e = tc_launch_moments<SCTLGPU_STOKES3D_DXU>(p, ni, nc, df, st); break;
+    case SCTLGPU_LAPLACE3D_FXU: e = tc_launch_moments<SCTLGPU_LAPLACE3D_FXU>(p, ni, nc, T->df, st); break;
+    case SCTLGPU_LAPLACE3D_DXU: e = tc_launch_moments<SCTLGPU_LAPLACE3D_DXU>(p, ni, nc, T->df, st); break;
+    case SCTLGPU_STOKES3D_FXU: e = tc_launch_moments<SCTLGPU_STOKES3D_FXU>(p, ni, nc, T->df, st); break;
+    default: e = tc_launch_moments<SCTLGPU_STOKES3D_DXU>(p, ni, nc, T->df, st); break;
   }
   if (e != cudaSuccess) return runtime_record(e);
-  return sctlgpu_near_plan_execute(T->plan, T->d_trg, T->d_r, T->d_n, T->d_v, nullptr, v_out,
-                                   (flags & SCTLGPU_ACCUMULATE) | SCTLGPU_DEVICE_PTRS, stream);
+  int rc = sctlgpu_near_plan_execute(T->plan, T->d_trg, T->d_r, T->d_n, T->d_v, nullptr, T->d_u, SCTLGPU_DEVICE_PTRS,
+                                     stream);
+  if (rc) return rc;
+  e = tc_launch_l2p(q, T->TD, T->df, (int)L.batches.size(), T->batch_max, st);
+  return e == cudaSuccess ? SCTLGPU_OK : runtime_record(e);
 }
 
 int sctlgpu_treecode_info(sctlgpu_treecode T, int64_t* stats, double* theta) {
   if (!T || !stats) return SCTLGPU_ERR_NULL_POINTER;
-  const TcLayout& L = T->L;
-  stats[0] = (int64_t)L.blocks.size();
-  stats[1] = L.n_src_slots;
-  stats[2] = L.n_slots;
-  stats[3] = (int64_t)L.clusters.size();
-  stats[4] = L.pp;
-  stats[5] = L.pc;
-  stats[6] = L.order;
-  if (theta) *theta = L.theta;
+  tc_sizes(T->L, stats);
+  if (theta) *theta = T->L.theta;
   return SCTLGPU_OK;
 }
 

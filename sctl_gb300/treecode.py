@@ -29,16 +29,18 @@ def _host(a):
     return np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
 
 
-def _params(order, theta, leaf_max, batch_max):
-    return capi.TreecodeParams(float(theta or 0.0), int(order or 0), int(leaf_max or 0), int(batch_max or 0))
+def _params(order, theta, leaf_max, batch_max, dual=True):
+    return capi.TreecodeParams(float(theta or 0.0), int(order or 0), int(leaf_max or 0), int(batch_max or 0),
+                               1 if dual else 0)
 
 
-_SIZE_KEYS = ("blocks", "source_slots", "slots", "clusters", "direct_interactions", "proxy_interactions", "order")
+_SIZE_KEYS = ("blocks", "source_slots", "slots", "clusters", "direct_interactions", "proxy_interactions", "order",
+              "target_list", "target_clusters")
 
 
 class Treecode:
     def __init__(self, kernel, r_src, r_trg, n_src=None, digits: int = 10, mode="mixed", order=0, theta=0.0,
-                 leaf_max=0, batch_max=0):
+                 leaf_max=0, batch_max=0, dual=True):
         self.kernel = capi.KERNEL_IDS[kernel] if isinstance(kernel, str) else int(kernel)
         self.mode = capi.MODE_IDS[mode] if isinstance(mode, str) else int(mode)
         self.digits = int(digits)
@@ -48,7 +50,7 @@ class Treecode:
         self.sd, self.td = sd, td
         lib = capi.load()
         h = ctypes.c_void_p()
-        prm = _params(order, theta, leaf_max, batch_max)
+        prm = _params(order, theta, leaf_max, batch_max, dual)
         rc = lib.sctlgpu_treecode_create(ctypes.byref(h), self.kernel, self.mode, self.digits, self.ns,
                                          xs.ctypes.data if xs.size else None,
                                          ns_.ctypes.data if ns_ is not None and ns_.size else None, self.nt,
@@ -74,7 +76,7 @@ class Treecode:
         return out
 
     def info(self):
-        sizes = (ctypes.c_int64 * 7)()
+        sizes = (ctypes.c_int64 * 9)()
         th = ctypes.c_double()
         capi.check(capi.load().sctlgpu_treecode_info(self._h, sizes, ctypes.byref(th)), "sctlgpu_treecode_info")
         d = dict(zip(_SIZE_KEYS, list(sizes)))
@@ -97,27 +99,30 @@ class Treecode:
             pass
 
 
-def layout(kernel, r_src, r_trg, digits: int = 10, order=0, theta=0.0, leaf_max=0, batch_max=0):
+def layout(kernel, r_src, r_trg, digits: int = 10, order=0, theta=0.0, leaf_max=0, batch_max=0, dual=True):
     """The host-only part of Treecode (no device): sizes, blocks (rows of src_begin, src_count,
-    trg_begin, trg_count over slots and sorted targets), the source of every slot (-1 padding,
-    -2 proxy), the target order, and per approximated cluster (slot begin, end, proxy begin, end)."""
+    trg_begin, trg_count; sources index the source slots, targets the target list of sorted
+    targets then target proxies), the source of every slot (-1 padding, -2 proxy), the target
+    order, per source cluster with proxies (slot begin, end, proxy begin, end) and per target
+    cluster with proxies (target begin, end, proxy begin, end)."""
     k = capi.KERNEL_IDS[kernel] if isinstance(kernel, str) else int(kernel)
     xs, xt = _host(r_src), _host(r_trg)
     ns, nt = xs.size // 3, xt.size // 3
     lib = capi.load()
-    prm = _params(order, theta, leaf_max, batch_max)
-    sizes = (ctypes.c_int64 * 7)()
+    prm = _params(order, theta, leaf_max, batch_max, dual)
+    sizes = (ctypes.c_int64 * 9)()
     th = ctypes.c_double()
     args = (k, ns, xs.ctypes.data if ns else None, nt, xt.ctypes.data if nt else None, ctypes.byref(prm), int(digits))
-    capi.check(lib.sctlgpu_treecode_layout(*args, sizes, ctypes.byref(th), None, None, None, None),
+    capi.check(lib.sctlgpu_treecode_layout(*args, sizes, ctypes.byref(th), None, None, None, None, None),
                "sctlgpu_treecode_layout")
     s = dict(zip(_SIZE_KEYS, list(sizes)))
     blocks = np.zeros((s["blocks"], 4), np.int64)
     slot_src = np.zeros(s["slots"], np.int64)
     trg_order = np.zeros(nt, np.int64)
     clusters = np.zeros((s["clusters"], 4), np.int64)
+    tclusters = np.zeros((s["target_clusters"], 4), np.int64)
     p = lambda a: a.ctypes.data if a.size else None  # noqa: E731
     capi.check(lib.sctlgpu_treecode_layout(*args, sizes, ctypes.byref(th), p(blocks), p(slot_src), p(trg_order),
-                                           p(clusters)), "sctlgpu_treecode_layout")
+                                           p(clusters), p(tclusters)), "sctlgpu_treecode_layout")
     s["theta"] = th.value
-    return s, blocks, slot_src, trg_order, clusters
+    return s, blocks, slot_src, trg_order, clusters, tclusters

@@ -1,11 +1,13 @@
 """The treecode's host side (sctlgpu_treecode_layout, no device): trees, slot layout and
 interaction blocks.  Properties checked on clustered and surface point sets:
 
-* every target batch sees every source exactly once -- directly (a leaf's slots) or through
-  the proxies of exactly one approximated cluster containing it;
-* batches partition the targets, and the target order is a permutation;
-* approximated clusters satisfy the acceptance test against their batches and hold more
-  sources than proxy slots;
+* every (target, source) pair is covered exactly once -- directly, through the proxies of a
+  source cluster, through the proxies of a target cluster (later interpolated to its
+  targets), or both -- with and without target-side proxies;
+* the target order is a permutation and the target list is the targets then the target
+  clusters' proxies;
+* approximated pairs of clusters satisfy the acceptance test, and clusters with proxies hold
+  more points than proxies;
 * every block starts and ends on a pair boundary (one pairing of the slot list serves all
   blocks), padding slots are the only sources missing from the slot list.
 """
@@ -39,57 +41,75 @@ def _box(p):
 
 @pytest.mark.parametrize("kind", ["sphere_ball", "clusters", "sheet"])
 @pytest.mark.parametrize("kernel", [0, 3])
-def test_layout_covers_every_source_once(kind, kernel):
+@pytest.mark.parametrize("dual", [True, False])
+def test_layout_covers_every_pair_once(kind, kernel, dual):
     ns, nt = 12000, 3000
     xs, xt = _points(kind, ns, nt, 3)
     order, theta = 3, 0.6
-    s, blocks, slot_src, trg_order, clusters = TC.layout(kernel, xs, xt, order=order, theta=theta, leaf_max=96,
-                                                         batch_max=64)
+    s, blocks, slot_src, trg_order, clusters, tclusters = TC.layout(kernel, xs, xt, order=order, theta=theta,
+                                                                    leaf_max=96, batch_max=64, dual=dual)
     npts = (order + 1) ** 3
     per_point = 3 if kernel == 3 else 1
     assert s["order"] == order and s["theta"] == theta
     assert s["clusters"] > 0 and s["proxy_interactions"] > 0, "the test geometry must exercise the proxies"
+    if not dual:
+        assert s["target_clusters"] == 0
     nsrc = s["source_slots"]
     real = slot_src[:nsrc]
     assert np.array_equal(np.sort(real[real >= 0]), np.arange(ns))
     assert np.all(slot_src[nsrc:] == -2)
     assert np.array_equal(np.sort(trg_order), np.arange(nt))
+    assert s["target_list"] == nt + npts * s["target_clusters"]
     assert np.all(blocks[:, 0] % 2 == 0) and np.all(blocks[:, 1] % 2 == 0)
-    pstart = {int(c[2]): c for c in clusters}
     assert np.all(clusters[:, 3] - clusters[:, 2] == (npts * per_point + 1) // 2 * 2)
-    batches = {}
+    assert np.all(tclusters[:, 3] - tclusters[:, 2] == npts) and np.all(tclusters[:, 1] - tclusters[:, 0] > npts)
+    sprox = {int(c[2]): c for c in clusters}
+    tprox = {int(c[2]): c for c in tclusters}
+    cnt = np.zeros((nt, ns), np.uint8)  # (sorted target, source) coverage
+    direct = approx = 0
     for b in blocks:
-        batches.setdefault((int(b[2]), int(b[3])), []).append(b)
-    t_ranges = sorted(batches)
-    assert t_ranges[0][0] == 0 and sum(n for _, n in t_ranges) == nt
-    for (a, n), (a2, _) in zip(t_ranges, t_ranges[1:]):
-        assert a + n == a2
-    pp = pc = 0
-    for (t0, tn), bl in batches.items():
-        cnt = np.zeros(ns, np.int64)
-        cb, rb = _box(xt[trg_order[t0:t0 + tn]])
-        for b in bl:
-            s0, sn = int(b[0]), int(b[1])
-            if s0 < nsrc:
-                assert s0 + sn <= nsrc
-                src = slot_src[s0:s0 + sn]
-                np.add.at(cnt, src[src >= 0], 1)
-                pp += sn * tn
-            else:
-                pos = s0
-                while pos < s0 + sn:  # merged proxy ranges of adjacent clusters
-                    c = pstart[pos]
-                    src = slot_src[c[0]:c[1]]
-                    src = src[src >= 0]
-                    assert src.size > npts * per_point
-                    np.add.at(cnt, src, 1)
-                    cc, rc = _box(xs[src])
-                    assert rb + rc < theta * np.linalg.norm(cb - cc) * (1 + 1e-12)
-                    pos = int(c[3])
-                assert pos == s0 + sn
-                pc += sn * tn
-        assert np.all(cnt == 1), (kind, np.unique(cnt))
-    assert pp == s["direct_interactions"] and pc == s["proxy_interactions"]
+        s0, sn, t0, tn = (int(v) for v in b)
+        if t0 < nt:
+            assert t0 + tn <= nt
+            ta, tb_ = t0, t0 + tn
+        else:
+            c = tprox[t0]
+            assert tn == npts
+            ta, tb_ = int(c[0]), int(c[1])
+        tset = np.arange(ta, tb_)
+        if s0 < nsrc:
+            assert s0 + sn <= nsrc
+            src = slot_src[s0:s0 + sn]
+            groups = [src[src >= 0]]
+        else:
+            groups, pos = [], s0
+            while pos < s0 + sn:  # merged proxy ranges of adjacent clusters
+                c = sprox[pos]
+                src = slot_src[c[0]:c[1]]
+                groups.append(src[src >= 0])
+                assert groups[-1].size > npts * per_point
+                pos = int(c[3])
+            assert pos == s0 + sn
+        for g in groups:
+            cnt[np.ix_(tset, g)] += 1
+            if t0 >= nt or s0 >= nsrc:  # approximated: the two boxes are separated
+                cb, rb = _box(xt[trg_order[tset]])
+                cc, rc = _box(xs[g])
+                assert rb + rc < theta * np.linalg.norm(cb - cc) * (1 + 1e-12)
+        if t0 < nt and s0 < nsrc:
+            direct += sn * tn
+        else:
+            approx += sn * tn
+    assert cnt.min() == 1 and cnt.max() == 1, (kind, dual)
+    assert direct == s["direct_interactions"] and approx == s["proxy_interactions"]
+
+
+def test_dual_layout_uses_target_proxies_and_saves_work():
+    xs, xt = _points("clusters", 20000, 20000, 5)
+    a = TC.layout(1, xs, xt, order=3, theta=0.6, leaf_max=96, batch_max=64, dual=True)[0]
+    b = TC.layout(1, xs, xt, order=3, theta=0.6, leaf_max=96, batch_max=64, dual=False)[0]
+    assert a["target_clusters"] > 0
+    assert a["direct_interactions"] + a["proxy_interactions"] < b["direct_interactions"] + b["proxy_interactions"]
 
 
 def test_layout_defaults_follow_digits():
@@ -100,7 +120,7 @@ def test_layout_defaults_follow_digits():
 
 def test_layout_and_create_reject_bad_arguments():
     xs, xt = _points("clusters", 500, 100, 2)
-    for kw in ({"order": 16}, {"theta": 1.0}):
+    for kw in ({"order": 16}, {"theta": 1.0}, {"batch_max": 4096}):
         with pytest.raises(capi.SctlGpuError) as e:
             TC.layout(1, xs, xt, **kw)
         assert e.value.status == capi.ERR_INVALID_ARGUMENT
@@ -120,8 +140,8 @@ def test_layout_and_create_reject_bad_arguments():
 
 def test_layout_empty_and_single_leaf():
     xs, xt = _points("clusters", 50, 20, 4)
-    s, blocks, slot_src, trg_order, clusters = TC.layout(0, xs, xt, order=4, leaf_max=64)
-    assert s["clusters"] == 0 and s["proxy_interactions"] == 0
+    s, blocks, slot_src, trg_order, clusters, tclusters = TC.layout(0, xs, xt, order=4, leaf_max=64)
+    assert s["clusters"] == 0 and s["target_clusters"] == 0 and s["proxy_interactions"] == 0
     assert s["direct_interactions"] == 20 * s["source_slots"]
     s, blocks, *_ = TC.layout(0, np.zeros((0, 3)), xt)
     assert s["blocks"] == 0 and s["slots"] == 0
