@@ -718,7 +718,7 @@ struct sctlgpu_treecode_s {
   bool df = false;  // moments and downward pass in double-float (plans in FP32 or double-float arithmetic)
   int device = 0, batch_max = 0;
   TcLayout L;
-  int64_t ns = 0, nt = 0, n_items = 0;
+  int64_t ns = 0, nt = 0, n_items = 0, n_pieces = 0;
   double *d_trg = nullptr, *d_r = nullptr, *d_n = nullptr, *d_v = nullptr, *d_part = nullptr, *d_u = nullptr;
   int64_t *d_slot_src = nullptr, *d_tperm = nullptr, *d_bt0 = nullptr;
   int32_t *d_btn = nullptr, *d_anc_ptr = nullptr, *d_anc = nullptr;
@@ -901,12 +901,20 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
     }
     hb.push_back(tb);
   }
+  // downward-pass work: every batch in pieces of <= batch_max targets (a leaf of coincident
+  // targets can hold more), each with the batch's list of target clusters
   std::vector<int64_t> hbt0;
-  std::vector<int32_t> hbtn;
-  for (int32_t b : L.batches) {
-    hbt0.push_back(L.trg[b].b);
-    hbtn.push_back((int32_t)(L.trg[b].e - L.trg[b].b));
+  std::vector<int32_t> hbtn, hanc_ptr{0}, hanc;
+  for (size_t bi = 0; bi < L.batches.size(); ++bi) {
+    const TcNode& B = L.trg[L.batches[bi]];
+    for (int64_t off = B.b; off < B.e; off += T->batch_max) {
+      hbt0.push_back(off);
+      hbtn.push_back((int32_t)std::min<int64_t>(T->batch_max, B.e - off));
+      for (int32_t a = L.anc_ptr[bi]; a < L.anc_ptr[bi + 1]; ++a) hanc.push_back(L.anc[a]);
+      hanc_ptr.push_back((int32_t)hanc.size());
+    }
   }
+  T->n_pieces = (int64_t)hbt0.size();
   cudaError_t e = cudaSuccess;
   auto up = [&](void** dst, const void* src, size_t bytes) {
     if (e != cudaSuccess) return;
@@ -924,8 +932,8 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   up((void**)&T->d_boxes, hb.data(), hb.size() * sizeof(TcTrgBox));
   up((void**)&T->d_bt0, hbt0.data(), hbt0.size() * sizeof(int64_t));
   up((void**)&T->d_btn, hbtn.data(), hbtn.size() * sizeof(int32_t));
-  up((void**)&T->d_anc_ptr, L.anc_ptr.data(), L.anc_ptr.size() * sizeof(int32_t));
-  up((void**)&T->d_anc, L.anc.data(), L.anc.size() * sizeof(int32_t));
+  up((void**)&T->d_anc_ptr, hanc_ptr.data(), hanc_ptr.size() * sizeof(int32_t));
+  up((void**)&T->d_anc, hanc.data(), hanc.size() * sizeof(int32_t));
   if (e == cudaSuccess)
     e = cudaMalloc((void**)&T->d_part, std::max<size_t>(16, (size_t)T->n_items * npts * Q * sizeof(double)));
   if (e == cudaSuccess) e = cudaMalloc((void**)&T->d_u, std::max<size_t>(16, (size_t)NT * td * sizeof(double)));
@@ -1005,7 +1013,7 @@ int sctlgpu_treecode_execute(sctlgpu_treecode T, const double* v_src, double* v_
   int rc = sctlgpu_near_plan_execute(T->plan, T->d_trg, T->d_r, T->d_n, T->d_v, nullptr, T->d_u, SCTLGPU_DEVICE_PTRS,
                                      stream);
   if (rc) return rc;
-  e = tc_launch_l2p(q, T->TD, T->df, (int)L.batches.size(), T->batch_max, st);
+  e = tc_launch_l2p(q, T->TD, T->df, (int)T->n_pieces, T->batch_max, st);
   return e == cudaSuccess ? SCTLGPU_OK : runtime_record(e);
 }
 

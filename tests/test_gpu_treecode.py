@@ -81,6 +81,24 @@ def test_treecode_accumulate_and_new_densities(cuda):
     assert float((u3 - (2 * u1 - u2)).norm() / u3.norm()) < 1e-12
 
 
+def test_treecode_coincident_targets_and_particle_cluster_form(cuda):
+    """3000 coincident targets (one leaf above batch_max: the downward pass works in pieces),
+    with the dual traversal and with the particle-cluster form."""
+    torch = cuda
+    k = 1
+    d = W.sphere_ball(1 << 17, 1 << 13, k, seed=21)
+    xt = d["r_trg"].copy()
+    xt[:3000] = xt[0]
+    sub = np.r_[0:5, 2990:3010, np.arange(3010, 1 << 13, 64)]
+    ref = O.eval(k, xt[sub], d["r_src"], d["n_src"], d["v_src"])
+    for dual in (True, False):
+        tc = TC.Treecode(k, d["r_src"], xt, n_src=d["n_src"], digits=10, dual=dual)
+        assert tc.info()["proxy_interactions"] > 0
+        u = tc.eval(dev(torch, d["v_src"])).cpu().numpy()
+        assert O.rel_l2(u[sub], ref) < 1e-10, dual
+        assert np.abs(u[:3000] - u[0]).max() <= 1e-12 * abs(u[0])
+
+
 def test_treecode_single_leaf_is_the_direct_sum(cuda):
     """One leaf, FP64 arithmetic: the treecode is the direct sum up to summation order."""
     torch = cuda
