@@ -138,33 +138,26 @@ __device__ __forceinline__ void fma_acc(d2& acc, d2 a, d2 b) {
 }  // namespace pdfq
 
 // Per-warp shared state of the double-float kernel.  All boxes of one round
-// have the same size (2^-depth), so only their corners are queued; the
-// weights-mode arrays exist only in the weights-mode layout (smaller footprint
-// = more resident warps for the potential mode).
-struct PanelWarpSmemDF {
-  f2 F[4][PQ_NODES];          // x_s - x_t (3 components) and sigma at the panel nodes
-  f2 Ls[PQ_GL][PQ_P], Lds[PQ_GL][PQ_P], Lt[PQ_GL][PQ_P], Ldt[PQ_GL][PQ_P];
-  f2 A[7][PQ_GL][PQ_P];
+// have the same size (2^-depth), so only their corners are queued.  Gauss rows
+// i and i + 4 of a box sit side by side (lane x, lane y) so that one lane
+// integrates two nodes with f32x2 arithmetic and one 16-byte shared load per
+// operand pair; the weights-mode arrays exist only in the weights-mode layout
+// (smaller footprint = more resident warps for the potential mode).
+struct PanelWarpSmemDFP {
+  f2 F[4][PQ_NODES];  // x_s - x_t (3 components) and sigma at the panel nodes
+  pdfq::d2 LsP[PQ_GL / 2][PQ_P], LdsP[PQ_GL / 2][PQ_P];  // basis and derivative along s, rows paired
+  f2 Lt[PQ_GL][PQ_P], Ldt[PQ_GL][PQ_P];                  // along t
+  pdfq::d2 AP[7][PQ_GL / 2][PQ_P];                        // L_s F (x,y,z,sigma) and L_s' F (x,y,z)
   float box[2][PQ_QUEUE][2];  // (s0, t0) of the boxes of this and the next round (dyadic: exact)
 };
-struct PanelWarpSmemDFW : PanelWarpSmemDF {
+// Weights mode: K dA at the box's Gauss nodes, Kd . L_t, and the panel's 100 accumulated weights.
+struct PanelWarpSmemDFPW : PanelWarpSmemDFP {
   f2 Kd[PQ_GL][PQ_GL];
   f2 T[PQ_GL][PQ_P];
   f2 W[PQ_NODES];
 };
-// Potential-mode layout: Gauss rows i and i + 4 side by side (lane x, lane y)
-// so that one lane integrates two nodes with f32x2 arithmetic and one 16-byte
-// shared load per operand pair.  Same footprint as PanelWarpSmemDF.
-struct PanelWarpSmemDFP {
-  f2 F[4][PQ_NODES];
-  pdfq::d2 LsP[PQ_GL / 2][PQ_P], LdsP[PQ_GL / 2][PQ_P];
-  f2 Lt[PQ_GL][PQ_P], Ldt[PQ_GL][PQ_P];
-  pdfq::d2 AP[7][PQ_GL / 2][PQ_P];
-  float box[2][PQ_QUEUE][2];
-};
-static_assert(sizeof(PanelWarpSmemDFP) == sizeof(PanelWarpSmemDF), "packed layout keeps the footprint");
 template <bool WEIGHTS>
-using DFSmem = typename std::conditional<WEIGHTS, PanelWarpSmemDFW, PanelWarpSmemDFP>::type;
+using DFSmem = typename std::conditional<WEIGHTS, PanelWarpSmemDFPW, PanelWarpSmemDFP>::type;
 
 __constant__ float c_gl_xh[PQ_GL], c_gl_xl[PQ_GL];        // Gauss-Legendre nodes, double-float
 __constant__ float c_gl_wh[PQ_GL], c_gl_wl[PQ_GL];        // and weights
@@ -217,9 +210,8 @@ __device__ __forceinline__ void basis_df(f2 s, f2 (&l)[PQ_P], f2 (&d)[PQ_P]) {
 // and r + 4 of the box's 8 x 8 rule in lanes x and y of f32x2 operations, each
 // lane with the same roundings as the scalar form.  acc gathers the lane's
 // two node sums.
-template <int KER>
-__device__ __forceinline__ void leaf_potential_pk(PanelWarpSmemDFP& sm, int lane, float bs, float bt, float bz,
-                                                  pdfq::d2& acc) {
+template <int KER, bool WEIGHTS, class SM>
+__device__ __forceinline__ void leaf_pk(SM& sm, int lane, float bs, float bt, float bz, pdfq::d2& acc) {
   constexpr int H = PQ_GL / 2;
   if (lane < 2 * PQ_GL) {
     const int i = lane % PQ_GL;
@@ -248,6 +240,7 @@ __device__ __forceinline__ void leaf_potential_pk(PanelWarpSmemDFP& sm, int lane
   __syncwarp();
   for (int e = lane; e < 7 * H * PQ_P; e += 32) {
     const int m = e / (H * PQ_P), r = (e / PQ_P) % H, b = e % PQ_P;
+    if (WEIGHTS && m == 3) continue;  // no density in weights mode
     const int c = m < 4 ? m : m - 4;
     const pdfq::d2* L = m < 4 ? sm.LsP[r] : sm.LdsP[r];
     pdfq::d2 v = {};
@@ -268,7 +261,7 @@ __device__ __forceinline__ void leaf_potential_pk(PanelWarpSmemDFP& sm, int lane
       pdfq::fma_acc(Xt[c], ac, ldt);
       pdfq::fma_acc(Xs[c], sm.AP[4 + c][r][b], lt);
     }
-    pdfq::fma_acc(sg, sm.AP[3][r][b], lt);
+    if (!WEIGHTS) pdfq::fma_acc(sg, sm.AP[3][r][b], lt);
   }
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
@@ -308,8 +301,34 @@ __device__ __forceinline__ void leaf_potential_pk(PanelWarpSmemDFP& sm, int lane
     y3.l = pdfq::vfma(y3.h, pdfq::vmul(pdfq::dup(1.5f), rho), y3.l);
     kda = mul(mul(rn, y3), w);
   }
-  pdfq::fma_acc(acc, kda, pdfq::norm(sg));
-  acc = pdfq::norm(acc);
+  if constexpr (WEIGHTS) {
+    const pdfq::d2 k = pdfq::norm(kda);
+    sm.Kd[r][j] = {k.h.x, k.l.x};
+    sm.Kd[r + H][j] = {k.h.y, k.l.y};
+    __syncwarp();
+    for (int e = lane; e < PQ_GL * PQ_P; e += 32) {  // T = Kd . L_t
+      const int i = e / PQ_P, b = e % PQ_P;
+      f2 v = {0.f, 0.f};
+#pragma unroll
+      for (int jj = 0; jj < PQ_GL; ++jj) dfq::fma_acc(v, sm.Kd[i][jj], sm.Lt[jj][b]);
+      sm.T[i][b] = dfq::norm(v);
+    }
+    __syncwarp();
+    for (int e = lane; e < PQ_NODES; e += 32) {  // W += L_s^T T, rows i and i + 4 from one packed entry
+      const int a = e / PQ_P, b = e % PQ_P;
+      f2 v = sm.W[e];
+#pragma unroll
+      for (int i = 0; i < H; ++i) {
+        const pdfq::d2 ls = sm.LsP[i][a];
+        dfq::fma_acc(v, {ls.h.x, ls.l.x}, sm.T[i][b]);
+        dfq::fma_acc(v, {ls.h.y, ls.l.y}, sm.T[i + H][b]);
+      }
+      sm.W[e] = dfq::norm(v);
+    }
+  } else {
+    pdfq::fma_acc(acc, kda, pdfq::norm(sg));
+    acc = pdfq::norm(acc);
+  }
 }
 
 template <int KER, bool WEIGHTS>
@@ -363,102 +382,8 @@ __global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParam
         for (unsigned mk = acc_mask; mk; mk &= mk - 1u) {
           const int src = __ffs(mk) - 1;
           const float bs = __shfl_sync(0xffffffffu, lbs, src), bt = __shfl_sync(0xffffffffu, lbt, src);
-          if constexpr (!WEIGHTS) {
-            leaf_potential_pk<KER>(sm, lane, bs, bt, bz, acc);
-            __syncwarp();
-          } else {
-            if (lane < 2 * PQ_GL) {
-              const int i = lane % PQ_GL;
-              // s = b0 + bz * g_i (b0, bz dyadic: exact floats)
-              const f2 g = {c_gl_xh[i], c_gl_xl[i]};
-              const f2 s = dfq::add({lane < PQ_GL ? bs : bt, 0.f}, dfq::mulf(g, bz));
-              f2 l[PQ_P], d[PQ_P];
-              basis_df(s, l, d);
-    #pragma unroll
-              for (int a = 0; a < PQ_P; ++a) {
-                if (lane < PQ_GL) {
-                  sm.Ls[i][a] = l[a];
-                  sm.Lds[i][a] = d[a];
-                } else {
-                  sm.Lt[i][a] = l[a];
-                  sm.Ldt[i][a] = d[a];
-                }
-              }
-            }
-            __syncwarp();
-            for (int e = lane; e < 7 * PQ_GL * PQ_P; e += 32) {
-              const int m = e / (PQ_GL * PQ_P), i = (e / PQ_P) % PQ_GL, b = e % PQ_P;
-              if (m == 3) continue;  // no density in weights mode
-              const int c = m < 4 ? m : m - 4;
-              const f2* L = m < 4 ? sm.Ls[i] : sm.Lds[i];
-              f2 v = {0.f, 0.f};
-    #pragma unroll
-              for (int a = 0; a < PQ_P; ++a) dfq::fma_acc(v, L[a], sm.F[c][a * PQ_P + b]);
-              sm.A[m][i][b] = dfq::norm(v);
-            }
-            __syncwarp();
-            const float bz2 = bz * bz;
-            for (int gq = lane; gq < PQ_GL * PQ_GL; gq += 32) {
-              const int i = gq / PQ_GL, j = gq % PQ_GL;
-              f2 X[3] = {}, Xs[3] = {}, Xt[3] = {};
-    #pragma unroll 2
-              for (int b = 0; b < PQ_P; ++b) {
-                const f2 lt = sm.Lt[j][b], ldt = sm.Ldt[j][b];
-    #pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                  dfq::fma_acc(X[c], sm.A[c][i][b], lt);
-                  dfq::fma_acc(Xt[c], sm.A[c][i][b], ldt);
-                  dfq::fma_acc(Xs[c], sm.A[4 + c][i][b], lt);
-                }
-              }
-    #pragma unroll
-              for (int c = 0; c < 3; ++c) {
-                X[c] = dfq::norm(X[c]);  // X = x_s - x_t = -r
-                Xs[c] = dfq::norm(Xs[c]);
-                Xt[c] = dfq::norm(Xt[c]);
-              }
-              // unnormalised normal n = Xs x Xt (|n| = area element of the parameter square)
-              const f2 n0 = dfq::sub(dfq::mul(Xs[1], Xt[2]), dfq::mul(Xs[2], Xt[1]));
-              const f2 n1 = dfq::sub(dfq::mul(Xs[2], Xt[0]), dfq::mul(Xs[0], Xt[2]));
-              const f2 n2 = dfq::sub(dfq::mul(Xs[0], Xt[1]), dfq::mul(Xs[1], Xt[0]));
-              f2 R = dfq::add(dfq::add(dfq::mul(X[0], X[0]), dfq::mul(X[1], X[1])), dfq::mul(X[2], X[2]));
-              float rho, y0;
-              const f2 y = dfq::rsqrt(R, &rho, &y0);
-              const f2 w = dfq::mulf(dfq::mul({c_gl_wh[i], c_gl_wl[i]}, {c_gl_wh[j], c_gl_wl[j]}), bz2);
-              f2 kda;
-              if (KER == 0) {  // single layer: |n| / r
-                const f2 J2 = dfq::add(dfq::add(dfq::mul(n0, n0), dfq::mul(n1, n1)), dfq::mul(n2, n2));
-                const float jh = sqrtf(J2.h);
-                const f2 jp = two_prod(jh, jh);
-                const f2 J = dfq::norm({jh, jh > 0.f ? ((J2.h - jp.h - jp.l) + J2.l) / (2.f * jh) : 0.f});
-                kda = dfq::mul(dfq::mul(J, y), w);
-              } else {  // double layer: (r . n) / r^3 with r = -X
-                const f2 rn = dfq::neg(
-                    dfq::add(dfq::add(dfq::mul(X[0], n0), dfq::mul(X[1], n1)), dfq::mul(X[2], n2)));
-                f2 y3 = dfq::mulf(two_prod(y0, y0), y0);  // y0^3 (1 + 3 rho / 2)
-                y3.l = fmaf(y3.h, 1.5f * rho, y3.l);
-                kda = dfq::mul(dfq::mul(rn, y3), w);
-              }
-              sm.Kd[i][j] = dfq::norm(kda);
-            }
-            __syncwarp();
-            for (int e = lane; e < PQ_GL * PQ_P; e += 32) {
-              const int i = e / PQ_P, b = e % PQ_P;
-              f2 v = {0.f, 0.f};
-  #pragma unroll
-              for (int j = 0; j < PQ_GL; ++j) dfq::fma_acc(v, sm.Kd[i][j], sm.Lt[j][b]);
-              sm.T[i][b] = dfq::norm(v);
-            }
-            __syncwarp();
-            for (int e = lane; e < PQ_NODES; e += 32) {
-              const int a = e / PQ_P, b = e % PQ_P;
-              f2 v = sm.W[e];
-  #pragma unroll
-              for (int i = 0; i < PQ_GL; ++i) dfq::fma_acc(v, sm.Ls[i][a], sm.T[i][b]);
-              sm.W[e] = dfq::norm(v);
-            }
-            __syncwarp();
-          }
+          leaf_pk<KER, WEIGHTS>(sm, lane, bs, bt, bz, acc);
+          __syncwarp();
         }
       };
       for (int base = 0; base < ncur; base += 32) {

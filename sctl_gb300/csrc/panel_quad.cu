@@ -513,7 +513,7 @@ int launch_panel(int kernel, bool weights, const PanelParams& p0, unsigned grid,
 
 int launch_panel_kernels(int kernel, bool weights, const PanelParams& p, unsigned grid, int dev, cudaStream_t st) {
   const size_t smem = PQ_WARPS * sizeof(PanelWarpSmem);
-  const size_t smem_p = PQ_WARPS * sizeof(PanelWarpSmemDF), smem_w = PQ_WARPS * sizeof(PanelWarpSmemDFW);
+  const size_t smem_p = PQ_WARPS * sizeof(DFSmem<false>), smem_w = PQ_WARPS * sizeof(DFSmem<true>);
   static bool attr[64] = {};
   if (!attr[dev]) {
     cudaFuncSetAttribute(panel_near_kernel<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
