@@ -307,6 +307,7 @@ typedef struct sctlgpu_treecode_params {
   int batch_max; /* targets per batch, <= 2048; <= 0: 512 */
   int dual;      /* nonzero: target clusters interpolate too (cluster-cluster interactions, a downward pass);
                     0: particle-cluster only */
+  double theta_trg; /* acceptance of target-side interpolation, <= theta; <= 0: theta */
 } sctlgpu_treecode_params;
 typedef struct sctlgpu_treecode_s* sctlgpu_treecode;
 int sctlgpu_treecode_create(sctlgpu_treecode* tc, int kernel, int mode, int digits, int64_t ns, const double* r_src,

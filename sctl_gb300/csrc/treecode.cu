@@ -127,16 +127,24 @@ void build_octree(const double* X, int64_t n, int64_t leaf_max, std::vector<int6
   }
 }
 
-// Interpolation box of a cluster: its tight box, every side at least 1e-3 of
-// the longest one (a flat cluster keeps a well-posed tensor grid), centred.
-void interp_box(const TcNode& C, double lo[3], double ext[3]) {
-  double emax = 0;
-  for (int d = 0; d < 3; ++d) emax = std::max(emax, C.hi[d] - C.lo[d]);
-  if (emax <= 0) emax = 1e-3 * std::max(1.0, std::fabs(C.c[0]) + std::fabs(C.c[1]) + std::fabs(C.c[2]));
+// Interpolation box of a cluster: exactly its tight box, so every proxy lies
+// inside the bounding box of the input points.  That keeps the mixed-precision
+// frame of the plan (derived from the bounding box of everything it sees)
+// identical to the frame of any other plan or direct sum over the same sources
+// and targets, so that terms a caller subtracts later (the smooth-rule
+// correction of near panels) cancel term by term.  A side of zero extent maps
+// every point to t = -1 (inv = 0): all weight on the proxies at that coordinate.
+void interp_box(const TcNode& C, double lo[3], double inv[3]) {
   for (int d = 0; d < 3; ++d) {
-    ext[d] = std::max(C.hi[d] - C.lo[d], 1e-3 * emax);
-    lo[d] = C.c[d] - 0.5 * ext[d];
+    lo[d] = C.lo[d];
+    const double ext = C.hi[d] - C.lo[d];
+    inv[d] = ext > 0 ? 2.0 / ext : 0.0;
   }
+}
+// Coordinate of Chebyshev point x in [-1, 1] on [lo, hi], with both ends exact
+// and every point inside [lo, hi].
+double cheb_coord(double lo, double hi, double x) {
+  return x >= 0 ? hi - 0.5 * (1.0 - x) * (hi - lo) : lo + 0.5 * (1.0 + x) * (hi - lo);
 }
 
 struct TcLayout {
@@ -154,6 +162,7 @@ struct TcLayout {
   std::vector<sctlgpu_block> blocks;
   int64_t pp = 0, approx = 0;     // interactions of the direct blocks and of the proxy blocks
   bool dual = true;
+  double theta_trg = 0;  // acceptance for target-side interpolation (<= theta)
   double xcheb[TC_MAX_NP], wcheb[TC_MAX_NP];
 };
 
@@ -169,10 +178,11 @@ void tc_defaults(int digits, int* order, double* theta) {
 }
 
 int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, const double* r_trg, int order,
-                    double theta, int64_t leaf_max, int64_t batch_max, bool dual, TcLayout& L) {
+                    double theta, double theta_trg, int64_t leaf_max, int64_t batch_max, bool dual, TcLayout& L) {
   if (order < 1 || order >= TC_MAX_NP || !(theta > 0) || theta >= 1.0) return SCTLGPU_ERR_INVALID_ARGUMENT;
-  if (batch_max > TC_MAX_BATCH) return SCTLGPU_ERR_INVALID_ARGUMENT;
+  if (batch_max > TC_MAX_BATCH || theta_trg > theta) return SCTLGPU_ERR_INVALID_ARGUMENT;
   L.dual = dual;
+  L.theta_trg = theta_trg > 0 ? theta_trg : theta;
   L.order = order;
   L.np = order + 1;
   L.npts = L.np * L.np * L.np;
@@ -243,7 +253,8 @@ int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, con
     const double dist = std::sqrt(dx * dx + dy * dy + dz * dz);
     const int64_t nT = T.e - T.b, nS = S.e - S.b, sS = S.se - S.sb;
     if (T.r + S.r < theta * dist) {
-      const bool src_ok = nS > Ps, trg_ok = L.dual && nT > Pt;
+      // target-side interpolation (a target cluster's proxies) only under the stricter theta_trg
+      const bool src_ok = nS > Ps, trg_ok = L.dual && nT > Pt && T.r + S.r < L.theta_trg * dist;
       double best = (double)nT * sS;
       char kind = 0;
       if (src_ok && (double)nT * Ps < best) best = (double)nT * Ps, kind = 1;
@@ -757,8 +768,8 @@ int tc_layout_from(int kernel, int digits, int64_t ns, const double* r_src, int6
   tc_defaults(digits, &order, &theta);
   const int bm = prm && prm->batch_max > 0 ? prm->batch_max : 512;
   if (batch_max) *batch_max = bm;
-  return tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, prm ? prm->leaf_max : 0, bm,
-                         !prm || prm->dual != 0, L);
+  return tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, prm ? prm->theta_trg : 0.0,
+                         prm ? prm->leaf_max : 0, bm, !prm || prm->dual != 0, L);
 }
 
 void tc_sizes(const TcLayout& L, int64_t* sizes) {
@@ -859,9 +870,7 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   for (int32_t id : L.clusters) {
     const TcNode& C = L.src[id];
     TcCluster tc{};
-    double ext[3];
-    interp_box(C, tc.lo, ext);
-    for (int d = 0; d < 3; ++d) tc.inv[d] = 2.0 / ext[d];
+    interp_box(C, tc.lo, tc.inv);
     tc.proxy = C.proxy;
     tc.item0 = (int32_t)hi.size();
     for (int64_t s0 = C.sb; s0 < C.se; s0 += TC_CHUNK)
@@ -872,7 +881,7 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
       const int i = pt / (L.np * L.np), j = (pt / L.np) % L.np, l = pt % L.np;
       const int64_t slot = C.proxy + k;
       const double g[3] = {L.xcheb[i], L.xcheb[j], L.xcheb[l]};
-      for (int d = 0; d < 3; ++d) hr[slot * 3 + d] = tc.lo[d] + 0.5 * (g[d] + 1.0) * ext[d];
+      for (int d = 0; d < 3; ++d) hr[slot * 3 + d] = cheb_coord(C.lo[d], C.hi[d], g[d]);
       const bool real = k < L.npts * L.per_point;
       if (kernel == SCTLGPU_LAPLACE3D_DXU && real) hv[slot] = 1.0;  // the moment is the proxy's normal
       if (kernel == SCTLGPU_STOKES3D_DXU && real) hn[slot * 3 + k % 3] = 1.0;  // normal e_c
@@ -890,14 +899,12 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   for (int32_t id : L.tclusters) {
     const TcNode& C = L.trg[id];
     TcTrgBox tb{};
-    double ext[3];
-    interp_box(C, tb.lo, ext);
-    for (int d = 0; d < 3; ++d) tb.inv[d] = 2.0 / ext[d];
+    interp_box(C, tb.lo, tb.inv);
     tb.proxy = C.proxy;
     for (int k = 0; k < L.npts; ++k) {
       const int i = k / (L.np * L.np), j = (k / L.np) % L.np, l = k % L.np;
       const double g[3] = {L.xcheb[i], L.xcheb[j], L.xcheb[l]};
-      for (int d = 0; d < 3; ++d) htrg[(C.proxy + k) * 3 + d] = tb.lo[d] + 0.5 * (g[d] + 1.0) * ext[d];
+      for (int d = 0; d < 3; ++d) htrg[(C.proxy + k) * 3 + d] = cheb_coord(C.lo[d], C.hi[d], g[d]);
     }
     hb.push_back(tb);
   }

@@ -29,9 +29,9 @@ def _host(a):
     return np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
 
 
-def _params(order, theta, leaf_max, batch_max, dual=True):
+def _params(order, theta, leaf_max, batch_max, dual=True, theta_trg=0.0):
     return capi.TreecodeParams(float(theta or 0.0), int(order or 0), int(leaf_max or 0), int(batch_max or 0),
-                               1 if dual else 0)
+                               1 if dual else 0, float(theta_trg or 0.0))
 
 
 _SIZE_KEYS = ("blocks", "source_slots", "slots", "clusters", "direct_interactions", "proxy_interactions", "order",
@@ -40,7 +40,7 @@ _SIZE_KEYS = ("blocks", "source_slots", "slots", "clusters", "direct_interaction
 
 class Treecode:
     def __init__(self, kernel, r_src, r_trg, n_src=None, digits: int = 10, mode="mixed", order=0, theta=0.0,
-                 leaf_max=0, batch_max=0, dual=True):
+                 leaf_max=0, batch_max=0, dual=True, theta_trg=0.0):
         self.kernel = capi.KERNEL_IDS[kernel] if isinstance(kernel, str) else int(kernel)
         self.mode = capi.MODE_IDS[mode] if isinstance(mode, str) else int(mode)
         self.digits = int(digits)
@@ -50,7 +50,7 @@ class Treecode:
         self.sd, self.td = sd, td
         lib = capi.load()
         h = ctypes.c_void_p()
-        prm = _params(order, theta, leaf_max, batch_max, dual)
+        prm = _params(order, theta, leaf_max, batch_max, dual, theta_trg)
         rc = lib.sctlgpu_treecode_create(ctypes.byref(h), self.kernel, self.mode, self.digits, self.ns,
                                          xs.ctypes.data if xs.size else None,
                                          ns_.ctypes.data if ns_ is not None and ns_.size else None, self.nt,
@@ -99,7 +99,8 @@ class Treecode:
             pass
 
 
-def layout(kernel, r_src, r_trg, digits: int = 10, order=0, theta=0.0, leaf_max=0, batch_max=0, dual=True):
+def layout(kernel, r_src, r_trg, digits: int = 10, order=0, theta=0.0, leaf_max=0, batch_max=0, dual=True,
+           theta_trg=0.0):
     """The host-only part of Treecode (no device): sizes, blocks (rows of src_begin, src_count,
     trg_begin, trg_count; sources index the source slots, targets the target list of sorted
     targets then target proxies), the source of every slot (-1 padding, -2 proxy), the target
@@ -109,7 +110,7 @@ def layout(kernel, r_src, r_trg, digits: int = 10, order=0, theta=0.0, leaf_max=
     xs, xt = _host(r_src), _host(r_trg)
     ns, nt = xs.size // 3, xt.size // 3
     lib = capi.load()
-    prm = _params(order, theta, leaf_max, batch_max, dual)
+    prm = _params(order, theta, leaf_max, batch_max, dual, theta_trg)
     sizes = (ctypes.c_int64 * 9)()
     th = ctypes.c_double()
     args = (k, ns, xs.ctypes.data if ns else None, nt, xt.ctypes.data if nt else None, ctypes.byref(prm), int(digits))

@@ -36,16 +36,21 @@ def test_gauss_law_double_layer(setup):
 
 def test_gauss_law_with_treecode_far_field(setup):
     """The whole evaluation with the far field by the treecode (ParticleFMM::Eval's fast path):
-    Gauss's law as above at 65,536 targets, and within 1e-9 of the direct-far-field evaluation."""
+    Gauss's law at 2^20 targets to 1e-9 (the direct-far-field evaluation reaches 9.2e-10 there),
+    and within 1e-9 of the direct-far-field evaluation.  At this size target clusters carry
+    proxies; their points must stay inside the bounding box of the inputs, or the treecode's
+    mixed-precision frame differs from the subtraction plan's and the near panels' large
+    smooth-rule terms no longer cancel term by term (5.9e-7 here when they did not)."""
     torch, T, S = setup
-    tg = T.targets(1 << 16, seed=15, hmin=1e-4, hmax=1.0)
+    tg = T.targets(1 << 20, seed=15, hmin=1e-4, hmax=1.0)
     xt = torch.from_numpy(tg["r_trg"]).cuda()
     one = torch.ones(T.np * T.p * T.p, dtype=torch.float64, device="cuda")
     pairs = S.near_pairs(xt)
     v = S.evaluate(xt, one, pairs=pairs, far="treecode").cpu().numpy()
-    assert S.treecode(xt).info()["proxy_interactions"] > 0
+    info = S.treecode(xt).info()
+    assert info["proxy_interactions"] > 0 and info["target_clusters"] > 0
     exact = np.where(tg["side"] < 0, -1.0, 0.0)
-    assert np.abs(v - exact).max() < 1e-8
+    assert np.abs(v - exact).max() < 1e-9
     sig = torch.from_numpy(T.sigma.reshape(-1)).cuda()
     a = S.evaluate(xt, sig, pairs=pairs, far="treecode").cpu().numpy()
     b = S.evaluate(xt, sig, pairs=pairs).cpu().numpy()
