@@ -484,6 +484,9 @@ def torus_section(torch, n_eval=1 << 20, n_train=440000, steps=4000, learned=Tru
                           "apply_frac_of_measured_hbm": alg / (apply_ms * 1e-3) / 1e9 / hbm,
                           "evaluate_ms": _ev_ms(torch, lambda: S.evaluate(xt, sig, pairs=pairs, plan=plan, matrix=M),
                                                 reps=2),
+                          "evaluate_treecode_far_ms": _ev_ms(
+                              torch, lambda: S.evaluate(xt, sig, pairs=pairs, plan=plan, matrix=M, far="treecode"),
+                              reps=2),
                           "max_rel_diff_vs_adaptive": ((with_m - plain).abs().max() / plain.abs().max()).item()}
     del M
     if not learned:
