@@ -164,79 +164,87 @@ __constant__ float c_gl_wh[PQ_GL], c_gl_wl[PQ_GL];        // and weights
 __constant__ float c_ch_xh[PQ_P], c_ch_xl[PQ_P];          // Chebyshev nodes, double-float
 __constant__ float c_ch_wh[PQ_P], c_ch_wl[PQ_P];          // barycentric weights, double-float
 
-// Double-float basis and derivative at s (s = bs + bz * g, g a Gauss node).
-__device__ __forceinline__ void basis_df(f2 s, f2 (&l)[PQ_P], f2 (&d)[PQ_P]) {
+// Double-float Lagrange basis and its derivative (barycentric formula, Newton-
+// refined reciprocals) at the 16 points s = b0 + bz * g of a box (8 along s, 8
+// along t; b0, bz dyadic, so exact), spread over the whole warp: two lanes per
+// point, each lane five of the ten terms; the partial sums (and a node hit,
+// where the basis is a unit vector and the derivative a differentiation-matrix
+// row) are exchanged with the partner lane.  Writes
+// the s-rows into the paired layout and the t-rows into Lt / Ldt.
+template <class SM>
+__device__ __forceinline__ void basis_df_warp(SM& sm, int lane, float bs, float bt, float bz) {
+  constexpr int H = PQ_GL / 2, K = PQ_P / 2;
+  const int pt = lane >> 1, a0 = (lane & 1) * K;
+  const int i = pt % PQ_GL;
+  const f2 g = {c_gl_xh[i], c_gl_xl[i]};
+  const f2 s = dfq::add({pt < PQ_GL ? bs : bt, 0.f}, dfq::mulf(g, bz));
   int hit = -1;
 #pragma unroll
-  for (int a = 0; a < PQ_P; ++a)
-    if (s.h == c_ch_xh[a] && s.l == c_ch_xl[a]) hit = a;
+  for (int k = 0; k < K; ++k)
+    if (s.h == c_ch_xh[a0 + k] && s.l == c_ch_xl[a0 + k]) hit = a0 + k;
+  hit = max(hit, __shfl_xor_sync(0xffffffffu, hit, 1));
+  f2 l[K], d[K];
   if (hit >= 0) {  // at a node: l is a unit vector, l' the differentiation-matrix row
     f2 diag = {0.f, 0.f};
     const f2 xh = {c_ch_xh[hit], c_ch_xl[hit]}, iwh = dfq::rcp({c_ch_wh[hit], c_ch_wl[hit]});
 #pragma unroll
-    for (int a = 0; a < PQ_P; ++a) {
-      l[a] = {(a == hit) ? 1.f : 0.f, 0.f};
-      d[a] = {0.f, 0.f};
+    for (int k = 0; k < K; ++k) {
+      const int a = a0 + k;
+      l[k] = {(a == hit) ? 1.f : 0.f, 0.f};
+      d[k] = {0.f, 0.f};
       if (a != hit) {
         const f2 w = dfq::mul({c_ch_wh[a], c_ch_wl[a]}, iwh);
-        d[a] = dfq::mul(w, dfq::rcp(dfq::sub(xh, {c_ch_xh[a], c_ch_xl[a]})));
-        diag = dfq::sub(diag, d[a]);
+        d[k] = dfq::mul(w, dfq::rcp(dfq::sub(xh, {c_ch_xh[a], c_ch_xl[a]})));
+        diag = dfq::sub(diag, d[k]);
       }
     }
+    diag = dfq::add(diag, {__shfl_xor_sync(0xffffffffu, diag.h, 1), __shfl_xor_sync(0xffffffffu, diag.l, 1)});
 #pragma unroll
-    for (int a = 0; a < PQ_P; ++a)
-      if (a == hit) d[a] = diag;
-    return;
+    for (int k = 0; k < K; ++k)
+      if (a0 + k == hit) d[k] = diag;
+  } else {
+    f2 T = {0.f, 0.f}, U = {0.f, 0.f}, r[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int a = a0 + k;
+      r[k] = dfq::rcp(dfq::sub(s, {c_ch_xh[a], c_ch_xl[a]}));
+      const f2 t = dfq::mul({c_ch_wh[a], c_ch_wl[a]}, r[k]);
+      l[k] = t;
+      T = dfq::add(T, t);
+      U = dfq::add(U, dfq::mul(t, r[k]));
+    }
+    T = dfq::add(T, {__shfl_xor_sync(0xffffffffu, T.h, 1), __shfl_xor_sync(0xffffffffu, T.l, 1)});
+    U = dfq::add(U, {__shfl_xor_sync(0xffffffffu, U.h, 1), __shfl_xor_sync(0xffffffffu, U.l, 1)});
+    const f2 iT = dfq::rcp(T), UT = dfq::mul(U, iT);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      l[k] = dfq::mul(l[k], iT);
+      d[k] = dfq::mul(l[k], dfq::sub(UT, r[k]));
+    }
   }
-  f2 T = {0.f, 0.f}, U = {0.f, 0.f}, r[PQ_P];
+  const int rr = i % H, y = i >= H ? 1 : 0;
 #pragma unroll
-  for (int a = 0; a < PQ_P; ++a) {
-    r[a] = dfq::rcp(dfq::sub(s, {c_ch_xh[a], c_ch_xl[a]}));
-    const f2 t = dfq::mul({c_ch_wh[a], c_ch_wl[a]}, r[a]);
-    l[a] = t;
-    T = dfq::add(T, t);
-    U = dfq::add(U, dfq::mul(t, r[a]));
-  }
-  const f2 iT = dfq::rcp(T), UT = dfq::mul(U, iT);
-#pragma unroll
-  for (int a = 0; a < PQ_P; ++a) {
-    l[a] = dfq::mul(l[a], iT);
-    d[a] = dfq::mul(l[a], dfq::sub(UT, r[a]));
+  for (int k = 0; k < K; ++k) {
+    const int a = a0 + k;
+    if (pt < PQ_GL) {
+      // d2 = {h.x, h.y, l.x, l.y}: row i's words sit at offsets y and 2 + y
+      float* ls = reinterpret_cast<float*>(&sm.LsP[rr][a]) + y;
+      float* ld = reinterpret_cast<float*>(&sm.LdsP[rr][a]) + y;
+      ls[0] = l[k].h;
+      ls[2] = l[k].l;
+      ld[0] = d[k].h;
+      ld[2] = d[k].l;
+    } else {
+      sm.Lt[i][a] = l[k];
+      sm.Ldt[i][a] = d[k];
+    }
   }
 }
 
-// One accepted box of size bz at (bs, bt), potential mode: basis values as
-// above, then L_s F and the 64 Gauss nodes with two nodes per lane -- rows r
-// and r + 4 of the box's 8 x 8 rule in lanes x and y of f32x2 operations, each
-// lane with the same roundings as the scalar form.  acc gathers the lane's
-// two node sums.
 template <int KER, bool WEIGHTS, class SM>
 __device__ __forceinline__ void leaf_pk(SM& sm, int lane, float bs, float bt, float bz, pdfq::d2& acc) {
   constexpr int H = PQ_GL / 2;
-  if (lane < 2 * PQ_GL) {
-    const int i = lane % PQ_GL;
-    const f2 g = {c_gl_xh[i], c_gl_xl[i]};
-    const f2 s = dfq::add({lane < PQ_GL ? bs : bt, 0.f}, dfq::mulf(g, bz));
-    f2 l[PQ_P], d[PQ_P];
-    basis_df(s, l, d);
-    const int r = i % H;
-    const int y = i >= H ? 1 : 0;
-#pragma unroll
-    for (int a = 0; a < PQ_P; ++a) {
-      if (lane < PQ_GL) {
-        // d2 = {h.x, h.y, l.x, l.y}: row i's words sit at offsets y and 2 + y
-        float* ls = reinterpret_cast<float*>(&sm.LsP[r][a]) + y;
-        float* ld = reinterpret_cast<float*>(&sm.LdsP[r][a]) + y;
-        ls[0] = l[a].h;
-        ls[2] = l[a].l;
-        ld[0] = d[a].h;
-        ld[2] = d[a].l;
-      } else {
-        sm.Lt[i][a] = l[a];
-        sm.Ldt[i][a] = d[a];
-      }
-    }
-  }
+  basis_df_warp(sm, lane, bs, bt, bz);
   __syncwarp();
   for (int e = lane; e < 7 * H * PQ_P; e += 32) {
     const int m = e / (H * PQ_P), r = (e / PQ_P) % H, b = e % PQ_P;
@@ -332,7 +340,7 @@ __device__ __forceinline__ void leaf_pk(SM& sm, int lane, float bs, float bt, fl
 }
 
 template <int KER, bool WEIGHTS>
-__global__ void __launch_bounds__(32 * PQ_WARPS) panel_near_kernel_df(PanelParams p) {
+__global__ void __launch_bounds__(32 * PQ_WARPS, WEIGHTS ? 3 : 4) panel_near_kernel_df(PanelParams p) {
   extern __shared__ __align__(16) unsigned char pq_smem_df[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   DFSmem<WEIGHTS>& sm = reinterpret_cast<DFSmem<WEIGHTS>*>(pq_smem_df)[warp];
