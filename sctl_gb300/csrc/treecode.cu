@@ -468,7 +468,9 @@ __device__ __forceinline__ f2 tc_split(double v) {
   const float h = (float)v;
   return {h, (float)(v - (double)h)};
 }
-__device__ __forceinline__ void tc_lagrange_df(double tt, int np, const TcMomParams& p, f2* L) {
+// Barycentric Lagrange basis at t in double-float; P holds the points (xh, xl) and weights (wf).
+template <class P>
+__device__ __forceinline__ void tc_lagrange_df(double tt, int np, const P& p, f2* L) {
   const f2 t = tc_split(tt);
   int hit = -1;
   f2 sum = {0.f, 0.f};
@@ -607,25 +609,6 @@ struct TcL2PParams {
   float xh[TC_MAX_NP], xl[TC_MAX_NP], wf[TC_MAX_NP];
 };
 
-__device__ __forceinline__ void tc_lagrange_df2(double tt, int np, const TcL2PParams& p, f2* L) {
-  const f2 t = tc_split(tt);
-  int hit = -1;
-  f2 sum = {0.f, 0.f};
-  for (int m = 0; m < np; ++m) {
-    const f2 d = df_norm(df_add(t, {-p.xh[m], -p.xl[m]}));
-    if (d.h == 0.f) hit = m;
-    const f2 q = d.h != 0.f ? df_mulf(tc_rcp(d), p.wf[m]) : f2{0.f, 0.f};
-    L[m] = q;
-    df_acc(sum, q);
-  }
-  if (hit >= 0) {
-    for (int m = 0; m < np; ++m) L[m] = {m == hit ? 1.f : 0.f, 0.f};
-  } else {
-    const f2 inv = tc_rcp(df_norm(sum));
-    for (int m = 0; m < np; ++m) L[m] = df_norm(df_mul(L[m], inv));
-  }
-}
-
 template <int TD, bool DF>
 __global__ void __launch_bounds__(TC_THREADS) tc_l2p_kernel(TcL2PParams p) {
   using V = typename std::conditional<DF, f2, double>::type;
@@ -655,20 +638,10 @@ __global__ void __launch_bounds__(TC_THREADS) tc_l2p_kernel(TcL2PParams p) {
       if (lane < 3) {
         double tt = (p.r[k * 3 + lane] - A.lo[lane]) * A.inv[lane] - 1.0;
         tt = fmin(1.0, fmax(-1.0, tt));
-        if constexpr (DF) {
-          tc_lagrange_df2(tt, np, p, Lw + lane * TC_MAX_NP);
-        } else {
-          double* L = Lw + lane * TC_MAX_NP;
-          int hit = -1;
-          double sum = 0.0;
-          for (int m = 0; m < np; ++m) {
-            const double d = tt - p.x[m];
-            if (d == 0.0) hit = m;
-            L[m] = d != 0.0 ? p.w[m] / d : 0.0;
-            sum += L[m];
-          }
-          for (int m = 0; m < np; ++m) L[m] = hit >= 0 ? (m == hit ? 1.0 : 0.0) : L[m] / sum;
-        }
+        if constexpr (DF)
+          tc_lagrange_df(tt, np, p, Lw + lane * TC_MAX_NP);
+        else
+          tc_lagrange(tt, np, p.x, p.w, Lw + lane * TC_MAX_NP);
       }
       __syncwarp();
       V acc[TD];
