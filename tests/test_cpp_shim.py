@@ -66,3 +66,29 @@ def test_reference_call_sites_run_the_gpu_kernel(cuda, tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=600, env=env)
     print(r.stdout)
     assert r.returncode == 0 and "PASS (0 check(s) failed)" in r.stdout, r.stdout + r.stderr
+
+
+def build_treecode_test(tmp_path):
+    exe = os.path.join(str(tmp_path), "test_treecode_capi")
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    cuda_lib = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "lib64")
+    cmd = [CXX, "-std=c++17", "-O2", "-I", INC, "-I", cuda_inc, os.path.join(ROOT, "tests", "cpp", "test_treecode_capi.cpp"),
+           "-L", LIBDIR, "-lsctlgpu", "-Wl,-rpath," + LIBDIR, "-L", cuda_lib, "-lcudart", "-Wl,-rpath," + cuda_lib,
+           "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
+    return exe
+
+
+def test_treecode_capi_compiles_and_links(tmp_path):
+    from sctl_gb300 import capi
+    capi.load()
+    assert os.path.exists(build_treecode_test(tmp_path))
+
+
+@pytest.mark.gpu
+def test_treecode_capi_from_cpp(cuda, tmp_path):
+    """The treecode bound from C++ as a ParticleFMM integration would: against sctlgpu_eval."""
+    exe = build_treecode_test(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "PASS (0 check(s) failed)" in r.stdout, r.stdout + r.stderr
