@@ -99,6 +99,33 @@ def test_treecode_coincident_targets_and_particle_cluster_form(cuda):
         assert np.abs(u[:3000] - u[0]).max() <= 1e-12 * abs(u[0])
 
 
+def test_treecode_sources_as_targets_and_flat_sources(cuda):
+    """Targets = sources (self-interaction pairs contribute nothing, as in the direct sum), and a
+    flat sheet of sources (zero extent in z: every cluster box is degenerate in one dimension)."""
+    torch = cuda
+    rng = np.random.default_rng(5)
+    k = 2
+    d = W.sphere_ball(1 << 17, 16, k, seed=30)
+    xs = d["r_src"]
+    tc = TC.Treecode(k, xs, xs, digits=10)
+    assert tc.info()["proxy_interactions"] > 0 and tc.info()["target_clusters"] > 0
+    u = tc.eval(dev(torch, d["v_src"])).cpu().numpy()
+    sub = np.arange(0, 1 << 17, 97)
+    ref = O.eval(k, xs[sub], xs, None, d["v_src"])
+    assert O.rel_l2(u.reshape(-1, 3)[sub].reshape(-1), ref) < 1e-10
+    k = 1
+    ns, nt = 1 << 17, 1 << 14
+    xs = np.c_[rng.uniform(-1, 1, (ns, 2)), np.zeros(ns)]
+    xn = np.tile([0.0, 0.0, 1.0], (ns, 1))
+    xt = np.c_[rng.uniform(-1, 1, (nt, 2)), rng.uniform(-0.5, 0.5, nt)]
+    f = rng.standard_normal(ns)
+    tc = TC.Treecode(k, xs, xt, n_src=xn, digits=10)
+    assert tc.info()["proxy_interactions"] > 0
+    u = tc.eval(dev(torch, f)).cpu().numpy()
+    sub = np.arange(0, nt, 31)
+    assert O.rel_l2(u[sub], O.eval(k, xt[sub], xs, xn, f)) < 1e-10
+
+
 def test_treecode_single_leaf_is_the_direct_sum(cuda):
     """One leaf, FP64 arithmetic: the treecode is the direct sum up to summation order."""
     torch = cuda
