@@ -474,12 +474,15 @@ def torus_section(torch, n_eval=1 << 20, n_train=440000, steps=4000, learned=Tru
     setup_s = time.perf_counter() - t0
     acc = torch.zeros(n_eval, dtype=torch.float64, device="cuda")
     apply_ms = _ev_ms(torch, lambda: M.apply(sig, acc), reps=5)
+    apply_unresolved_ms = _ev_ms(torch, lambda: M.apply_unresolved(sig, acc), reps=5)
     hbm = peaks().get("hbm_gbs", 6800.0)
-    # bytes per application: the stored blocks, plus per pair its panel index and order entry, plus
-    # per target its offsets and the read-modify-write of the potential (densities stay in L2)
+    # bytes per application: the stored blocks, plus per pair its resolved entry (K offset, F offset
+    # and length), plus per target its offsets and the read-modify-write of the potential (densities
+    # stay in L2)
     alg = M.nbytes + M.n_pairs * 16 + n_eval * (8 + 16)
     with_m = S.evaluate(xt, sig, pairs=pairs, plan=plan, matrix=M)
     res["near_matrix"] = {"setup_s": setup_s, "matrix_bytes": M.nbytes, "apply_ms": apply_ms,
+                          "apply_through_index_chain_ms": apply_unresolved_ms,
                           "apply_gb_s": alg / (apply_ms * 1e-3) / 1e9,
                           "apply_frac_of_measured_hbm": alg / (apply_ms * 1e-3) / 1e9 / hbm,
                           "evaluate_ms": _ev_ms(torch, lambda: S.evaluate(xt, sig, pairs=pairs, plan=plan, matrix=M),

@@ -358,6 +358,23 @@ int sctlgpu_near_matrix_apply_pairs(int k0, int k1, int64_t n_trg, const int64_t
                                     const int64_t* elem_nds_cnt, int64_t n_k, const float* K2, int64_t n_f,
                                     const double* F, double* U, void* stream);
 
+/*
+ * The index chain of the two entry points above (target-major entry -> pair ->
+ * element -> nodes), resolved once for stored matrices (SetupNear keeps the same
+ * structure for every ComputeNearInterac): resolved[2j] = K offset of entry j,
+ * resolved[2j+1] = (F offset << 20) | F length, or -1 where an index is out of range
+ * (that entry is skipped and flagged when applied).  Device arrays, asynchronous.
+ */
+int sctlgpu_near_matrix_resolve(int k0, int k1, int64_t n_near, const int64_t* trg_pair, int64_t n_pairs,
+                                const int64_t* pair_elem, const int64_t* pair_kdsp, int64_t n_elem,
+                                const int64_t* elem_nds_dsp, const int64_t* elem_nds_cnt, int64_t n_k, int64_t n_f,
+                                int64_t* resolved, void* stream);
+/* ComputeNearInterac from resolved entries: one coalesced 16-byte load per entry instead of the
+ * chain of dependent index loads.  Exactly one of K (FP64 blocks) and K2 (float pairs) non-NULL. */
+int sctlgpu_near_matrix_apply_resolved(int k0, int k1, int64_t n_trg, const int64_t* trg_dsp, int64_t n_near,
+                                       const int64_t* resolved, int64_t n_k, const double* K, const float* K2,
+                                       int64_t n_f, const double* F, double* U, void* stream);
+
 /* x[0..n) -> out[2i], out[2i+1] = hi, lo float pair of x[i] (device pointers, 8-byte
  * aligned; out may be x itself), asynchronous on `stream`. */
 int sctlgpu_to_float_pairs(int64_t n, const double* x, float* out, void* stream);

@@ -75,6 +75,8 @@ SIGNATURES = {
     "sctlgpu_near_matrix_apply_pairs": (_i, [_i, _i, _i64, _vp, _i64, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp,
                                             _i64, _vp, _vp, _vp]),
     "sctlgpu_to_float_pairs": (_i, [_i64, _vp, _vp, _vp]),
+    "sctlgpu_near_matrix_resolve": (_i, [_i, _i, _i64, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _i64, _i64, _vp, _vp]),
+    "sctlgpu_near_matrix_apply_resolved": (_i, [_i, _i, _i64, _vp, _i64, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _vp]),
     "sctlgpu_device_status_word": (_i, [_vp, ctypes.POINTER(ctypes.c_uint)]),
     "sctlgpu_panel_arithmetic": (_i, [_i]),
     "sctlgpu_tc_gemm_bf16": (_i, [_i, _i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _vp]),

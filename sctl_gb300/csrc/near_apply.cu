@@ -42,6 +42,7 @@ struct NearApplyParams {
   const int64_t* pair_kdsp;     // [n_pairs] first entry of the pair's block in K
   const int64_t* elem_nds_dsp;  // [n_elem]
   const int64_t* elem_nds_cnt;  // [n_elem]
+  const int64_t* resolved;      // [2 * n_near] or null: per target-major entry its K offset and (F offset, length)
   const double* K;    // FP64 blocks, or
   const float2* K2;   // the same as float pairs
   const double* F;
@@ -158,16 +159,27 @@ __global__ void to_float_pairs_kernel(int64_t n, const double* x, float2* out) {
   }
 }
 
-template <int K1, bool PAIRS>
+// Entry j of the resolved table: resolved[2j] = K offset, resolved[2j + 1] = (F offset << 20) | length,
+// or -1 for an entry whose indices were out of range.
+constexpr int NA_LEN_BITS = 20;
+
+template <int K1, bool PAIRS, bool RESOLVED>
 __global__ void __launch_bounds__(32 * NA_WARPS) near_apply_kernel(NearApplyParams p) {
   using Acc = typename std::conditional<PAIRS, f2, double>::type;
   const int lane = threadIdx.x & 31;
   const int64_t nwarps = (int64_t)gridDim.x * NA_WARPS;
-  for (int64_t t = (int64_t)blockIdx.x * NA_WARPS + (threadIdx.x >> 5); t < p.n_trg; t += nwarps) {
+  int64_t t = (int64_t)blockIdx.x * NA_WARPS + (threadIdx.x >> 5);
+  // the next target's pair range is loaded one target ahead
+  int64_t nj0 = t < p.n_trg ? p.trg_dsp[t] : 0, nj1 = t < p.n_trg ? p.trg_dsp[t + 1] : 0;
+  for (; t < p.n_trg; t += nwarps) {
     Acc acc[K1];
 #pragma unroll
     for (int c = 0; c < K1; ++c) acc[c] = Acc{};
-    int64_t j0 = p.trg_dsp[t], j1 = p.trg_dsp[t + 1];
+    int64_t j0 = nj0, j1 = nj1;
+    if (t + nwarps < p.n_trg) {
+      nj0 = p.trg_dsp[t + nwarps];
+      nj1 = p.trg_dsp[t + nwarps + 1];
+    }
     bool bad = false;
     if (j0 < 0 || j1 > p.n_near || j1 < j0) {
       bad = true;
@@ -179,14 +191,24 @@ __global__ void __launch_bounds__(32 * NA_WARPS) near_apply_kernel(NearApplyPara
       const int64_t j = jb + lane;
       int64_t n = -1, fofs = 0, kofs = 0;
       if (j < j1) {
-        const int64_t pr = p.trg_pair ? p.trg_pair[j] : j;
-        if (pr >= 0 && pr < p.n_pairs) {
-          const int64_t e = p.pair_elem[pr];
-          if (e >= 0 && e < p.n_elem) {
-            n = p.elem_nds_cnt[e] * p.k0;
-            fofs = p.elem_nds_dsp[e] * p.k0;
-            kofs = p.pair_kdsp[pr];
-            if (n < 0 || fofs < 0 || fofs + n > p.n_f || kofs < 0 || kofs + n * K1 > p.n_k) n = -1;
+        if constexpr (RESOLVED) {  // one coalesced 16-byte load per entry
+          const int64_t r1 = p.resolved[2 * j + 1];
+          kofs = p.resolved[2 * j];
+          if (r1 >= 0) {
+            n = r1 & ((INT64_C(1) << NA_LEN_BITS) - 1);
+            fofs = r1 >> NA_LEN_BITS;
+            if (fofs + n > p.n_f || kofs < 0 || kofs + n * K1 > p.n_k) n = -1;
+          }
+        } else {
+          const int64_t pr = p.trg_pair ? p.trg_pair[j] : j;
+          if (pr >= 0 && pr < p.n_pairs) {
+            const int64_t e = p.pair_elem[pr];
+            if (e >= 0 && e < p.n_elem) {
+              n = p.elem_nds_cnt[e] * p.k0;
+              fofs = p.elem_nds_dsp[e] * p.k0;
+              kofs = p.pair_kdsp[pr];
+              if (n < 0 || fofs < 0 || fofs + n > p.n_f || kofs < 0 || kofs + n * K1 > p.n_k) n = -1;
+            }
           }
         }
         if (n < 0) bad = true;
@@ -230,10 +252,39 @@ __global__ void __launch_bounds__(32 * NA_WARPS) near_apply_kernel(NearApplyPara
 
 template <int K1>
 void launch_k1(const NearApplyParams& p, unsigned grid, cudaStream_t st) {
-  if (p.K2)
-    near_apply_kernel<K1, true><<<grid, 32 * NA_WARPS, 0, st>>>(p);
-  else
-    near_apply_kernel<K1, false><<<grid, 32 * NA_WARPS, 0, st>>>(p);
+  if (p.resolved) {
+    if (p.K2)
+      near_apply_kernel<K1, true, true><<<grid, 32 * NA_WARPS, 0, st>>>(p);
+    else
+      near_apply_kernel<K1, false, true><<<grid, 32 * NA_WARPS, 0, st>>>(p);
+  } else {
+    if (p.K2)
+      near_apply_kernel<K1, true, false><<<grid, 32 * NA_WARPS, 0, st>>>(p);
+    else
+      near_apply_kernel<K1, false, false><<<grid, 32 * NA_WARPS, 0, st>>>(p);
+  }
+}
+
+// The index chain of one target-major entry resolved once (the storage SetupNear keeps).
+__global__ void near_resolve_kernel(NearApplyParams p, int64_t* out) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < p.n_near;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    int64_t n = -1, fofs = 0, kofs = 0;
+    const int64_t pr = p.trg_pair ? p.trg_pair[j] : j;
+    if (pr >= 0 && pr < p.n_pairs) {
+      const int64_t e = p.pair_elem[pr];
+      if (e >= 0 && e < p.n_elem) {
+        n = p.elem_nds_cnt[e] * p.k0;
+        fofs = p.elem_nds_dsp[e] * p.k0;
+        kofs = p.pair_kdsp[pr];
+        if (n < 0 || n >= (INT64_C(1) << NA_LEN_BITS) || fofs < 0 || fofs + n > p.n_f || kofs < 0 ||
+            kofs + n * p.k1 > p.n_k)
+          n = -1;
+      }
+    }
+    out[2 * j] = n < 0 ? 0 : kofs;
+    out[2 * j + 1] = n < 0 ? -1 : (fofs << NA_LEN_BITS) | n;
+  }
 }
 
 }  // namespace
@@ -244,13 +295,15 @@ using namespace sctlgpu;
 static int near_apply(int k0, int k1, int64_t n_trg, const int64_t* trg_dsp, int64_t n_near, const int64_t* trg_pair,
                       int64_t n_pairs, const int64_t* pair_elem, const int64_t* pair_kdsp, int64_t n_elem,
                       const int64_t* elem_nds_dsp, const int64_t* elem_nds_cnt, int64_t n_k, const double* K,
-                      const float* K2, int64_t n_f, const double* F, double* U, void* stream) {
+                      const float* K2, int64_t n_f, const double* F, double* U, void* stream,
+                      const int64_t* resolved = nullptr) {
   if (k0 < 1 || !(k1 == 1 || k1 == 2 || k1 == 3 || k1 == 4 || k1 == 9) || n_trg < 0 || n_near < 0 ||
-      n_pairs < 0 || n_elem < 0 || n_k < 0 || n_f < 0 || (!trg_pair && n_near > n_pairs))
+      n_pairs < 0 || n_elem < 0 || n_k < 0 || n_f < 0 || (!trg_pair && !resolved && n_near > n_pairs))
     return SCTLGPU_ERR_INVALID_SIZE;
   if (n_trg == 0) return SCTLGPU_OK;
-  if (!trg_dsp || !U || (n_pairs && (!pair_elem || !pair_kdsp || (!K && !K2))) ||
-      (n_elem && (!elem_nds_dsp || !elem_nds_cnt || !F)))
+  if (!trg_dsp || !U || (n_near && (!K && !K2)) ||
+      (!resolved && ((n_pairs && (!pair_elem || !pair_kdsp)) || (n_elem && (!elem_nds_dsp || !elem_nds_cnt)))) ||
+      (resolved == nullptr ? (n_elem && !F) : (n_f && !F)) || (resolved && n_near && !resolved))
     return SCTLGPU_ERR_NULL_POINTER;
   if (K2 && ((uintptr_t)K2 & 7)) return SCTLGPU_ERR_INVALID_SIZE;  // float pairs: 8-byte aligned
   int dev;
@@ -273,6 +326,7 @@ static int near_apply(int k0, int k1, int64_t n_trg, const int64_t* trg_dsp, int
   p.pair_kdsp = pair_kdsp;
   p.elem_nds_dsp = elem_nds_dsp;
   p.elem_nds_cnt = elem_nds_cnt;
+  p.resolved = resolved;
   p.K = K;
   p.K2 = reinterpret_cast<const float2*>(K2);
   p.F = F;
@@ -324,6 +378,50 @@ extern "C" int sctlgpu_near_matrix_apply_pairs(int k0, int k1, int64_t n_trg, co
                                                double* U, void* stream) {
   return near_apply(k0, k1, n_trg, trg_dsp, n_near, trg_pair, n_pairs, pair_elem, pair_kdsp, n_elem, elem_nds_dsp,
                     elem_nds_cnt, n_k, nullptr, K2, n_f, F, U, stream);
+}
+
+extern "C" int sctlgpu_near_matrix_resolve(int k0, int k1, int64_t n_near, const int64_t* trg_pair, int64_t n_pairs,
+                                           const int64_t* pair_elem, const int64_t* pair_kdsp, int64_t n_elem,
+                                           const int64_t* elem_nds_dsp, const int64_t* elem_nds_cnt, int64_t n_k,
+                                           int64_t n_f, int64_t* resolved, void* stream) {
+  if (k0 < 1 || !(k1 == 1 || k1 == 2 || k1 == 3 || k1 == 4 || k1 == 9) || n_near < 0 || n_pairs < 0 || n_elem < 0 ||
+      n_k < 0 || n_f < 0 || (!trg_pair && n_near > n_pairs))
+    return SCTLGPU_ERR_INVALID_SIZE;
+  if (n_near == 0) return SCTLGPU_OK;
+  if (!resolved || (n_pairs && (!pair_elem || !pair_kdsp)) || (n_elem && (!elem_nds_dsp || !elem_nds_cnt)))
+    return SCTLGPU_ERR_NULL_POINTER;
+  int dev;
+  unsigned* status;
+  int sms;
+  int rc = runtime_device(&dev, &status, &sms);
+  if (rc) return rc;
+  NearApplyParams p{};
+  p.k0 = k0;
+  p.k1 = k1;
+  p.n_near = n_near;
+  p.n_pairs = n_pairs;
+  p.n_elem = n_elem;
+  p.n_k = n_k;
+  p.n_f = n_f;
+  p.trg_pair = trg_pair;
+  p.pair_elem = pair_elem;
+  p.pair_kdsp = pair_kdsp;
+  p.elem_nds_dsp = elem_nds_dsp;
+  p.elem_nds_cnt = elem_nds_cnt;
+  const int64_t b = (n_near + 255) / 256;
+  near_resolve_kernel<<<(unsigned)(b < (int64_t)sms * 8 ? b : (int64_t)sms * 8), 256, 0, (cudaStream_t)stream>>>(
+      p, resolved);
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  return runtime_record(cudaGetLastError());
+}
+
+extern "C" int sctlgpu_near_matrix_apply_resolved(int k0, int k1, int64_t n_trg, const int64_t* trg_dsp,
+                                                  int64_t n_near, const int64_t* resolved, int64_t n_k,
+                                                  const double* K, const float* K2, int64_t n_f, const double* F,
+                                                  double* U, void* stream) {
+  if ((K == nullptr) == (K2 == nullptr)) return SCTLGPU_ERR_INVALID_ARGUMENT;  // exactly one form of the blocks
+  return near_apply(k0, k1, n_trg, trg_dsp, n_near, nullptr, 0, nullptr, nullptr, 0, nullptr, nullptr, n_k, K, K2,
+                    n_f, F, U, stream, resolved);
 }
 
 extern "C" int sctlgpu_to_float_pairs(int64_t n, const double* x, float* out, void* stream) {

@@ -206,6 +206,12 @@ class NearMatrix:
         self.pair_kdsp = (torch.arange(self.n_pairs, dtype=torch.int64, device=dev) * S.nn).contiguous()
         self.elem_nds_dsp = (torch.arange(S.np, dtype=torch.int64, device=dev) * S.nn).contiguous()
         self.elem_nds_cnt = torch.full((S.np,), S.nn, dtype=torch.int64, device=dev)
+        # the index chain (target-major entry -> pair -> element -> nodes) resolved once
+        self.resolved = torch.empty(2 * max(self.n_pairs, 1), dtype=torch.int64, device=dev)
+        capi.check(capi.load().sctlgpu_near_matrix_resolve(
+            1, 1, self.n_pairs, self.trg_pair.data_ptr(), self.n_pairs, self.pair_elem.data_ptr(),
+            self.pair_kdsp.data_ptr(), self.np, self.elem_nds_dsp.data_ptr(), self.elem_nds_cnt.data_ptr(),
+            self.W.numel(), S.np * S.nn, self.resolved.data_ptr(), stream), "near_matrix_resolve")
 
     @property
     def nbytes(self):
@@ -213,7 +219,17 @@ class NearMatrix:
         return self.W.numel() * 8
 
     def apply(self, sigma, out):
-        """out[t] += sum over t's near pairs of W_j . sigma[panel_j]."""
+        """out[t] += sum over t's near pairs of W_j . sigma[panel_j] (from the resolved entries)."""
+        f = sigma.reshape(-1).contiguous()
+        w = self.W.data_ptr()
+        capi.check(capi.load().sctlgpu_near_matrix_apply_resolved(
+            1, 1, self.nt, self.trg_dsp.data_ptr(), self.n_pairs, self.resolved.data_ptr(), self.W.numel(),
+            None if self.float_pairs else w, w if self.float_pairs else None, f.numel(), f.data_ptr(),
+            out.data_ptr(), torch.cuda.current_stream().cuda_stream), "near_matrix_apply")
+        return out
+
+    def apply_unresolved(self, sigma, out):
+        """The same through the index chain (sctlgpu_near_matrix_apply[_pairs], the reference's arrays)."""
         f = sigma.reshape(-1).contiguous()
         fn = capi.load().sctlgpu_near_matrix_apply_pairs if self.float_pairs else capi.load().sctlgpu_near_matrix_apply
         capi.check(fn(

@@ -175,6 +175,22 @@ def test_near_matrix_apply_general_layout(cuda, k0, k1):
     got2 = U2.cpu().numpy()
     np.testing.assert_allclose(got2, want, rtol=1e-12, atol=1e-12)
     np.testing.assert_array_equal(got2[(nt - 5) * k1:], U0[(nt - 5) * k1:])
+    # the index chain resolved once: both forms of the blocks give the same sums as through the chain
+    res = torch.empty(2 * n_pairs, dtype=torch.int64, device="cuda")
+    assert lib.sctlgpu_near_matrix_resolve(k0, k1, n_pairs, g["ord"].data_ptr(), n_pairs, g["pe"].data_ptr(),
+                                           g["kd"].data_ptr(), n_elem, g["ed"].data_ptr(), g["ec"].data_ptr(),
+                                           K.size, F.size, res.data_ptr(), None) == capi.OK
+    for kk, k2, ref in ((g["K"], None, got), (None, K2, got2)):
+        U3 = d(U0, torch.float64)
+        rc = lib.sctlgpu_near_matrix_apply_resolved(k0, k1, nt, g["tdsp"].data_ptr(), n_pairs, res.data_ptr(), K.size,
+                                                    kk.data_ptr() if kk is not None else None,
+                                                    k2.data_ptr() if k2 is not None else None, F.size,
+                                                    g["F"].data_ptr(), U3.data_ptr(), None)
+        assert rc == capi.OK
+        np.testing.assert_array_equal(U3.cpu().numpy(), ref)
+    assert lib.sctlgpu_near_matrix_apply_resolved(k0, k1, nt, g["tdsp"].data_ptr(), n_pairs, res.data_ptr(), K.size,
+                                                  g["K"].data_ptr(), K2.data_ptr(), F.size, g["F"].data_ptr(),
+                                                  U3.data_ptr(), None) == capi.ERR_INVALID_ARGUMENT
     assert capi.load().sctlgpu_device_status(None) == capi.OK
 
 
