@@ -301,7 +301,7 @@ static int near_apply(int k0, int k1, int64_t n_trg, const int64_t* trg_dsp, int
       n_pairs < 0 || n_elem < 0 || n_k < 0 || n_f < 0 || (!trg_pair && !resolved && n_near > n_pairs))
     return SCTLGPU_ERR_INVALID_SIZE;
   if (n_trg == 0) return SCTLGPU_OK;
-  if (!trg_dsp || !U || (n_near && (!K && !K2)) ||
+  if (!trg_dsp || !U || ((resolved ? n_near : n_pairs) && !K && !K2) ||
       (!resolved && ((n_pairs && (!pair_elem || !pair_kdsp)) || (n_elem && (!elem_nds_dsp || !elem_nds_cnt)))) ||
       (resolved == nullptr ? (n_elem && !F) : (n_f && !F)) || (resolved && n_near && !resolved))
     return SCTLGPU_ERR_NULL_POINTER;
