@@ -259,7 +259,7 @@ __device__ __forceinline__ void leaf_pk(SM& sm, int lane, float bs, float bt, fl
   __syncwarp();
   const int r = lane / PQ_GL, j = lane % PQ_GL;  // nodes (r, j) and (r + 4, j)
   pdfq::d2 X[3] = {}, Xs[3] = {}, Xt[3] = {}, sg = {};
-#pragma unroll 2
+#pragma unroll 1
   for (int b = 0; b < PQ_P; ++b) {
     const pdfq::d2 lt = pdfq::dupf2(sm.Lt[j][b]), ldt = pdfq::dupf2(sm.Ldt[j][b]);
 #pragma unroll
