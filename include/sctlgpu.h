@@ -288,7 +288,9 @@ int sctlgpu_near_list_destroy(sctlgpu_near_list list);
  * that for the Stokes double layer), batch_max = 512.
  * execute: v_src (device, ns * SrcDim, source order as given; SetDensitySL /
  * DL) -> v_out (device, nt * TrgDim, target order as given); flags may hold
- * SCTLGPU_ACCUMULATE; asynchronous on `stream`.
+ * SCTLGPU_ACCUMULATE; asynchronous on `stream`.  A treecode's device buffers
+ * are reused by every execution: executions of one treecode must not overlap
+ * (one stream, or one treecode per concurrent stream).
  * info / layout: sizes[9] = {blocks, source slots (leaves padded to even
  * counts), all source slots (with proxies), source clusters with proxies,
  * direct interactions, interactions through proxies, order, target list
