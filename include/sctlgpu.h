@@ -286,9 +286,11 @@ int sctlgpu_near_list_destroy(sctlgpu_near_list list);
  * the device-side plan.  params may be NULL: order and theta then follow
  * `digits`, leaf_max = 1.5 proxy slots per cluster ((order+1)^3, three times
  * that for the Stokes double layer), batch_max = 512.
- * execute: v_src (device, ns * SrcDim, source order as given; SetDensitySL /
- * DL) -> v_out (device, nt * TrgDim, target order as given); flags may hold
- * SCTLGPU_ACCUMULATE; asynchronous on `stream`.  A treecode's device buffers
+ * execute: v_src (ns * SrcDim, source order as given; SetDensitySL / DL) ->
+ * v_out (nt * TrgDim, target order as given); flags may hold
+ * SCTLGPU_ACCUMULATE.  Host arrays (synchronous, staged through device buffers
+ * kept with the treecode; also reports a device-side timeout), or device arrays
+ * with SCTLGPU_DEVICE_PTRS (asynchronous on `stream`).  A treecode's device buffers
  * are reused by every execution: executions of one treecode must not overlap
  * (one stream, or one treecode per concurrent stream).
  * info / layout: sizes[9] = {blocks, source slots (leaves padded to even

@@ -27,6 +27,7 @@
 #include <cstdlib>
 #include <string>
 #include <type_traits>
+#include <vector>
 
 #include "sctlgpu.h"
 
@@ -168,6 +169,105 @@ using Stokes3D_DxU = GpuKernel<SCTLGPU_STOKES3D_DXU>;
 using Stokes3D_FxT = GpuKernel<SCTLGPU_STOKES3D_FXT>;
 using Stokes3D_FSxU = GpuKernel<SCTLGPU_STOKES3D_FSXU>;
 using Stokes3D_FxUP = GpuKernel<SCTLGPU_STOKES3D_FXUP>;
+
+// ParticleFMM's evaluation for one (source, target) pair of names, on the GPU:
+// the same setters and Eval / EvalDirect (fmm-wrapper.txx:270-281, 505-623),
+// for Real = double and the four hot-path kernels.  Like the reference, Eval
+// takes the fast path for 40,000 targets or more (EvalPVFMM, :854-1038, cut-over
+// :864-867) -- here the treecode, rebuilt when the coordinates or the accuracy
+// changed (the reference's setup_tree flag) -- and EvalDirect otherwise; U is
+// re-initialised to Nt * TrgDim and overwritten (:562-563).
+template <int KID>
+class GpuFarField {
+  static_assert(KID >= SCTLGPU_LAPLACE3D_FXU && KID <= SCTLGPU_STOKES3D_DXU, "the four hot-path kernels");
+
+ public:
+  static constexpr long kDirectBelow = 40000;
+
+  GpuFarField() = default;
+  GpuFarField(const GpuFarField&) = delete;
+  GpuFarField& operator=(const GpuFarField&) = delete;
+  ~GpuFarField() { Release(); }
+
+  void SetAccuracy(int digits) {  // fmm-wrapper.txx:270-281
+    if (digits != digits_) Release();
+    digits_ = digits;
+  }
+  template <class VecT>
+  void SetSrcCoord(const VecT& coord, const VecT& normal) {  // :505-519
+    Copy(xs_, coord);
+    Copy(xn_, normal);
+    Release();
+  }
+  template <class VecT>
+  void SetSrcCoord(const VecT& coord) {
+    Copy(xs_, coord);
+    xn_.clear();
+    Release();
+  }
+  template <class VecT>
+  void SetSrcDensity(const VecT& density) {  // :521-524
+    Copy(f_, density);
+  }
+  template <class VecT>
+  void SetTrgCoord(const VecT& coord) {  // :526-540
+    Copy(xt_, coord);
+    Release();
+  }
+
+  template <class VecT>
+  void Eval(VecT& U) {  // :542-549
+    const long nt = (long)xt_.size() / 3;
+    if (nt < kDirectBelow) return EvalDirect(U);
+    Check();
+    Resize(U, nt);
+    if (nt == 0) return;
+    int rc = SCTLGPU_OK;
+    if (!tc_)
+      rc = sctlgpu_treecode_create(&tc_, KID, Mode(), digits_, (long)xs_.size() / 3, Ptr(xs_), NDim() ? Ptr(xn_) : nullptr,
+                                   nt, Ptr(xt_), nullptr);
+    if (rc == SCTLGPU_OK) rc = sctlgpu_treecode_execute(tc_, Ptr(f_), &U[0], 0, nullptr);
+    if (rc != SCTLGPU_OK) SCTLGPU_ON_ERROR(rc, "GpuFarField::Eval");
+  }
+  template <class VecT>
+  void EvalDirect(VecT& U) {  // :551-623
+    Check();
+    const long nt = (long)xt_.size() / 3, ns = (long)xs_.size() / 3;
+    Resize(U, nt);
+    if (nt == 0) return;
+    const int rc = sctlgpu_eval(KID, Mode(), digits_, nt, Ptr(xt_), ns, Ptr(xs_), NDim() ? Ptr(xn_) : nullptr,
+                                Ptr(f_), &U[0], 0, nullptr);
+    if (rc != SCTLGPU_OK) SCTLGPU_ON_ERROR(rc, "GpuFarField::EvalDirect");
+  }
+
+ private:
+  static long NDim() { return GpuKernel<KID>::NormalDim(); }
+  static int Mode() { return double_mode() == SCTLGPU_F64 ? SCTLGPU_F64 : SCTLGPU_MIXED; }
+  static const double* Ptr(const std::vector<double>& v) { return v.empty() ? nullptr : v.data(); }
+  template <class VecT>
+  static void Copy(std::vector<double>& dst, const VecT& src) {
+    dst.resize((size_t)src.Dim());
+    for (long i = 0; i < (long)src.Dim(); ++i) dst[(size_t)i] = (double)src[i];
+  }
+  template <class VecT>
+  static void Resize(VecT& U, long nt) {
+    if ((long)U.Dim() != nt * GpuKernel<KID>::TrgDim()) U.ReInit(nt * GpuKernel<KID>::TrgDim());
+  }
+  void Check() const {
+    const long ns = (long)xs_.size() / 3;
+    if ((long)xs_.size() != ns * 3 || (long)xt_.size() % 3 || (long)f_.size() != ns * GpuKernel<KID>::SrcDim() ||
+        (NDim() && (long)xn_.size() != ns * NDim()))
+      SCTLGPU_ON_ERROR(SCTLGPU_ERR_INVALID_SIZE, "GpuFarField");
+  }
+  void Release() {
+    if (tc_) sctlgpu_treecode_destroy(tc_);
+    tc_ = nullptr;
+  }
+
+  std::vector<double> xs_, xn_, xt_, f_;
+  int digits_ = 10;  // ParticleFMM's default accuracy (fmm-wrapper.txx:205)
+  sctlgpu_treecode tc_ = nullptr;
+};
 
 }  // namespace sctlgpu
 

@@ -704,6 +704,7 @@ struct sctlgpu_treecode_s {
   TcLayout L;
   int64_t ns = 0, nt = 0, n_items = 0, n_pieces = 0;
   double *d_trg = nullptr, *d_r = nullptr, *d_n = nullptr, *d_v = nullptr, *d_part = nullptr, *d_u = nullptr;
+  double *h_in = nullptr, *h_out = nullptr;  // device staging of host-array executions (allocated on first use)
   int64_t *d_slot_src = nullptr, *d_tperm = nullptr, *d_bt0 = nullptr;
   int32_t *d_btn = nullptr, *d_anc_ptr = nullptr, *d_anc = nullptr;
   TcCluster* d_clusters = nullptr;
@@ -717,6 +718,7 @@ namespace {
 void tc_free(sctlgpu_treecode_s* T) {
   if (T->plan) sctlgpu_near_plan_destroy(T->plan);
   for (void* q : {(void*)T->d_trg, (void*)T->d_r, (void*)T->d_n, (void*)T->d_v, (void*)T->d_part, (void*)T->d_u,
+                  (void*)T->h_in, (void*)T->h_out,
                   (void*)T->d_slot_src, (void*)T->d_tperm, (void*)T->d_bt0, (void*)T->d_btn, (void*)T->d_anc_ptr,
                   (void*)T->d_anc, (void*)T->d_clusters, (void*)T->d_items, (void*)T->d_boxes})
     cudaFree(q);
@@ -936,12 +938,36 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   return SCTLGPU_OK;
 }
 
+static int tc_execute_device(sctlgpu_treecode T, const double* v_src, double* v_out, unsigned flags, void* stream);
+
 int sctlgpu_treecode_execute(sctlgpu_treecode T, const double* v_src, double* v_out, unsigned flags, void* stream) {
   if (!T) return SCTLGPU_ERR_NULL_POINTER;
   if (flags & ~(unsigned)(SCTLGPU_ACCUMULATE | SCTLGPU_DEVICE_PTRS)) return SCTLGPU_ERR_INVALID_ARGUMENT;
   if ((T->ns && !v_src) || (T->nt && !v_out)) return SCTLGPU_ERR_NULL_POINTER;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev != T->device) return SCTLGPU_ERR_INVALID_ARGUMENT;
+  if (flags & SCTLGPU_DEVICE_PTRS) return tc_execute_device(T, v_src, v_out, flags, stream);
+  // host arrays: staged through device buffers kept with the treecode, synchronous
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t bin = (size_t)T->ns * T->SD * sizeof(double), bout = (size_t)T->nt * T->TD * sizeof(double);
+  cudaError_t e = cudaSuccess;
+  if (!T->h_in && (e = cudaMalloc((void**)&T->h_in, std::max<size_t>(bin, 16))) != cudaSuccess) return runtime_record(e);
+  if (!T->h_out && (e = cudaMalloc((void**)&T->h_out, std::max<size_t>(bout, 16))) != cudaSuccess)
+    return runtime_record(e);
+  if (bin && (e = cudaMemcpyAsync(T->h_in, v_src, bin, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    return runtime_record(e);
+  if ((flags & SCTLGPU_ACCUMULATE) && bout &&
+      (e = cudaMemcpyAsync(T->h_out, v_out, bout, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    return runtime_record(e);
+  const int rc = tc_execute_device(T, T->h_in, T->h_out, flags | SCTLGPU_DEVICE_PTRS, stream);
+  if (rc) return rc;
+  if (bout && (e = cudaMemcpyAsync(v_out, T->h_out, bout, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return runtime_record(e);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return runtime_record(e);
+  return sctlgpu_near_plan_status(T->plan, stream);
+}
+
+static int tc_execute_device(sctlgpu_treecode T, const double* v_src, double* v_out, unsigned flags, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   const TcLayout& L = T->L;
   cudaError_t e = cudaSuccess;

@@ -1,16 +1,19 @@
 // The treecode's C ABI bound the way a ParticleFMM integration would (host
-// coordinates at setup, device densities and potentials per evaluation),
-// checked against the direct sum of the same library (sctlgpu_eval, host
-// arrays): relative l2 within 10^-digits for digits 6 and 10, Laplace and
-// Stokes double layers, plus the accumulate flag.
+// coordinates at setup, device or host densities and potentials per
+// evaluation), checked against the direct sum of the same library
+// (sctlgpu_eval, host arrays): relative l2 within 10^-digits for digits 6 and
+// 10, Laplace and Stokes double layers, the accumulate flag, host-array
+// execution; and the shim's GpuFarField (ParticleFMM's setters, Eval and
+// EvalDirect) on both sides of the 40,000-target cut-over.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <random>
 #include <vector>
 
-#include "sctlgpu.h"
+#include "sctlgpu.hpp"
 
 static int failures = 0;
 #define CHECK(c, ...)                  \
@@ -71,7 +74,7 @@ int main() {
       cudaMalloc(&d_f, f.size() * sizeof(double));
       cudaMalloc(&d_u, nt * td * sizeof(double));
       cudaMemcpy(d_f, f.data(), f.size() * sizeof(double), cudaMemcpyHostToDevice);
-      rc = sctlgpu_treecode_execute(tc, d_f, d_u, 0, nullptr);
+      rc = sctlgpu_treecode_execute(tc, d_f, d_u, SCTLGPU_DEVICE_PTRS, nullptr);
       CHECK(rc == SCTLGPU_OK, "execute rc %d", rc);
       std::vector<double> u(nt * td);
       cudaMemcpy(u.data(), d_u, u.size() * sizeof(double), cudaMemcpyDeviceToHost);
@@ -81,9 +84,13 @@ int main() {
                   (long long)ns * nt, err);
       CHECK(err < std::pow(10.0, -digits), "kernel %d digits %d: rel l2 %.3e", kid, digits, err);
       // accumulate: a second execution adds the same potentials
-      rc = sctlgpu_treecode_execute(tc, d_f, d_u, SCTLGPU_ACCUMULATE, nullptr);
+      rc = sctlgpu_treecode_execute(tc, d_f, d_u, SCTLGPU_ACCUMULATE | SCTLGPU_DEVICE_PTRS, nullptr);
       std::vector<double> u2(nt * td);
       cudaMemcpy(u2.data(), d_u, u2.size() * sizeof(double), cudaMemcpyDeviceToHost);
+      // host arrays: the same potentials, synchronously
+      std::vector<double> uh(nt * td, 0.0);
+      CHECK(sctlgpu_treecode_execute(tc, f.data(), uh.data(), 0, nullptr) == SCTLGPU_OK, "host execute");
+      CHECK(rel_l2(uh, u) < 1e-14, "host-array execution equals the device one");
       for (auto& v : u) v *= 2;
       CHECK(rc == SCTLGPU_OK && rel_l2(u2, u) < 1e-13, "accumulate");
       CHECK(sctlgpu_treecode_status(tc, nullptr) == SCTLGPU_OK, "status");
@@ -91,6 +98,43 @@ int main() {
       cudaFree(d_f);
       cudaFree(d_u);
     }
+  }
+  // ParticleFMM's calls on the shim's GpuFarField: Eval = treecode for >= 40,000 targets
+  {
+    struct Vec {  // the members of sctl::Vector the shim uses
+      std::vector<double> v;
+      long Dim() const { return (long)v.size(); }
+      double& operator[](long i) { return v[i]; }
+      const double& operator[](long i) const { return v[i]; }
+      void ReInit(long n) { v.assign(n, 0.0); }
+      void SetZero() { std::fill(v.begin(), v.end(), 0.0); }
+    };
+    const long nt2 = 1 << 16;  // above the cut-over
+    std::vector<double> xt2(nt2 * 3);
+    for (long i = 0; i < nt2; ++i) {
+      double v[3] = {nrm(rng), nrm(rng), nrm(rng)};
+      const double r = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]), rad = 2.0 * std::cbrt(uni(rng));
+      for (int d = 0; d < 3; ++d) xt2[i * 3 + d] = v[d] / r * rad;
+    }
+    Vec Xs{xs}, Xn{xn}, Xt{xt2}, F{std::vector<double>(ns)}, U, Ud;
+    for (auto& x : F.v) x = nrm(rng);
+    sctlgpu::set_double_mode(SCTLGPU_MIXED);
+    sctlgpu::GpuFarField<SCTLGPU_LAPLACE3D_DXU> fmm;
+    fmm.SetAccuracy(10);
+    fmm.SetSrcCoord(Xs, Xn);
+    fmm.SetSrcDensity(F);
+    fmm.SetTrgCoord(Xt);
+    fmm.Eval(U);
+    fmm.EvalDirect(Ud);
+    const double err = rel_l2(U.v, Ud.v);
+    std::printf("GpuFarField Laplace3D_DxU, %ld targets: Eval vs EvalDirect rel l2 %.2e\n", nt2, err);
+    CHECK(U.Dim() == nt2 && err < 1e-10 && err > 0, "GpuFarField treecode %.3e", err);
+    Vec Xt_small{std::vector<double>(xt.begin(), xt.begin() + 3 * 1000)};
+    fmm.SetTrgCoord(Xt_small);
+    fmm.Eval(U);
+    fmm.EvalDirect(Ud);
+    CHECK(U.Dim() == 1000 && U.v == Ud.v, "GpuFarField below 40,000 targets is EvalDirect");
+    sctlgpu::set_double_mode(SCTLGPU_F64);
   }
   // argument errors are status codes, before any device work
   sctlgpu_treecode tc = nullptr;
