@@ -293,11 +293,12 @@ int sctlgpu_near_list_destroy(sctlgpu_near_list list);
  * with SCTLGPU_DEVICE_PTRS (asynchronous on `stream`).  A treecode's device buffers
  * are reused by every execution: executions of one treecode must not overlap
  * (one stream, or one treecode per concurrent stream).
- * info / layout: sizes[9] = {blocks, source slots (leaves padded to even
+ * info / layout: sizes[10] = {blocks, source slots (leaves padded to even
  * counts), all source slots (with proxies), source clusters with proxies,
  * direct interactions, interactions through proxies, order, target list
- * (targets, then target proxies), target clusters with proxies}, and the
- * acceptance parameter.  layout is the host-only part of create (no device
+ * (targets, then target proxies), target clusters with proxies, 1 when the
+ * traversal saves less than a quarter of Ns * Nt and evaluations run the
+ * direct sum instead}, and the acceptance parameter.  layout is the host-only part of create (no device
  * needed): the blocks (sources index the source slots, targets the target
  * list), the source of every slot (-1 padding, -2 proxy), the target order,
  * per source cluster with proxies {slot begin, end, proxy slot begin, end}

@@ -50,7 +50,8 @@ namespace {
 constexpr int TC_MAX_NP = 16;   // Chebyshev points per dimension (order + 1)
 constexpr int TC_CHUNK = 256;   // source slots per moment work item
 constexpr int TC_THREADS = 256;
-constexpr int TC_MAX_BATCH = 2048;  // targets per batch (the downward pass keeps a batch's sums in shared memory)
+constexpr int TC_MAX_BATCH = 2048;
+constexpr double TC_DIRECT_FRACTION = 0.75;  // treecode interactions above this share of Ns * Nt: direct sum  // targets per batch (the downward pass keeps a batch's sums in shared memory)
 
 struct TcNode {
   int64_t b = 0, e = 0;    // points [b, e) of the tree's permutation
@@ -162,6 +163,7 @@ struct TcLayout {
   std::vector<sctlgpu_block> blocks;
   int64_t pp = 0, approx = 0;     // interactions of the direct blocks and of the proxy blocks
   bool dual = true;
+  bool direct = false;   // the traversal saves too little: evaluations run the direct sum
   double theta_trg = 0;  // acceptance for target-side interpolation (<= theta)
   double xcheb[TC_MAX_NP], wcheb[TC_MAX_NP];
 };
@@ -330,6 +332,9 @@ int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, con
     (direct ? L.pp : L.approx) += (cur.s1 - cur.s0) * cur.tn;
     k = j;
   }
+  // Below ~25 % saved interactions the proxies' overheads (moments, downward pass, smaller
+  // blocks) eat the gain: such geometries are evaluated by the direct sum.
+  L.direct = (double)(L.pp + L.approx) > TC_DIRECT_FRACTION * (double)ns * (double)nt;
   return SCTLGPU_OK;
 }
 
@@ -705,6 +710,7 @@ struct sctlgpu_treecode_s {
   int64_t ns = 0, nt = 0, n_items = 0, n_pieces = 0;
   double *d_trg = nullptr, *d_r = nullptr, *d_n = nullptr, *d_v = nullptr, *d_part = nullptr, *d_u = nullptr;
   double *h_in = nullptr, *h_out = nullptr;  // device staging of host-array executions (allocated on first use)
+  double *d_xs = nullptr, *d_xn = nullptr, *d_xt = nullptr;  // the direct form: inputs in their own order
   int64_t *d_slot_src = nullptr, *d_tperm = nullptr, *d_bt0 = nullptr;
   int32_t *d_btn = nullptr, *d_anc_ptr = nullptr, *d_anc = nullptr;
   TcCluster* d_clusters = nullptr;
@@ -718,7 +724,7 @@ namespace {
 void tc_free(sctlgpu_treecode_s* T) {
   if (T->plan) sctlgpu_near_plan_destroy(T->plan);
   for (void* q : {(void*)T->d_trg, (void*)T->d_r, (void*)T->d_n, (void*)T->d_v, (void*)T->d_part, (void*)T->d_u,
-                  (void*)T->h_in, (void*)T->h_out,
+                  (void*)T->h_in, (void*)T->h_out, (void*)T->d_xs, (void*)T->d_xn, (void*)T->d_xt,
                   (void*)T->d_slot_src, (void*)T->d_tperm, (void*)T->d_bt0, (void*)T->d_btn, (void*)T->d_anc_ptr,
                   (void*)T->d_anc, (void*)T->d_clusters, (void*)T->d_items, (void*)T->d_boxes})
     cudaFree(q);
@@ -757,6 +763,7 @@ void tc_sizes(const TcLayout& L, int64_t* sizes) {
   sizes[6] = L.order;
   sizes[7] = L.n_trg_slots;
   sizes[8] = (int64_t)L.tclusters.size();
+  sizes[9] = L.direct ? 1 : 0;
 }
 
 }  // namespace
@@ -828,6 +835,23 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   if ((rc = tc_layout_from(kernel, digits, ns, r_src, nt, r_trg, prm, L, &T->batch_max))) {
     delete T;
     return rc;
+  }
+  if (L.direct) {  // the direct sum over the inputs as given
+    cudaError_t e = cudaSuccess;
+    auto up = [&](double** dst, const double* src, int64_t n) {
+      if (e != cudaSuccess) return;
+      e = cudaMalloc((void**)dst, std::max<size_t>((size_t)n * sizeof(double), 16));
+      if (e == cudaSuccess && n) e = cudaMemcpy(*dst, src, (size_t)n * sizeof(double), cudaMemcpyHostToDevice);
+    };
+    up(&T->d_xs, r_src, 3 * ns);
+    if (nd) up(&T->d_xn, n_src, 3 * ns);
+    up(&T->d_xt, r_trg, 3 * nt);
+    if (e != cudaSuccess) {
+      tc_free(T);
+      return runtime_record(e);
+    }
+    *out = T;
+    return SCTLGPU_OK;
   }
   // source slots: sources (sorted, padded), then the source proxies
   const int64_t S = L.n_slots;
@@ -964,10 +988,13 @@ int sctlgpu_treecode_execute(sctlgpu_treecode T, const double* v_src, double* v_
   if (bout && (e = cudaMemcpyAsync(v_out, T->h_out, bout, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
     return runtime_record(e);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return runtime_record(e);
-  return sctlgpu_near_plan_status(T->plan, stream);
+  return T->plan ? sctlgpu_near_plan_status(T->plan, stream) : SCTLGPU_OK;
 }
 
 static int tc_execute_device(sctlgpu_treecode T, const double* v_src, double* v_out, unsigned flags, void* stream) {
+  if (T->L.direct)
+    return sctlgpu_eval(T->kernel, T->mode, T->digits, T->nt, T->d_xt, T->ns, T->d_xs, T->d_xn, v_src, v_out,
+                        (flags & SCTLGPU_ACCUMULATE) | SCTLGPU_DEVICE_PTRS, stream);
   cudaStream_t st = (cudaStream_t)stream;
   const TcLayout& L = T->L;
   cudaError_t e = cudaSuccess;
@@ -1032,6 +1059,10 @@ int sctlgpu_treecode_info(sctlgpu_treecode T, int64_t* stats, double* theta) {
 
 int sctlgpu_treecode_status(sctlgpu_treecode T, void* stream) {
   if (!T) return SCTLGPU_ERR_NULL_POINTER;
+  if (!T->plan) {  // the direct form: the runtime's status word
+    const cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    return e == cudaSuccess ? sctlgpu_device_status(stream) : runtime_record(e);
+  }
   return sctlgpu_near_plan_status(T->plan, stream);
 }
 

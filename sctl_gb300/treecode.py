@@ -35,7 +35,7 @@ def _params(order, theta, leaf_max, batch_max, dual=True, theta_trg=0.0):
 
 
 _SIZE_KEYS = ("blocks", "source_slots", "slots", "clusters", "direct_interactions", "proxy_interactions", "order",
-              "target_list", "target_clusters")
+              "target_list", "target_clusters", "direct_fallback")
 
 
 class Treecode:
@@ -76,7 +76,7 @@ class Treecode:
         return out
 
     def info(self):
-        sizes = (ctypes.c_int64 * 9)()
+        sizes = (ctypes.c_int64 * 10)()
         th = ctypes.c_double()
         capi.check(capi.load().sctlgpu_treecode_info(self._h, sizes, ctypes.byref(th)), "sctlgpu_treecode_info")
         d = dict(zip(_SIZE_KEYS, list(sizes)))
@@ -111,7 +111,7 @@ def layout(kernel, r_src, r_trg, digits: int = 10, order=0, theta=0.0, leaf_max=
     ns, nt = xs.size // 3, xt.size // 3
     lib = capi.load()
     prm = _params(order, theta, leaf_max, batch_max, dual, theta_trg)
-    sizes = (ctypes.c_int64 * 9)()
+    sizes = (ctypes.c_int64 * 10)()
     th = ctypes.c_double()
     args = (k, ns, xs.ctypes.data if ns else None, nt, xt.ctypes.data if nt else None, ctypes.byref(prm), int(digits))
     capi.check(lib.sctlgpu_treecode_layout(*args, sizes, ctypes.byref(th), None, None, None, None, None),

@@ -66,7 +66,7 @@ int main() {
       rc = sctlgpu_treecode_create(&tc, kid, SCTLGPU_MIXED, digits, ns, xs.data(), xn.data(), nt, xt.data(), nullptr);
       CHECK(rc == SCTLGPU_OK && tc, "create rc %d", rc);
       if (!tc) continue;
-      int64_t sizes[9];
+      int64_t sizes[10];
       double theta = 0;
       sctlgpu_treecode_info(tc, sizes, &theta);
       CHECK(sizes[5] > 0, "kernel %d digits %d: no proxy interactions", kid, digits);

@@ -5,8 +5,8 @@ a target sample, and the GPU direct sum on whole target sets.
 Tolerance: relative l2 of the potentials within 10^-digits (the accuracy `digits` asks of
 ParticleFMM, SetAccuracy fmm-wrapper.txx:270-281) for digits 6 and 10, on the sphere/ball
 workload, clustered sources and the torus far field; plus the accumulate flag, an all-direct
-tree (one leaf) that must agree with the direct sum to rounding, and repeated evaluations
-with new densities.
+tree (one leaf) that must agree with the direct sum to rounding, the fallback to the direct sum
+where the traversal saves too little, and repeated evaluations with new densities.
 """
 import numpy as np
 import pytest
@@ -67,8 +67,9 @@ def test_treecode_clusters_f64_and_mixed(cuda, digits):
 def test_treecode_accumulate_and_new_densities(cuda):
     torch = cuda
     k = 2
-    d = W.sphere_ball(1 << 16, 1 << 13, k, seed=9)
-    tc = TC.Treecode(k, d["r_src"], d["r_trg"], digits=8)
+    d = W.sphere_ball(1 << 18, 1 << 14, k, seed=9)
+    tc = TC.Treecode(k, d["r_src"], d["r_trg"], digits=6)
+    assert tc.info()["direct_fallback"] == 0
     v1 = dev(torch, d["v_src"])
     v2 = dev(torch, np.random.default_rng(1).standard_normal(d["v_src"].size))
     u1 = tc.eval(v1).clone()
@@ -86,14 +87,14 @@ def test_treecode_coincident_targets_and_particle_cluster_form(cuda):
     with the dual traversal and with the particle-cluster form."""
     torch = cuda
     k = 1
-    d = W.sphere_ball(1 << 17, 1 << 13, k, seed=21)
+    d = W.sphere_ball(1 << 18, 1 << 13, k, seed=21)
     xt = d["r_trg"].copy()
     xt[:3000] = xt[0]
     sub = np.r_[0:5, 2990:3010, np.arange(3010, 1 << 13, 64)]
     ref = O.eval(k, xt[sub], d["r_src"], d["n_src"], d["v_src"])
     for dual in (True, False):
         tc = TC.Treecode(k, d["r_src"], xt, n_src=d["n_src"], digits=10, dual=dual)
-        assert tc.info()["proxy_interactions"] > 0
+        assert tc.info()["proxy_interactions"] > 0 and tc.info()["direct_fallback"] == 0
         u = tc.eval(dev(torch, d["v_src"])).cpu().numpy()
         assert O.rel_l2(u[sub], ref) < 1e-10, dual
         assert np.abs(u[:3000] - u[0]).max() <= 1e-12 * abs(u[0])
@@ -124,6 +125,23 @@ def test_treecode_sources_as_targets_and_flat_sources(cuda):
     u = tc.eval(dev(torch, f)).cpu().numpy()
     sub = np.arange(0, nt, 31)
     assert O.rel_l2(u[sub], O.eval(k, xt[sub], xs, xn, f)) < 1e-10
+
+
+def test_treecode_falls_back_to_the_direct_sum(cuda):
+    """A geometry where the traversal would keep over three quarters of Ns * Nt: evaluations run
+    the direct sum, identical to sctlgpu_eval on the same arrays."""
+    torch = cuda
+    k = 2
+    d = W.sphere_ball(1 << 16, 1 << 13, k, seed=9)
+    tc = TC.Treecode(k, d["r_src"], d["r_trg"], digits=8)
+    assert tc.info()["direct_fallback"] == 1
+    u = tc.eval(dev(torch, d["v_src"])).cpu().numpy()
+    ref = S.Stokes3D_FxU.Eval(None, d["r_trg"], d["r_src"], None, d["v_src"], digits=8, mode="mixed")
+    np.testing.assert_array_equal(u, ref)
+    out = torch.from_numpy(u.copy()).cuda()
+    tc.eval(dev(torch, d["v_src"]), out=out, accumulate=True)
+    np.testing.assert_allclose(out.cpu().numpy(), 2 * u, rtol=1e-15, atol=0)
+    assert tc.status() == capi.OK
 
 
 def test_treecode_single_leaf_is_the_direct_sum(cuda):
