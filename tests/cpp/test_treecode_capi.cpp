@@ -120,7 +120,7 @@ int main() {
     for (auto& x : F.v) x = nrm(rng);
     sctlgpu::set_double_mode(SCTLGPU_MIXED);
     sctlgpu::GpuFarField<SCTLGPU_LAPLACE3D_DXU> fmm;
-    fmm.SetAccuracy(10);
+    fmm.SetAccuracy(6);  // the treecode saves most at low digits: this geometry keeps the treecode path
     fmm.SetSrcCoord(Xs, Xn);
     fmm.SetSrcDensity(F);
     fmm.SetTrgCoord(Xt);
@@ -128,7 +128,7 @@ int main() {
     fmm.EvalDirect(Ud);
     const double err = rel_l2(U.v, Ud.v);
     std::printf("GpuFarField Laplace3D_DxU, %ld targets: Eval vs EvalDirect rel l2 %.2e\n", nt2, err);
-    CHECK(U.Dim() == nt2 && err < 1e-10 && err > 0, "GpuFarField treecode %.3e", err);
+    CHECK(U.Dim() == nt2 && err < 1e-6 && err > 0, "GpuFarField treecode %.3e", err);
     Vec Xt_small{std::vector<double>(xt.begin(), xt.begin() + 3 * 1000)};
     fmm.SetTrgCoord(Xt_small);
     fmm.Eval(U);
