@@ -705,7 +705,7 @@ using namespace sctlgpu;
 struct sctlgpu_treecode_s {
   int kernel = 0, mode = 0, digits = 0, ND = 0, SD = 0, TD = 0;
   bool df = false;  // moments and downward pass in double-float (plans in FP32 or double-float arithmetic)
-  int device = 0, batch_max = 0;
+  int device = 0, sms = 1, batch_max = 0;
   TcLayout L;
   int64_t ns = 0, nt = 0, n_items = 0, n_pieces = 0;
   double *d_trg = nullptr, *d_r = nullptr, *d_n = nullptr, *d_v = nullptr, *d_part = nullptr, *d_u = nullptr;
@@ -828,6 +828,7 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   T->SD = sd;
   T->TD = td;
   T->device = dev;
+  T->sms = sms;
   T->ns = ns;
   T->nt = nt;
   T->df = mode == SCTLGPU_MIXED && runtime_mixed_arith(runtime_effective_digits(mode, digits)) != MIXED_ARITH_F64;
@@ -1001,7 +1002,7 @@ static int tc_execute_device(sctlgpu_treecode T, const double* v_src, double* v_
   if (T->nt == 0) return SCTLGPU_OK;
   if (L.n_src_slots) {
     const int64_t work = L.n_src_slots * T->SD;
-    tc_gather_kernel<<<(unsigned)std::min<int64_t>((work + 255) / 256, 152 * 16), 256, 0, st>>>(
+    tc_gather_kernel<<<(unsigned)std::min<int64_t>((work + 255) / 256, (int64_t)T->sms * 16), 256, 0, st>>>(
         L.n_src_slots, T->SD, T->d_slot_src, v_src, T->d_v);
     g_launches.fetch_add(1, std::memory_order_relaxed);
     if ((e = cudaGetLastError()) != cudaSuccess) return runtime_record(e);
