@@ -51,7 +51,8 @@ constexpr int TC_MAX_NP = 16;   // Chebyshev points per dimension (order + 1)
 constexpr int TC_CHUNK = 256;   // source slots per moment work item
 constexpr int TC_THREADS = 256;
 constexpr int TC_MAX_BATCH = 2048;
-constexpr double TC_DIRECT_FRACTION = 0.75;  // treecode interactions above this share of Ns * Nt: direct sum  // targets per batch (the downward pass keeps a batch's sums in shared memory)
+constexpr double TC_DIRECT_FRACTION = 0.75;  // treecode interactions above this share of Ns * Nt: direct sum
+constexpr double TC_MAX_PARTIAL_BYTES = 16e9;  // partial-moment buffer (2^20 sources, degree 11: 0.7-2 GB)  // targets per batch (the downward pass keeps a batch's sums in shared memory)
 
 struct TcNode {
   int64_t b = 0, e = 0;    // points [b, e) of the tree's permutation
@@ -890,6 +891,11 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   }
   T->n_items = (int64_t)hi.size();
   const int64_t npts = L.npts, Q = kernel == SCTLGPU_STOKES3D_DXU ? 9 : (kernel == SCTLGPU_LAPLACE3D_FXU ? 1 : 3);
+  // partial moments of every chunk (deterministic reduction): refuse what would not leave room
+  if ((double)T->n_items * npts * Q * sizeof(double) > TC_MAX_PARTIAL_BYTES) {
+    tc_free(T);
+    return SCTLGPU_ERR_TOO_LARGE;
+  }
   // target list: sorted targets, then the target clusters' proxies (their Chebyshev points)
   const int64_t NT = L.n_trg_slots;
   std::vector<double> htrg((size_t)NT * 3);
