@@ -283,8 +283,7 @@ int sctlgpu_near_list_destroy(sctlgpu_near_list list);
  * create: the geometry (host arrays; the reference's SetSrcCoord / SetTrgCoord,
  * fmm-wrapper.txx:505-540): source coordinates and normals (double-layer
  * kernels), target coordinates; builds both trees, the interaction blocks and
- * the device-side plan (SCTLGPU_ERR_TOO_LARGE where the per-chunk partial
- * moments would exceed 16 GB: ~10^8 sources at degree 15).  params may be NULL: order and theta then follow
+ * the device-side plan.  params may be NULL: order and theta then follow
  * `digits`, leaf_max = 1.5 proxy slots per cluster ((order+1)^3, three times
  * that for the Stokes double layer), batch_max = 512.
  * execute: v_src (ns * SrcDim, source order as given; SetDensitySL / DL) ->
@@ -314,6 +313,7 @@ typedef struct sctlgpu_treecode_params {
   int dual;      /* nonzero: target clusters interpolate too (cluster-cluster interactions, a downward pass);
                     0: particle-cluster only */
   double theta_trg; /* acceptance of target-side interpolation, <= theta; <= 0: theta */
+  double moment_bytes; /* device scratch for partial moments (more is done in passes); <= 0: 1e9 */
 } sctlgpu_treecode_params;
 typedef struct sctlgpu_treecode_s* sctlgpu_treecode;
 int sctlgpu_treecode_create(sctlgpu_treecode* tc, int kernel, int mode, int digits, int64_t ns, const double* r_src,

@@ -95,7 +95,8 @@ SIGNATURES = {
 class TreecodeParams(ctypes.Structure):
     """sctlgpu_treecode_params."""
     _fields_ = [("theta", ctypes.c_double), ("order", ctypes.c_int), ("leaf_max", ctypes.c_int),
-                ("batch_max", ctypes.c_int), ("dual", ctypes.c_int), ("theta_trg", ctypes.c_double)]
+                ("batch_max", ctypes.c_int), ("dual", ctypes.c_int), ("theta_trg", ctypes.c_double),
+                ("moment_bytes", ctypes.c_double)]
 NEAR_CLASSES = 10
 NOALLOC_SCRATCH_BYTES = 64 << 20
 

@@ -52,7 +52,7 @@ constexpr int TC_CHUNK = 256;   // source slots per moment work item
 constexpr int TC_THREADS = 256;
 constexpr int TC_MAX_BATCH = 2048;
 constexpr double TC_DIRECT_FRACTION = 0.75;  // treecode interactions above this share of Ns * Nt: direct sum
-constexpr double TC_MAX_PARTIAL_BYTES = 16e9;  // partial-moment buffer (2^20 sources, degree 11: 0.7-2 GB)  // targets per batch (the downward pass keeps a batch's sums in shared memory)
+constexpr double TC_PART_BYTES = 1e9;  // partial moments held at once (2^20 sources, degree 11: 0.7-2 GB in all)  // targets per batch (the downward pass keeps a batch's sums in shared memory)
 
 struct TcNode {
   int64_t b = 0, e = 0;    // points [b, e) of the tree's permutation
@@ -357,7 +357,8 @@ struct TcMomParams {
   const double* r;  // slot coordinates
   const double* n;  // slot normals (double-layer kernels)
   const double* v;  // slot densities
-  double* part;     // per item: npts x Q partial moments
+  double* part;     // per item of the pass: npts x Q partial moments
+  int item0, item1; // the pass's items [item0, item1)
   double* pn;       // proxy normals (Laplace double layer)
   double* pv;       // proxy densities
   int np;
@@ -419,7 +420,7 @@ __global__ void __launch_bounds__(TC_THREADS) tc_moments_kernel(TcMomParams p) {
   const int np = p.np, npts = np * np * np;
   double* Ls = tc_sm;                          // [TC_CHUNK][3][np]
   double* qs = tc_sm + TC_CHUNK * 3 * np;      // [TC_CHUNK][Q]
-  const TcItem it = p.items[blockIdx.x];
+  const TcItem it = p.items[p.item0 + blockIdx.x];
   const TcCluster C = p.clusters[it.cluster];
   for (int s = threadIdx.x; s < TC_CHUNK; s += blockDim.x) {
     const bool valid = s < it.n;
@@ -502,7 +503,7 @@ __global__ void __launch_bounds__(TC_THREADS) tc_moments_df_kernel(TcMomParams p
   const int np = p.np, npts = np * np * np;
   f2* Ls = reinterpret_cast<f2*>(tc_sm);  // [TC_CHUNK][3][np]
   f2* qs = Ls + TC_CHUNK * 3 * np;        // [TC_CHUNK][Q]
-  const TcItem it = p.items[blockIdx.x];
+  const TcItem it = p.items[p.item0 + blockIdx.x];
   const TcCluster C = p.clusters[it.cluster];
   for (int s = threadIdx.x; s < TC_CHUNK; s += blockDim.x) {
     const bool valid = s < it.n;
@@ -553,27 +554,34 @@ __global__ void tc_reduce_kernel(TcMomParams p, int n_clusters) {
   if (c >= n_clusters) return;
   const TcCluster C = p.clusters[c];
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < npts; k += gridDim.x * blockDim.x) {
+    // this pass's items of the cluster, in order; the pass holding the cluster's first item
+    // writes, later passes add (the same order of additions as one pass)
+    const int i0 = max(C.item0, p.item0), i1 = min(C.item1, p.item1);
+    if (i0 >= i1) continue;
     double m[Q];
     for (int q = 0; q < Q; ++q) m[q] = 0.0;
-    for (int it = C.item0; it < C.item1; ++it) {
-      const double* src = p.part + ((int64_t)it * npts + k) * Q;
+    for (int it = i0; it < i1; ++it) {
+      const double* src = p.part + ((int64_t)(it - p.item0) * npts + k) * Q;
 #pragma unroll
       for (int q = 0; q < Q; ++q) m[q] += src[q];
     }
+    const bool first = C.item0 >= p.item0;
+    auto put = [&](double* dst, double v) { *dst = first ? v : *dst + v; };
     if constexpr (KER == SCTLGPU_LAPLACE3D_FXU) {
-      p.pv[C.proxy + k] = m[0];
+      put(&p.pv[C.proxy + k], m[0]);
     } else if constexpr (KER == SCTLGPU_LAPLACE3D_DXU) {
-      for (int q = 0; q < 3; ++q) p.pn[(C.proxy + k) * 3 + q] = m[q];
+      for (int q = 0; q < 3; ++q) put(&p.pn[(C.proxy + k) * 3 + q], m[q]);
     } else if constexpr (KER == SCTLGPU_STOKES3D_FXU) {
-      for (int q = 0; q < 3; ++q) p.pv[(C.proxy + k) * 3 + q] = m[q];
+      for (int q = 0; q < 3; ++q) put(&p.pv[(C.proxy + k) * 3 + q], m[q]);
     } else {  // proxy (k, c): normal e_c, density M_k[c][:]
-      for (int q = 0; q < Q; ++q) p.pv[(C.proxy + 3 * k + q / 3) * 3 + q % 3] = m[q];
+      for (int q = 0; q < Q; ++q) put(&p.pv[(C.proxy + 3 * k + q / 3) * 3 + q % 3], m[q]);
     }
   }
 }
 
+// Moments in passes of at most `pass_items` chunks (the partial buffer's capacity).
 template <int KER>
-cudaError_t tc_launch_moments(const TcMomParams& p, int n_items, int n_clusters, bool df, cudaStream_t st) {
+cudaError_t tc_launch_moments(TcMomParams p, int n_items, int pass_items, int n_clusters, bool df, cudaStream_t st) {
   constexpr int Q = TcCharge<KER>::Q;
   if (n_items == 0) return cudaSuccess;
   // f2 and double tiles: both fit the same byte count (8 bytes per value)
@@ -581,13 +589,18 @@ cudaError_t tc_launch_moments(const TcMomParams& p, int n_items, int n_clusters,
   auto kern = df ? tc_moments_df_kernel<KER> : tc_moments_kernel<KER>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  kern<<<n_items, TC_THREADS, smem, st>>>(p);
-  g_launches.fetch_add(1, std::memory_order_relaxed);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const int npts = p.np * p.np * p.np;
-  tc_reduce_kernel<KER><<<dim3((npts + 255) / 256, n_clusters), 256, 0, st>>>(p, n_clusters);
-  g_launches.fetch_add(1, std::memory_order_relaxed);
-  return cudaGetLastError();
+  for (int i0 = 0; i0 < n_items; i0 += pass_items) {
+    p.item0 = i0;
+    p.item1 = std::min(n_items, i0 + pass_items);
+    kern<<<p.item1 - p.item0, TC_THREADS, smem, st>>>(p);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    tc_reduce_kernel<KER><<<dim3((npts + 255) / 256, n_clusters), 256, 0, st>>>(p, n_clusters);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 // Downward pass and output: every sorted target k gets its plan sum u[k] plus, for each of
@@ -709,6 +722,7 @@ struct sctlgpu_treecode_s {
   int device = 0, sms = 1, batch_max = 0;
   TcLayout L;
   int64_t ns = 0, nt = 0, n_items = 0, n_pieces = 0;
+  int pass_items = 1;  // moment chunks per pass
   double *d_trg = nullptr, *d_r = nullptr, *d_n = nullptr, *d_v = nullptr, *d_part = nullptr, *d_u = nullptr;
   double *h_in = nullptr, *h_out = nullptr;  // device staging of host-array executions (allocated on first use)
   double *d_xs = nullptr, *d_xn = nullptr, *d_xt = nullptr;  // the direct form: inputs in their own order
@@ -891,11 +905,11 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   }
   T->n_items = (int64_t)hi.size();
   const int64_t npts = L.npts, Q = kernel == SCTLGPU_STOKES3D_DXU ? 9 : (kernel == SCTLGPU_LAPLACE3D_FXU ? 1 : 3);
-  // partial moments of every chunk (deterministic reduction): refuse what would not leave room
-  if ((double)T->n_items * npts * Q * sizeof(double) > TC_MAX_PARTIAL_BYTES) {
-    tc_free(T);
-    return SCTLGPU_ERR_TOO_LARGE;
-  }
+  // partial moments per chunk, reduced per cluster in chunk order; at most TC_PART_BYTES of
+  // them at a time (more chunks: several passes)
+  const double part_bytes = prm && prm->moment_bytes > 0 ? prm->moment_bytes : TC_PART_BYTES;
+  T->pass_items = (int)std::max<int64_t>(
+      1, std::min<int64_t>(T->n_items, (int64_t)(part_bytes / (double)(npts * Q * sizeof(double)))));
   // target list: sorted targets, then the target clusters' proxies (their Chebyshev points)
   const int64_t NT = L.n_trg_slots;
   std::vector<double> htrg((size_t)NT * 3);
@@ -948,7 +962,7 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   up((void**)&T->d_anc_ptr, hanc_ptr.data(), hanc_ptr.size() * sizeof(int32_t));
   up((void**)&T->d_anc, hanc.data(), hanc.size() * sizeof(int32_t));
   if (e == cudaSuccess)
-    e = cudaMalloc((void**)&T->d_part, std::max<size_t>(16, (size_t)T->n_items * npts * Q * sizeof(double)));
+    e = cudaMalloc((void**)&T->d_part, std::max<size_t>(16, (size_t)T->pass_items * npts * Q * sizeof(double)));
   if (e == cudaSuccess) e = cudaMalloc((void**)&T->d_u, std::max<size_t>(16, (size_t)NT * td * sizeof(double)));
   if (e != cudaSuccess) {
     tc_free(T);
@@ -1044,10 +1058,10 @@ static int tc_execute_device(sctlgpu_treecode T, const double* v_src, double* v_
   }
   const int nc = (int)L.clusters.size(), ni = (int)T->n_items;
   switch (T->kernel) {
-    case SCTLGPU_LAPLACE3D_FXU: e = tc_launch_moments<SCTLGPU_LAPLACE3D_FXU>(p, ni, nc, T->df, st); break;
-    case SCTLGPU_LAPLACE3D_DXU: e = tc_launch_moments<SCTLGPU_LAPLACE3D_DXU>(p, ni, nc, T->df, st); break;
-    case SCTLGPU_STOKES3D_FXU: e = tc_launch_moments<SCTLGPU_STOKES3D_FXU>(p, ni, nc, T->df, st); break;
-    default: e = tc_launch_moments<SCTLGPU_STOKES3D_DXU>(p, ni, nc, T->df, st); break;
+    case SCTLGPU_LAPLACE3D_FXU: e = tc_launch_moments<SCTLGPU_LAPLACE3D_FXU>(p, ni, T->pass_items, nc, T->df, st); break;
+    case SCTLGPU_LAPLACE3D_DXU: e = tc_launch_moments<SCTLGPU_LAPLACE3D_DXU>(p, ni, T->pass_items, nc, T->df, st); break;
+    case SCTLGPU_STOKES3D_FXU: e = tc_launch_moments<SCTLGPU_STOKES3D_FXU>(p, ni, T->pass_items, nc, T->df, st); break;
+    default: e = tc_launch_moments<SCTLGPU_STOKES3D_DXU>(p, ni, T->pass_items, nc, T->df, st); break;
   }
   if (e != cudaSuccess) return runtime_record(e);
   int rc = sctlgpu_near_plan_execute(T->plan, T->d_trg, T->d_r, T->d_n, T->d_v, nullptr, T->d_u, SCTLGPU_DEVICE_PTRS,

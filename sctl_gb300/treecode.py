@@ -29,9 +29,9 @@ def _host(a):
     return np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
 
 
-def _params(order, theta, leaf_max, batch_max, dual=True, theta_trg=0.0):
+def _params(order, theta, leaf_max, batch_max, dual=True, theta_trg=0.0, moment_bytes=0.0):
     return capi.TreecodeParams(float(theta or 0.0), int(order or 0), int(leaf_max or 0), int(batch_max or 0),
-                               1 if dual else 0, float(theta_trg or 0.0))
+                               1 if dual else 0, float(theta_trg or 0.0), float(moment_bytes or 0.0))
 
 
 _SIZE_KEYS = ("blocks", "source_slots", "slots", "clusters", "direct_interactions", "proxy_interactions", "order",
@@ -40,7 +40,7 @@ _SIZE_KEYS = ("blocks", "source_slots", "slots", "clusters", "direct_interaction
 
 class Treecode:
     def __init__(self, kernel, r_src, r_trg, n_src=None, digits: int = 10, mode="mixed", order=0, theta=0.0,
-                 leaf_max=0, batch_max=0, dual=True, theta_trg=0.0):
+                 leaf_max=0, batch_max=0, dual=True, theta_trg=0.0, moment_bytes=0.0):
         self.kernel = capi.KERNEL_IDS[kernel] if isinstance(kernel, str) else int(kernel)
         self.mode = capi.MODE_IDS[mode] if isinstance(mode, str) else int(mode)
         self.digits = int(digits)
@@ -50,7 +50,7 @@ class Treecode:
         self.sd, self.td = sd, td
         lib = capi.load()
         h = ctypes.c_void_p()
-        prm = _params(order, theta, leaf_max, batch_max, dual, theta_trg)
+        prm = _params(order, theta, leaf_max, batch_max, dual, theta_trg, moment_bytes)
         rc = lib.sctlgpu_treecode_create(ctypes.byref(h), self.kernel, self.mode, self.digits, self.ns,
                                          xs.ctypes.data if xs.size else None,
                                          ns_.ctypes.data if ns_ is not None and ns_.size else None, self.nt,

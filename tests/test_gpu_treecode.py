@@ -127,6 +127,21 @@ def test_treecode_sources_as_targets_and_flat_sources(cuda):
     assert O.rel_l2(u[sub], O.eval(k, xt[sub], xs, xn, f)) < 1e-10
 
 
+def test_treecode_moments_in_passes_are_identical(cuda):
+    """A partial-moment scratch of 2 MB forces many moment passes; the per-cluster sums keep their
+    order, so the moments are those of the single pass (the potentials then agree to the order of
+    the plan's atomic additions)."""
+    torch = cuda
+    k = 3
+    d = W.sphere_ball(1 << 18, 1 << 14, k, seed=44)
+    v = dev(torch, d["v_src"])
+    a = TC.Treecode(k, d["r_src"], d["r_trg"], n_src=d["n_src"], digits=6).eval(v).cpu().numpy()
+    tc = TC.Treecode(k, d["r_src"], d["r_trg"], n_src=d["n_src"], digits=6, moment_bytes=2e6)
+    assert tc.info()["direct_fallback"] == 0 and tc.info()["clusters"] > 0
+    b = tc.eval(v).cpu().numpy()
+    assert O.rel_l2(b, a) < 1e-15
+
+
 def test_treecode_falls_back_to_the_direct_sum(cuda):
     """A geometry where the traversal would keep over three quarters of Ns * Nt: evaluations run
     the direct sum, identical to sctlgpu_eval on the same arrays."""
