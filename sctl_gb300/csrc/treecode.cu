@@ -34,7 +34,9 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <atomic>
 #include <numeric>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -82,9 +84,65 @@ void set_box(const double* X, const std::vector<int64_t>& perm, TcNode& nd) {
   nd.r = std::sqrt(r2);
 }
 
-// Octree on tight boxes: a node with more than `leaf_max` points is split at
-// its box centre into its non-empty octants (children consecutive, in octant
-// order, which is also their order in `perm`).
+// Splits node `id` of `nodes` at its box centre into its non-empty octants
+// (children appended consecutively, in octant order, which is also their order
+// in `perm`), the children's tight boxes gathered while the points are moved.
+// Returns false for a node that stays a leaf.
+bool split_node(const double* X, std::vector<int64_t>& perm, std::vector<int64_t>& tmp, std::vector<TcNode>& nodes,
+                int32_t id, int depth, int64_t leaf_max) {
+  const TcNode nd = nodes[id];
+  if (nd.e - nd.b <= leaf_max || depth >= 60) return false;
+  if (nd.hi[0] == nd.lo[0] && nd.hi[1] == nd.lo[1] && nd.hi[2] == nd.lo[2]) return false;  // coincident points
+  int64_t cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0}, off[8];
+  auto octant = [&](const double* x) {
+    return (x[0] > nd.c[0] ? 1 : 0) | (x[1] > nd.c[1] ? 2 : 0) | (x[2] > nd.c[2] ? 4 : 0);
+  };
+  for (int64_t i = nd.b; i < nd.e; ++i) ++cnt[octant(X + perm[i] * 3)];
+  off[0] = nd.b;
+  for (int o = 1; o < 8; ++o) off[o] = off[o - 1] + cnt[o - 1];
+  int64_t pos[8];
+  std::copy(off, off + 8, pos);
+  double lo[8][3], hi[8][3];
+  for (int o = 0; o < 8; ++o)
+    for (int d = 0; d < 3; ++d) {
+      lo[o][d] = INFINITY;
+      hi[o][d] = -INFINITY;
+    }
+  for (int64_t i = nd.b; i < nd.e; ++i) {
+    const double* x = X + perm[i] * 3;
+    const int o = octant(x);
+    for (int d = 0; d < 3; ++d) {
+      lo[o][d] = std::min(lo[o][d], x[d]);
+      hi[o][d] = std::max(hi[o][d], x[d]);
+    }
+    tmp[pos[o]++] = perm[i];
+  }
+  std::copy(tmp.begin() + nd.b, tmp.begin() + nd.e, perm.begin() + nd.b);
+  nodes[id].child0 = (int32_t)nodes.size();
+  for (int o = 0; o < 8; ++o) {
+    if (!cnt[o]) continue;
+    TcNode ch;
+    ch.parent = id;
+    ch.b = off[o];
+    ch.e = off[o] + cnt[o];
+    double r2 = 0;
+    for (int d = 0; d < 3; ++d) {
+      ch.lo[d] = lo[o][d];
+      ch.hi[d] = hi[o][d];
+      ch.c[d] = 0.5 * (ch.lo[d] + ch.hi[d]);
+      r2 += 0.25 * (ch.hi[d] - ch.lo[d]) * (ch.hi[d] - ch.lo[d]);
+    }
+    ch.r = std::sqrt(r2);
+    nodes.push_back(ch);
+    ++nodes[id].nchild;
+  }
+  return true;
+}
+
+// Octree on tight boxes: nodes with more than `leaf_max` points are split (split_node).  The
+// first levels are split in order until there are subtrees for every host thread; those are
+// built concurrently (disjoint ranges of `perm`) and appended in order, so the node numbering
+// keeps children consecutive and after their parent.
 void build_octree(const double* X, int64_t n, int64_t leaf_max, std::vector<int64_t>& perm,
                   std::vector<TcNode>& nodes) {
   perm.resize((size_t)n);
@@ -95,37 +153,55 @@ void build_octree(const double* X, int64_t n, int64_t leaf_max, std::vector<int6
   if (n == 0) return;
   set_box(X, perm, nodes[0]);
   std::vector<int64_t> tmp((size_t)n);
-  std::vector<std::pair<int32_t, int>> stack{{0, 0}};
-  while (!stack.empty()) {
-    const auto [id, depth] = stack.back();
-    stack.pop_back();
-    const TcNode nd = nodes[id];
-    if (nd.e - nd.b <= leaf_max || depth >= 60) continue;
-    if (nd.hi[0] == nd.lo[0] && nd.hi[1] == nd.lo[1] && nd.hi[2] == nd.lo[2]) continue;  // coincident points
-    int64_t cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0}, off[8];
-    auto octant = [&](int64_t p) {
-      const double* x = X + p * 3;
-      return (x[0] > nd.c[0] ? 1 : 0) | (x[1] > nd.c[1] ? 2 : 0) | (x[2] > nd.c[2] ? 4 : 0);
-    };
-    for (int64_t i = nd.b; i < nd.e; ++i) ++cnt[octant(perm[i])];
-    off[0] = nd.b;
-    for (int o = 1; o < 8; ++o) off[o] = off[o - 1] + cnt[o - 1];
-    int64_t pos[8];
-    std::copy(off, off + 8, pos);
-    for (int64_t i = nd.b; i < nd.e; ++i) tmp[pos[octant(perm[i])]++] = perm[i];
-    std::copy(tmp.begin() + nd.b, tmp.begin() + nd.e, perm.begin() + nd.b);
-    nodes[id].child0 = (int32_t)nodes.size();
-    for (int o = 0; o < 8; ++o) {
-      if (!cnt[o]) continue;
-      TcNode ch;
-      ch.parent = id;
-      ch.b = off[o];
-      ch.e = off[o] + cnt[o];
-      set_box(X, perm, ch);
-      nodes.push_back(ch);
-      ++nodes[id].nchild;
+  const int nthreads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  // breadth-first to a frontier of >= 4 subtrees per thread (or until nothing splits)
+  std::vector<std::pair<int32_t, int>> frontier{{0, 0}};
+  while (frontier.size() < (size_t)4 * nthreads) {
+    std::vector<std::pair<int32_t, int>> next;
+    bool any = false;
+    for (const auto& [id, depth] : frontier) {
+      if (split_node(X, perm, tmp, nodes, id, depth, leaf_max)) {
+        any = true;
+        for (int k = 0; k < nodes[id].nchild; ++k) next.push_back({nodes[id].child0 + k, depth + 1});
+      }
     }
-    for (int k = nodes[id].nchild - 1; k >= 0; --k) stack.push_back({nodes[id].child0 + k, depth + 1});
+    if (!any) return;
+    frontier.swap(next);
+  }
+  // each frontier node's subtree in a local node list (local node 0 = the frontier node)
+  std::vector<std::vector<TcNode>> local(frontier.size());
+  std::atomic<size_t> next_task{0};
+  auto work = [&] {
+    for (size_t f = next_task++; f < frontier.size(); f = next_task++) {
+      std::vector<TcNode>& L = local[f];
+      L.assign(1, nodes[frontier[f].first]);
+      L[0].child0 = -1;
+      L[0].nchild = 0;
+      std::vector<std::pair<int32_t, int>> stack{{0, frontier[f].second}};
+      while (!stack.empty()) {
+        const auto [id, depth] = stack.back();
+        stack.pop_back();
+        if (!split_node(X, perm, tmp, L, id, depth, leaf_max)) continue;
+        for (int k = L[id].nchild - 1; k >= 0; --k) stack.push_back({L[id].child0 + k, depth + 1});
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int w = 1; w < nthreads; ++w) pool.emplace_back(work);
+  work();
+  for (auto& th : pool) th.join();
+  for (size_t f = 0; f < frontier.size(); ++f) {  // append, renumbering local ids
+    const int32_t g = frontier[f].first, base = (int32_t)nodes.size() - 1;  // local id i >= 1 -> base + i
+    const std::vector<TcNode>& L = local[f];
+    if (L[0].nchild == 0) continue;
+    nodes[g].child0 = base + L[0].child0;
+    nodes[g].nchild = L[0].nchild;
+    for (size_t i = 1; i < L.size(); ++i) {
+      TcNode nd = L[i];
+      nd.parent = nd.parent == 0 ? g : base + nd.parent;
+      if (nd.nchild) nd.child0 += base;
+      nodes.push_back(nd);
+    }
   }
 }
 
@@ -198,8 +274,11 @@ int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, con
     L.xcheb[m] = std::cos(M_PI * m / order);
     L.wcheb[m] = (m % 2 ? -1.0 : 1.0) * ((m == 0 || m == order) ? 0.5 : 1.0);
   }
-  build_octree(r_src, ns, leaf_max, L.sperm, L.src);
-  build_octree(r_trg, nt, batch_max, L.tperm, L.trg);
+  {  // the two trees are independent
+    std::thread tt([&] { build_octree(r_trg, nt, batch_max, L.tperm, L.trg); });
+    build_octree(r_src, ns, leaf_max, L.sperm, L.src);
+    tt.join();
+  }
   // source slots: leaves in permutation order, each padded to an even count
   std::vector<int32_t> leaves;
   for (int32_t i = 0; i < (int32_t)L.src.size(); ++i)
