@@ -192,6 +192,25 @@ def test_near_matrix_apply_general_layout(cuda, k0, k1):
                                                   g["K"].data_ptr(), K2.data_ptr(), F.size, g["F"].data_ptr(),
                                                   U3.data_ptr(), None) == capi.ERR_INVALID_ARGUMENT
     assert capi.load().sctlgpu_device_status(None) == capi.OK
+    # an element index out of range: resolved as invalid, skipped and flagged when applied
+    bad = int(order[0])
+    pe_bad = pe.copy()
+    pe_bad[bad] = n_elem + 5
+    g["pe_bad"] = d(pe_bad)
+    assert lib.sctlgpu_near_matrix_resolve(k0, k1, n_pairs, g["ord"].data_ptr(), n_pairs, g["pe_bad"].data_ptr(),
+                                           g["kd"].data_ptr(), n_elem, g["ed"].data_ptr(), g["ec"].data_ptr(),
+                                           K.size, F.size, res.data_ptr(), None) == capi.OK
+    U4 = d(U0, torch.float64)
+    assert lib.sctlgpu_near_matrix_apply_resolved(k0, k1, nt, g["tdsp"].data_ptr(), n_pairs, res.data_ptr(), K.size,
+                                                  g["K"].data_ptr(), None, F.size, g["F"].data_ptr(), U4.data_ptr(),
+                                                  None) == capi.OK
+    assert capi.load().sctlgpu_device_status(None) == capi.ERR_DEVICE_TIMEOUT  # status bit 4: a pair skipped
+    assert capi.load().sctlgpu_device_status(None) == capi.OK  # reading clears it
+    n = cnt[pe[bad]] * k0
+    blk = K[kdsp[bad]:kdsp[bad] + n * k1].reshape(k1, n)
+    want4 = want.copy()
+    want4[pt[bad] * k1:(pt[bad] + 1) * k1] -= blk @ F[dsp[pe[bad]] * k0:dsp[pe[bad]] * k0 + n]
+    np.testing.assert_allclose(U4.cpu().numpy(), want4, rtol=1e-12, atol=1e-12)
 
 
 @pytest.mark.parametrize("kernel", [0, 1])
