@@ -268,7 +268,7 @@ int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, con
   L.per_point = kernel == SCTLGPU_STOKES3D_DXU ? 3 : 1;
   L.proxy_slots = (L.npts * L.per_point + 1) / 2 * 2;
   L.theta = theta;
-  if (leaf_max <= 0) leaf_max = std::max<int64_t>(64, (3 * (int64_t)L.npts * L.per_point) / 2);
+  if (leaf_max <= 0) leaf_max = std::max<int64_t>(64, (int64_t)L.npts * L.per_point);
   if (batch_max <= 0) batch_max = 512;
   for (int m = 0; m <= order; ++m) {  // Chebyshev points of the second kind and their barycentric weights
     L.xcheb[m] = std::cos(M_PI * m / order);
