@@ -285,7 +285,8 @@ int sctlgpu_near_list_destroy(sctlgpu_near_list list);
  * kernels), target coordinates; builds both trees, the interaction blocks and
  * the device-side plan.  params may be NULL: order and theta then follow
  * `digits`, leaf_max = the proxy slots per cluster ((order+1)^3, three times
- * that for the Stokes double layer), batch_max = 512.
+ * that for the Stokes double layer), batch_max = 512 or 256, whichever leaves
+ * fewer interactions (512 unless 256 saves 3 %).
  * execute: v_src (ns * SrcDim, source order as given; SetDensitySL / DL) ->
  * v_out (nt * TrgDim, target order as given); flags may hold
  * SCTLGPU_ACCUMULATE.  Host arrays (synchronous, staged through device buffers
@@ -309,7 +310,7 @@ typedef struct sctlgpu_treecode_params {
   double theta;  /* a pair of clusters is separated when (r_trg + r_src) < theta * distance; <= 0: from digits */
   int order;     /* interpolation degree per dimension, 1..15; <= 0: from digits */
   int leaf_max;  /* sources per leaf; <= 0: the proxy slots per cluster */
-  int batch_max; /* targets per batch, <= 2048; <= 0: 512 */
+  int batch_max; /* targets per batch, <= 2048; <= 0: 512 or 256 (fewer interactions) */
   int dual;      /* nonzero: target clusters interpolate too (cluster-cluster interactions, a downward pass);
                     0: particle-cluster only */
   double theta_trg; /* acceptance of target-side interpolation, <= theta; <= 0: theta */

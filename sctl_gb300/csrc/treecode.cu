@@ -841,10 +841,29 @@ int tc_layout_from(int kernel, int digits, int64_t ns, const double* r_src, int6
   int order = prm ? prm->order : 0;
   double theta = prm ? prm->theta : 0.0;
   tc_defaults(digits, &order, &theta);
-  const int bm = prm && prm->batch_max > 0 ? prm->batch_max : 512;
-  if (batch_max) *batch_max = bm;
-  return tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, prm ? prm->theta_trg : 0.0,
-                         prm ? prm->leaf_max : 0, bm, !prm || prm->dual != 0, L);
+  const double theta_trg = prm ? prm->theta_trg : 0.0;
+  const int64_t leaf = prm ? prm->leaf_max : 0;
+  const bool dual = !prm || prm->dual != 0;
+  if (prm && prm->batch_max > 0) {
+    if (batch_max) *batch_max = prm->batch_max;
+    return tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, theta_trg, leaf, prm->batch_max, dual, L);
+  }
+  // Batches of 512 and of 256 targets: the one with fewer interactions, the larger on a near tie
+  // (fewer blocks).  Targets filling a volume favour 256 (sphere/ball: 0.147 vs 0.166 of Ns * Nt
+  // at digits 10, 7-17 % faster), targets hugging a surface tie (torus).
+  int rc = tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, theta_trg, leaf, 512, dual, L);
+  if (rc) return rc;
+  if (batch_max) *batch_max = 512;
+  if (nt > 512) {
+    TcLayout S;
+    rc = tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, theta_trg, leaf, 256, dual, S);
+    if (rc) return rc;
+    if ((double)(S.pp + S.approx) < 0.97 * (double)(L.pp + L.approx)) {
+      L = std::move(S);
+      if (batch_max) *batch_max = 256;
+    }
+  }
+  return SCTLGPU_OK;
 }
 
 void tc_sizes(const TcLayout& L, int64_t* sizes) {
