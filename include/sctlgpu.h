@@ -274,7 +274,9 @@ int sctlgpu_near_list_destroy(sctlgpu_near_list list);
  * the four hot-path kernels, with work below the direct sum's Ns * Nt.  The
  * algorithm differs from PVFMM's (a barycentric Lagrange treecode over a
  * source and a target tree: separated clusters are replaced by proxies at
- * (order+1)^3 Chebyshev points -- source proxies carry interpolated moments,
+ * the tensor-product Chebyshev points of their boxes, up to order+1 per
+ * dimension (fewer along a side much thinner than the longest, one along a side
+ * of zero extent) -- source proxies carry interpolated moments,
  * target proxies collect potentials that a downward pass interpolates to the
  * targets -- and everything else is summed directly); every
  * interaction runs in the batched near-field kernels with `mode` / `digits`
@@ -284,7 +286,7 @@ int sctlgpu_near_list_destroy(sctlgpu_near_list list);
  * fmm-wrapper.txx:505-540): source coordinates and normals (double-layer
  * kernels), target coordinates; builds both trees, the interaction blocks and
  * the device-side plan.  params may be NULL: order and theta then follow
- * `digits`, leaf_max = the proxy slots per cluster ((order+1)^3, three times
+ * `digits`, leaf_max = the proxy slots of a full grid ((order+1)^3, three times
  * that for the Stokes double layer), batch_max = 512 or 256, whichever leaves
  * fewer interactions (512 unless 256 saves 3 %).
  * execute: v_src (ns * SrcDim, source order as given; SetDensitySL / DL) ->
@@ -302,14 +304,15 @@ int sctlgpu_near_list_destroy(sctlgpu_near_list list);
  * direct sum instead}, and the acceptance parameter.  layout is the host-only part of create (no device
  * needed): the blocks (sources index the source slots, targets the target
  * list), the source of every slot (-1 padding, -2 proxy), the target order,
- * per source cluster with proxies {slot begin, end, proxy slot begin, end}
- * and per target cluster with proxies {target begin, end, proxy begin, end};
- * any output may be NULL.
+ * per source cluster with proxies {slot begin, end, proxy slot begin, end,
+ * grid points along x, y, z} and per target cluster with proxies {target begin,
+ * end, proxy begin, end, grid points along x, y, z} (7 entries each); any
+ * output may be NULL.
  */
 typedef struct sctlgpu_treecode_params {
   double theta;  /* a pair of clusters is separated when (r_trg + r_src) < theta * distance; <= 0: from digits */
   int order;     /* interpolation degree per dimension, 1..15; <= 0: from digits */
-  int leaf_max;  /* sources per leaf; <= 0: the proxy slots per cluster */
+  int leaf_max;  /* sources per leaf; <= 0: the proxy slots of a full grid */
   int batch_max; /* targets per batch, <= 2048; <= 0: 512 or 256 (fewer interactions) */
   int dual;      /* nonzero: target clusters interpolate too (cluster-cluster interactions, a downward pass);
                     0: particle-cluster only */

@@ -16,8 +16,9 @@
 //  * traversal per batch from the root: a cluster is approximated when
 //    (r_batch + r_cluster) < theta |c_batch - c_cluster| and it holds more
 //    sources than proxy slots, a leaf is summed directly, anything else descends.
-//  * an approximated cluster carries (order + 1)^3 proxy sources at the
-//    tensor-product Chebyshev points (second kind) of its box; with the
+//  * an approximated cluster carries proxy sources at the tensor-product
+//    Chebyshev points (second kind) of its box -- order + 1 along its longest
+//    side, fewer along a much thinner side (tc_grid) -- and with the
 //    Lagrange basis L_k, K(x, y) ~ sum_k L_k(y) K(x, z_k) for y in the box, so
 //    the proxies carry the moments M_k = sum_s L_k(y_s) q_s of the cluster's
 //    source charges q_s: the density (single layers), the density times the
@@ -63,6 +64,8 @@ struct TcNode {
   int32_t child0 = -1, nchild = 0;  // children are consecutive nodes
   int32_t parent = -1;
   int64_t proxy = -1;  // sources: first proxy slot; targets: first proxy entry of the target list
+  int32_t g[3] = {1, 1, 1};  // Chebyshev points per dimension of the node's interpolation grid
+  int32_t npts = 1;          // g[0] * g[1] * g[2]
 };
 
 void set_box(const double* X, const std::vector<int64_t>& perm, TcNode& nd) {
@@ -225,8 +228,39 @@ double cheb_coord(double lo, double hi, double x) {
   return x >= 0 ? hi - 0.5 * (1.0 - x) * (hi - lo) : lo + 0.5 * (1.0 + x) * (hi - lo);
 }
 
+// Points per dimension of a cluster's interpolation grid.  Tensor-product Chebyshev
+// interpolation errs by about the sum over the dimensions of rho_k^-(points_k - 1), where
+// rho_k = s_k + sqrt(s_k^2 - 1) and s_k = (r / theta) / h_k is the closest distance the
+// acceptance test admits (r / theta from the centre) in half-widths h_k of that side.  The
+// longest side keeps the full order; a thinner side -- a patch of a surface seen edge-on -- gets
+// the fewest points whose term stays below a third of the longest side's, and a side of zero
+// extent one point (its coordinate is the same for every point of the cluster: exact).  (A
+// tenth measured the same errors and ran 3-10 % slower; equal terms raised the sphere/ball error
+// at digits 10 from 3e-12 to 1.7e-11.)
+void tc_grid(TcNode& C, int order, double theta) {
+  double h[3], hmax = 0;
+  for (int d = 0; d < 3; ++d) {
+    h[d] = 0.5 * (C.hi[d] - C.lo[d]);
+    hmax = std::max(hmax, h[d]);
+  }
+  auto lrho = [](double s) { return std::log(s + std::sqrt(std::max(0.0, s * s - 1.0))); };
+  const double reach = C.r / theta;
+  const double need = hmax > 0 ? order * lrho(reach / hmax) + std::log(3.0) : 0.0;
+  C.npts = 1;
+  for (int d = 0; d < 3; ++d) {
+    int p = 0;
+    if (h[d] > 0) {
+      const double l = lrho(reach / h[d]);
+      p = l > 0 ? (int)std::ceil(need / l) : order;
+      p = std::min(order, std::max(1, p));
+    }
+    C.g[d] = p + 1;
+    C.npts *= p + 1;
+  }
+}
+
 struct TcLayout {
-  int order = 0, np = 0, npts = 0, per_point = 1, proxy_slots = 0;  // proxy_slots: per cluster, even
+  int order = 0, np = 0, npts = 0, per_point = 1;  // np, npts: the largest grid (order + 1 per dimension)
   double theta = 0;
   std::vector<TcNode> src, trg;
   std::vector<int64_t> sperm, tperm;
@@ -242,8 +276,33 @@ struct TcLayout {
   bool dual = true;
   bool direct = false;   // the traversal saves too little: evaluations run the direct sum
   double theta_trg = 0;  // acceptance for target-side interpolation (<= theta)
-  double xcheb[TC_MAX_NP], wcheb[TC_MAX_NP];
 };
+
+// Proxy slots of a source cluster: its grid points times the proxies per point, padded to an
+// even count (pair boundaries).
+int64_t tc_proxy_slots(const TcLayout& L, const TcNode& C) { return ((int64_t)C.npts * L.per_point + 1) / 2 * 2; }
+
+// Chebyshev points of the second kind of every degree (x_m = cos(pi m / p), m = 0..p) and their
+// barycentric weights (-1)^m, halved at the ends; degree 0 is the single point 1 with weight 1.
+struct TcCheb {
+  double x[TC_MAX_NP][TC_MAX_NP], w[TC_MAX_NP][TC_MAX_NP];
+  float xh[TC_MAX_NP][TC_MAX_NP], xl[TC_MAX_NP][TC_MAX_NP], wf[TC_MAX_NP][TC_MAX_NP];  // double-float points
+};
+const TcCheb& tc_cheb() {
+  static const TcCheb tab = [] {
+    TcCheb t{};
+    for (int p = 0; p < TC_MAX_NP; ++p)
+      for (int m = 0; m <= p; ++m) {
+        t.x[p][m] = p ? std::cos(M_PI * m / p) : 1.0;
+        t.w[p][m] = p ? (m % 2 ? -1.0 : 1.0) * ((m == 0 || m == p) ? 0.5 : 1.0) : 1.0;
+        t.xh[p][m] = (float)t.x[p][m];
+        t.xl[p][m] = (float)(t.x[p][m] - (double)t.xh[p][m]);
+        t.wf[p][m] = (float)t.w[p][m];  // +-1 or +-1/2: exact
+      }
+    return t;
+  }();
+  return tab;
+}
 
 // Default (order, theta) per digits: Chebyshev interpolation of K(x, .) on a box
 // seen from distance >= r / theta converges like rho^-order with
@@ -266,19 +325,16 @@ int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, con
   L.np = order + 1;
   L.npts = L.np * L.np * L.np;
   L.per_point = kernel == SCTLGPU_STOKES3D_DXU ? 3 : 1;
-  L.proxy_slots = (L.npts * L.per_point + 1) / 2 * 2;
   L.theta = theta;
   if (leaf_max <= 0) leaf_max = std::max<int64_t>(64, (int64_t)L.npts * L.per_point);
   if (batch_max <= 0) batch_max = 512;
-  for (int m = 0; m <= order; ++m) {  // Chebyshev points of the second kind and their barycentric weights
-    L.xcheb[m] = std::cos(M_PI * m / order);
-    L.wcheb[m] = (m % 2 ? -1.0 : 1.0) * ((m == 0 || m == order) ? 0.5 : 1.0);
-  }
   {  // the two trees are independent
     std::thread tt([&] { build_octree(r_trg, nt, batch_max, L.tperm, L.trg); });
     build_octree(r_src, ns, leaf_max, L.sperm, L.src);
     tt.join();
   }
+  for (TcNode& nd : L.src) tc_grid(nd, order, theta);
+  for (TcNode& nd : L.trg) tc_grid(nd, order, L.theta_trg);
   // source slots: leaves in permutation order, each padded to an even count
   std::vector<int32_t> leaves;
   for (int32_t i = 0; i < (int32_t)L.src.size(); ++i)
@@ -308,7 +364,6 @@ int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, con
   // a side may use its proxies only when it holds more points than proxies; otherwise the
   // larger node (by radius) is split, and two leaves are summed directly.  Without `dual`,
   // every batch starts from the source root and only the source side is ever approximated.
-  const int64_t Ps = (int64_t)L.npts * L.per_point, Pt = L.npts;
   struct Rec {
     int32_t t, s;
     char kind;  // 0 direct, 1 source proxies, 2 target proxies, 3 both
@@ -334,6 +389,7 @@ int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, con
     const double dx = T.c[0] - S.c[0], dy = T.c[1] - S.c[1], dz = T.c[2] - S.c[2];
     const double dist = std::sqrt(dx * dx + dy * dy + dz * dz);
     const int64_t nT = T.e - T.b, nS = S.e - S.b, sS = S.se - S.sb;
+    const int64_t Ps = (int64_t)S.npts * L.per_point, Pt = T.npts;  // the clusters' proxies
     if (T.r + S.r < theta * dist) {
       // target-side interpolation (a target cluster's proxies) only under the stricter theta_trg
       const bool src_ok = nS > Ps, trg_ok = L.dual && nT > Pt && T.r + S.r < L.theta_trg * dist;
@@ -362,7 +418,7 @@ int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, con
   for (int32_t i = 0; i < (int32_t)L.src.size(); ++i)
     if (sused[i]) {
       L.src[i].proxy = pcur;
-      pcur += L.proxy_slots;
+      pcur += tc_proxy_slots(L, L.src[i]);
       L.clusters.push_back(i);
     }
   L.n_slots = pcur;
@@ -372,7 +428,7 @@ int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, con
   for (int32_t i = 0; i < (int32_t)L.trg.size(); ++i)
     if (tused[i]) {
       L.trg[i].proxy = tcur;
-      tcur += Pt;
+      tcur += L.trg[i].npts;
       tindex[i] = (int32_t)L.tclusters.size();
       L.tclusters.push_back(i);
     }
@@ -394,7 +450,8 @@ int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, con
   for (const Rec& r : recs) {
     const TcNode &T = L.trg[r.t], &S = L.src[r.s];
     const bool tp = r.kind & 2, sp = r.kind & 1;
-    bl.push_back({tp ? T.proxy : T.b, tp ? Pt : T.e - T.b, sp ? S.proxy : S.sb, sp ? S.proxy + Ps : S.se});
+    bl.push_back({tp ? T.proxy : T.b, tp ? (int64_t)T.npts : T.e - T.b, sp ? S.proxy : S.sb,
+                  sp ? S.proxy + tc_proxy_slots(L, S) : S.se});  // with the zero-charge padding slot
   }
   std::sort(bl.begin(), bl.end(), [](const Blk& a, const Blk& b) {
     return a.t0 != b.t0 ? a.t0 < b.t0 : (a.tn != b.tn ? a.tn < b.tn : a.s0 < b.s0);
@@ -424,6 +481,7 @@ struct TcCluster {
   double lo[3], inv[3];  // interpolation box: t = (y - lo) * inv - 1 in [-1, 1]
   int64_t proxy;         // first proxy slot
   int32_t item0, item1;  // moment work items [item0, item1)
+  int32_t g[3];          // grid points per dimension
 };
 struct TcItem {
   int32_t cluster;
@@ -440,9 +498,8 @@ struct TcMomParams {
   int item0, item1; // the pass's items [item0, item1)
   double* pn;       // proxy normals (Laplace double layer)
   double* pv;       // proxy densities
-  int np;
-  double x[TC_MAX_NP], w[TC_MAX_NP];
-  float xh[TC_MAX_NP], xl[TC_MAX_NP], wf[TC_MAX_NP];  // the points as double-float pairs; weights exact
+  int np;           // the largest grid's points per dimension (shared-memory stride)
+  const TcCheb* cheb;
 };
 
 template <int KER>
@@ -496,18 +553,19 @@ template <int KER>
 __global__ void __launch_bounds__(TC_THREADS) tc_moments_kernel(TcMomParams p) {
   constexpr int Q = TcCharge<KER>::Q;
   extern __shared__ double tc_sm[];
-  const int np = p.np, npts = np * np * np;
+  const int np = p.np, npmax3 = np * np * np;
   double* Ls = tc_sm;                          // [TC_CHUNK][3][np]
   double* qs = tc_sm + TC_CHUNK * 3 * np;      // [TC_CHUNK][Q]
   const TcItem it = p.items[p.item0 + blockIdx.x];
   const TcCluster C = p.clusters[it.cluster];
+  const int g0 = C.g[0], g1 = C.g[1], g2 = C.g[2], npts = g0 * g1 * g2;
   for (int s = threadIdx.x; s < TC_CHUNK; s += blockDim.x) {
     const bool valid = s < it.n;
     const int64_t slot = it.s0 + s;
     for (int d = 0; d < 3; ++d) {
       double t = valid ? (p.r[slot * 3 + d] - C.lo[d]) * C.inv[d] - 1.0 : 0.0;
       t = fmin(1.0, fmax(-1.0, t));
-      tc_lagrange(t, np, p.x, p.w, Ls + (s * 3 + d) * np);
+      tc_lagrange(t, C.g[d], p.cheb->x[C.g[d] - 1], p.cheb->w[C.g[d] - 1], Ls + (s * 3 + d) * np);
     }
     double q[Q];
     for (int c = 0; c < Q; ++c) q[c] = 0.0;
@@ -527,7 +585,7 @@ __global__ void __launch_bounds__(TC_THREADS) tc_moments_kernel(TcMomParams p) {
   }
   __syncthreads();
   for (int k = threadIdx.x; k < npts; k += blockDim.x) {
-    const int i = k / (np * np), j = (k / np) % np, l = k % np;
+    const int i = k / (g1 * g2), j = (k / g2) % g1, l = k % g2;
     double acc[Q];
     for (int c = 0; c < Q; ++c) acc[c] = 0.0;
     for (int s = 0; s < it.n; ++s) {
@@ -535,7 +593,7 @@ __global__ void __launch_bounds__(TC_THREADS) tc_moments_kernel(TcMomParams p) {
 #pragma unroll
       for (int c = 0; c < Q; ++c) acc[c] = fma(wgt, qs[s * Q + c], acc[c]);
     }
-    double* out = p.part + ((int64_t)blockIdx.x * npts + k) * Q;
+    double* out = p.part + ((int64_t)blockIdx.x * npmax3 + k) * Q;
 #pragma unroll
     for (int c = 0; c < Q; ++c) out[c] = acc[c];
   }
@@ -554,16 +612,16 @@ __device__ __forceinline__ f2 tc_split(double v) {
   const float h = (float)v;
   return {h, (float)(v - (double)h)};
 }
-// Barycentric Lagrange basis at t in double-float; P holds the points (xh, xl) and weights (wf).
-template <class P>
-__device__ __forceinline__ void tc_lagrange_df(double tt, int np, const P& p, f2* L) {
+// Barycentric Lagrange basis at t in double-float, for the np points of degree np - 1 of C.
+__device__ __forceinline__ void tc_lagrange_df(double tt, int np, const TcCheb* C, f2* L) {
+  const float *xh = C->xh[np - 1], *xl = C->xl[np - 1], *wf = C->wf[np - 1];
   const f2 t = tc_split(tt);
   int hit = -1;
   f2 sum = {0.f, 0.f};
   for (int m = 0; m < np; ++m) {
-    const f2 d = df_norm(df_add(t, {-p.xh[m], -p.xl[m]}));
+    const f2 d = df_norm(df_add(t, {-xh[m], -xl[m]}));
     if (d.h == 0.f) hit = m;
-    const f2 q = d.h != 0.f ? df_mulf(tc_rcp(d), p.wf[m]) : f2{0.f, 0.f};
+    const f2 q = d.h != 0.f ? df_mulf(tc_rcp(d), wf[m]) : f2{0.f, 0.f};
     L[m] = q;
     df_acc(sum, q);
   }
@@ -579,18 +637,19 @@ template <int KER>
 __global__ void __launch_bounds__(TC_THREADS) tc_moments_df_kernel(TcMomParams p) {
   constexpr int Q = TcCharge<KER>::Q;
   extern __shared__ double tc_sm[];
-  const int np = p.np, npts = np * np * np;
+  const int np = p.np, npmax3 = np * np * np;
   f2* Ls = reinterpret_cast<f2*>(tc_sm);  // [TC_CHUNK][3][np]
   f2* qs = Ls + TC_CHUNK * 3 * np;        // [TC_CHUNK][Q]
   const TcItem it = p.items[p.item0 + blockIdx.x];
   const TcCluster C = p.clusters[it.cluster];
+  const int g1 = C.g[1], g2 = C.g[2], npts = C.g[0] * g1 * g2;
   for (int s = threadIdx.x; s < TC_CHUNK; s += blockDim.x) {
     const bool valid = s < it.n;
     const int64_t slot = it.s0 + s;
     for (int d = 0; d < 3; ++d) {
       double t = valid ? (p.r[slot * 3 + d] - C.lo[d]) * C.inv[d] - 1.0 : 0.0;
       t = fmin(1.0, fmax(-1.0, t));
-      tc_lagrange_df(t, np, p, Ls + (s * 3 + d) * np);
+      tc_lagrange_df(t, C.g[d], p.cheb, Ls + (s * 3 + d) * np);
     }
     double q[Q];
     for (int c = 0; c < Q; ++c) q[c] = 0.0;
@@ -610,7 +669,7 @@ __global__ void __launch_bounds__(TC_THREADS) tc_moments_df_kernel(TcMomParams p
   }
   __syncthreads();
   for (int k = threadIdx.x; k < npts; k += blockDim.x) {
-    const int i = k / (np * np), j = (k / np) % np, l = k % np;
+    const int i = k / (g1 * g2), j = (k / g2) % g1, l = k % g2;
     f2 acc[Q];
     for (int c = 0; c < Q; ++c) acc[c] = {0.f, 0.f};
     for (int s = 0; s < it.n; ++s) {
@@ -618,7 +677,7 @@ __global__ void __launch_bounds__(TC_THREADS) tc_moments_df_kernel(TcMomParams p
 #pragma unroll
       for (int c = 0; c < Q; ++c) df_acc(acc[c], df_mul(wgt, qs[s * Q + c]));
     }
-    double* out = p.part + ((int64_t)blockIdx.x * npts + k) * Q;
+    double* out = p.part + ((int64_t)blockIdx.x * npmax3 + k) * Q;
 #pragma unroll
     for (int c = 0; c < Q; ++c) out[c] = (double)acc[c].h + (double)acc[c].l;
   }
@@ -628,10 +687,11 @@ __global__ void __launch_bounds__(TC_THREADS) tc_moments_df_kernel(TcMomParams p
 template <int KER>
 __global__ void tc_reduce_kernel(TcMomParams p, int n_clusters) {
   constexpr int Q = TcCharge<KER>::Q;
-  const int npts = p.np * p.np * p.np;
+  const int npmax3 = p.np * p.np * p.np;
   const int c = blockIdx.y;
   if (c >= n_clusters) return;
   const TcCluster C = p.clusters[c];
+  const int npts = C.g[0] * C.g[1] * C.g[2];
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < npts; k += gridDim.x * blockDim.x) {
     // this pass's items of the cluster, in order; the pass holding the cluster's first item
     // writes, later passes add (the same order of additions as one pass)
@@ -640,7 +700,7 @@ __global__ void tc_reduce_kernel(TcMomParams p, int n_clusters) {
     double m[Q];
     for (int q = 0; q < Q; ++q) m[q] = 0.0;
     for (int it = i0; it < i1; ++it) {
-      const double* src = p.part + ((int64_t)(it - p.item0) * npts + k) * Q;
+      const double* src = p.part + ((int64_t)(it - p.item0) * npmax3 + k) * Q;
 #pragma unroll
       for (int q = 0; q < Q; ++q) m[q] += src[q];
     }
@@ -686,10 +746,11 @@ cudaError_t tc_launch_moments(TcMomParams p, int n_items, int pass_items, int n_
 // its target clusters A with proxies (its batch and the batch's ancestors),
 // sum_k L_k(x) u[A's proxy k] -- the interpolation of the potentials the plan accumulated at
 // A's Chebyshev points -- and is written (or added) to out[perm[k]].  One CTA per batch, one
-// warp per target: the lanes split the (order+1)^3 terms, in double-float (DF) or FP64.
+// warp per target: the lanes split the cluster's grid points, in double-float (DF) or FP64.
 struct TcTrgBox {
   double lo[3], inv[3];
   int64_t proxy;  // first proxy entry of the target list
+  int32_t g[3];   // grid points per dimension
 };
 struct TcL2PParams {
   const TcTrgBox* boxes;
@@ -702,26 +763,26 @@ struct TcL2PParams {
   const int64_t* perm;  // sorted target -> output index
   double* out;
   int accumulate;
-  int np;
-  double x[TC_MAX_NP], w[TC_MAX_NP];
-  float xh[TC_MAX_NP], xl[TC_MAX_NP], wf[TC_MAX_NP];
+  int np;  // the largest grid's points per dimension (shared-memory size)
+  const TcCheb* cheb;
 };
 
 template <int TD, bool DF>
 __global__ void __launch_bounds__(TC_THREADS) tc_l2p_kernel(TcL2PParams p) {
   using V = typename std::conditional<DF, f2, double>::type;
   extern __shared__ double tc_sm[];
-  const int np = p.np, npts = np * np * np;
+  const int npmax3 = p.np * p.np * p.np;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   V* P = reinterpret_cast<V*>(tc_sm);                         // [npts][TD] proxy potentials of one cluster
-  V* Lw = P + (size_t)npts * TD + warp * 3 * TC_MAX_NP;       // per warp: [3][np] basis values
-  double* acc_t = tc_sm + (size_t)npts * TD + nwarps * 3 * TC_MAX_NP;  // [batch_max][TD] target sums
+  V* Lw = P + (size_t)npmax3 * TD + warp * 3 * TC_MAX_NP;     // per warp: [3][points] basis values
+  double* acc_t = tc_sm + (size_t)npmax3 * TD + nwarps * 3 * TC_MAX_NP;  // [batch_max][TD] target sums
   const int b = blockIdx.x;
   const int64_t t0 = p.bt0[b];
   const int tn = p.btn[b];
   for (int e = threadIdx.x; e < tn * TD; e += blockDim.x) acc_t[e] = p.u[t0 * TD + e];
   for (int a = p.anc_ptr[b]; a < p.anc_ptr[b + 1]; ++a) {
     const TcTrgBox A = p.boxes[p.anc[a]];
+    const int g1 = A.g[1], g2 = A.g[2], npts = A.g[0] * g1 * g2;
     __syncthreads();
     for (int e = threadIdx.x; e < npts * TD; e += blockDim.x) {
       const double v = p.u[A.proxy * TD + e];
@@ -736,16 +797,17 @@ __global__ void __launch_bounds__(TC_THREADS) tc_l2p_kernel(TcL2PParams p) {
       if (lane < 3) {
         double tt = (p.r[k * 3 + lane] - A.lo[lane]) * A.inv[lane] - 1.0;
         tt = fmin(1.0, fmax(-1.0, tt));
+        const int gd = A.g[lane];
         if constexpr (DF)
-          tc_lagrange_df(tt, np, p, Lw + lane * TC_MAX_NP);
+          tc_lagrange_df(tt, gd, p.cheb, Lw + lane * TC_MAX_NP);
         else
-          tc_lagrange(tt, np, p.x, p.w, Lw + lane * TC_MAX_NP);
+          tc_lagrange(tt, gd, p.cheb->x[gd - 1], p.cheb->w[gd - 1], Lw + lane * TC_MAX_NP);
       }
       __syncwarp();
       V acc[TD];
       for (int c = 0; c < TD; ++c) acc[c] = V{};
       for (int kk = lane; kk < npts; kk += 32) {
-        const int i = kk / (np * np), j = (kk / np) % np, l = kk % np;
+        const int i = kk / (g1 * g2), j = (kk / g2) % g1, l = kk % g2;
         if constexpr (DF) {
           const f2 wgt = df_mul(df_mul(Lw[i], Lw[TC_MAX_NP + j]), Lw[2 * TC_MAX_NP + l]);
 #pragma unroll
@@ -810,6 +872,7 @@ struct sctlgpu_treecode_s {
   TcCluster* d_clusters = nullptr;
   TcItem* d_items = nullptr;
   TcTrgBox* d_boxes = nullptr;
+  TcCheb* d_cheb = nullptr;
   sctlgpu_near_plan plan = nullptr;
 };
 
@@ -820,7 +883,7 @@ void tc_free(sctlgpu_treecode_s* T) {
   for (void* q : {(void*)T->d_trg, (void*)T->d_r, (void*)T->d_n, (void*)T->d_v, (void*)T->d_part, (void*)T->d_u,
                   (void*)T->h_in, (void*)T->h_out, (void*)T->d_xs, (void*)T->d_xn, (void*)T->d_xt,
                   (void*)T->d_slot_src, (void*)T->d_tperm, (void*)T->d_bt0, (void*)T->d_btn, (void*)T->d_anc_ptr,
-                  (void*)T->d_anc, (void*)T->d_clusters, (void*)T->d_items, (void*)T->d_boxes})
+                  (void*)T->d_anc, (void*)T->d_clusters, (void*)T->d_items, (void*)T->d_boxes, (void*)T->d_cheb})
     cudaFree(q);
   delete T;
 }
@@ -903,18 +966,14 @@ int sctlgpu_treecode_layout(int kernel, int64_t ns, const double* r_src, int64_t
   if (clusters)
     for (size_t k = 0; k < L.clusters.size(); ++k) {
       const TcNode& C = L.src[L.clusters[k]];
-      clusters[4 * k + 0] = C.sb;
-      clusters[4 * k + 1] = C.se;
-      clusters[4 * k + 2] = C.proxy;
-      clusters[4 * k + 3] = C.proxy + L.proxy_slots;
+      const int64_t row[7] = {C.sb, C.se, C.proxy, C.proxy + tc_proxy_slots(L, C), C.g[0], C.g[1], C.g[2]};
+      std::copy(row, row + 7, clusters + 7 * k);
     }
   if (trg_clusters)
     for (size_t k = 0; k < L.tclusters.size(); ++k) {
       const TcNode& C = L.trg[L.tclusters[k]];
-      trg_clusters[4 * k + 0] = C.b;
-      trg_clusters[4 * k + 1] = C.e;
-      trg_clusters[4 * k + 2] = C.proxy;
-      trg_clusters[4 * k + 3] = C.proxy + L.npts;
+      const int64_t row[7] = {C.b, C.e, C.proxy, C.proxy + C.npts, C.g[0], C.g[1], C.g[2]};
+      std::copy(row, row + 7, trg_clusters + 7 * k);
     }
   return SCTLGPU_OK;
 }
@@ -978,6 +1037,12 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
     if (nd && !pad)
       for (int d = 0; d < 3; ++d) hn[i * 3 + d] = n_src[s * 3 + d];
   }
+  const TcCheb& cb = tc_cheb();
+  // coordinates of grid point k of a cluster's grid
+  auto grid_point = [&](const TcNode& C, int k, double* x) {
+    const int ijk[3] = {k / (C.g[1] * C.g[2]), (k / C.g[2]) % C.g[1], k % C.g[2]};
+    for (int d = 0; d < 3; ++d) x[d] = cheb_coord(C.lo[d], C.hi[d], cb.x[C.g[d] - 1][ijk[d]]);
+  };
   std::vector<TcCluster> hc;
   std::vector<TcItem> hi;
   for (int32_t id : L.clusters) {
@@ -985,17 +1050,17 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
     TcCluster tc{};
     interp_box(C, tc.lo, tc.inv);
     tc.proxy = C.proxy;
+    for (int d = 0; d < 3; ++d) tc.g[d] = C.g[d];
     tc.item0 = (int32_t)hi.size();
     for (int64_t s0 = C.sb; s0 < C.se; s0 += TC_CHUNK)
       hi.push_back({(int32_t)hc.size(), (int32_t)std::min<int64_t>(TC_CHUNK, C.se - s0), s0});
     tc.item1 = (int32_t)hi.size();
-    for (int k = 0; k < L.proxy_slots; ++k) {
-      const int pt = std::min(k / L.per_point, L.npts - 1);  // the padding slot repeats the last point
-      const int i = pt / (L.np * L.np), j = (pt / L.np) % L.np, l = pt % L.np;
+    const int64_t slots = tc_proxy_slots(L, C);
+    for (int k = 0; k < slots; ++k) {
+      const int pt = std::min(k / L.per_point, C.npts - 1);  // the padding slot repeats the last point
       const int64_t slot = C.proxy + k;
-      const double g[3] = {L.xcheb[i], L.xcheb[j], L.xcheb[l]};
-      for (int d = 0; d < 3; ++d) hr[slot * 3 + d] = cheb_coord(C.lo[d], C.hi[d], g[d]);
-      const bool real = k < L.npts * L.per_point;
+      grid_point(C, pt, hr.data() + slot * 3);
+      const bool real = k < C.npts * L.per_point;
       if (kernel == SCTLGPU_LAPLACE3D_DXU && real) hv[slot] = 1.0;  // the moment is the proxy's normal
       if (kernel == SCTLGPU_STOKES3D_DXU && real) hn[slot * 3 + k % 3] = 1.0;  // normal e_c
     }
@@ -1019,11 +1084,8 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
     TcTrgBox tb{};
     interp_box(C, tb.lo, tb.inv);
     tb.proxy = C.proxy;
-    for (int k = 0; k < L.npts; ++k) {
-      const int i = k / (L.np * L.np), j = (k / L.np) % L.np, l = k % L.np;
-      const double g[3] = {L.xcheb[i], L.xcheb[j], L.xcheb[l]};
-      for (int d = 0; d < 3; ++d) htrg[(C.proxy + k) * 3 + d] = cheb_coord(C.lo[d], C.hi[d], g[d]);
-    }
+    for (int d = 0; d < 3; ++d) tb.g[d] = C.g[d];
+    for (int k = 0; k < C.npts; ++k) grid_point(C, k, htrg.data() + (C.proxy + k) * 3);
     hb.push_back(tb);
   }
   // downward-pass work: every batch in pieces of <= batch_max targets (a leaf of coincident
@@ -1055,6 +1117,7 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   up((void**)&T->d_items, hi.data(), hi.size() * sizeof(TcItem));
   up((void**)&T->d_tperm, L.tperm.data(), L.tperm.size() * sizeof(int64_t));
   up((void**)&T->d_boxes, hb.data(), hb.size() * sizeof(TcTrgBox));
+  up((void**)&T->d_cheb, &cb, sizeof(TcCheb));
   up((void**)&T->d_bt0, hbt0.data(), hbt0.size() * sizeof(int64_t));
   up((void**)&T->d_btn, hbtn.data(), hbtn.size() * sizeof(int32_t));
   up((void**)&T->d_anc_ptr, hanc_ptr.data(), hanc_ptr.size() * sizeof(int32_t));
@@ -1135,6 +1198,7 @@ static int tc_execute_device(sctlgpu_treecode T, const double* v_src, double* v_
   p.pn = T->d_n;
   p.pv = T->d_v;
   p.np = L.np;
+  p.cheb = T->d_cheb;
   TcL2PParams q{};
   q.boxes = T->d_boxes;
   q.bt0 = T->d_bt0;
@@ -1147,13 +1211,7 @@ static int tc_execute_device(sctlgpu_treecode T, const double* v_src, double* v_
   q.out = v_out;
   q.accumulate = (flags & SCTLGPU_ACCUMULATE) ? 1 : 0;
   q.np = L.np;
-  for (int m = 0; m < L.np; ++m) {
-    p.x[m] = q.x[m] = L.xcheb[m];
-    p.w[m] = q.w[m] = L.wcheb[m];
-    p.xh[m] = q.xh[m] = (float)L.xcheb[m];
-    p.xl[m] = q.xl[m] = (float)(L.xcheb[m] - (double)p.xh[m]);
-    p.wf[m] = q.wf[m] = (float)L.wcheb[m];  // +-1 or +-1/2: exact
-  }
+  q.cheb = T->d_cheb;
   const int nc = (int)L.clusters.size(), ni = (int)T->n_items;
   switch (T->kernel) {
     case SCTLGPU_LAPLACE3D_FXU: e = tc_launch_moments<SCTLGPU_LAPLACE3D_FXU>(p, ni, T->pass_items, nc, T->df, st); break;

@@ -104,8 +104,9 @@ def layout(kernel, r_src, r_trg, digits: int = 10, order=0, theta=0.0, leaf_max=
     """The host-only part of Treecode (no device): sizes, blocks (rows of src_begin, src_count,
     trg_begin, trg_count; sources index the source slots, targets the target list of sorted
     targets then target proxies), the source of every slot (-1 padding, -2 proxy), the target
-    order, per source cluster with proxies (slot begin, end, proxy begin, end) and per target
-    cluster with proxies (target begin, end, proxy begin, end)."""
+    order, per source cluster with proxies (slot begin, end, proxy begin, end, grid points along
+    x, y, z) and per target cluster with proxies (target begin, end, proxy begin, end, grid
+    points along x, y, z)."""
     k = capi.KERNEL_IDS[kernel] if isinstance(kernel, str) else int(kernel)
     xs, xt = _host(r_src), _host(r_trg)
     ns, nt = xs.size // 3, xt.size // 3
@@ -120,8 +121,8 @@ def layout(kernel, r_src, r_trg, digits: int = 10, order=0, theta=0.0, leaf_max=
     blocks = np.zeros((s["blocks"], 4), np.int64)
     slot_src = np.zeros(s["slots"], np.int64)
     trg_order = np.zeros(nt, np.int64)
-    clusters = np.zeros((s["clusters"], 4), np.int64)
-    tclusters = np.zeros((s["target_clusters"], 4), np.int64)
+    clusters = np.zeros((s["clusters"], 7), np.int64)
+    tclusters = np.zeros((s["target_clusters"], 7), np.int64)
     p = lambda a: a.ctypes.data if a.size else None  # noqa: E731
     capi.check(lib.sctlgpu_treecode_layout(*args, sizes, ctypes.byref(th), p(blocks), p(slot_src), p(trg_order),
                                            p(clusters), p(tclusters)), "sctlgpu_treecode_layout")

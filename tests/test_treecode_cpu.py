@@ -8,6 +8,8 @@ interaction blocks.  Properties checked on clustered and surface point sets:
   clusters' proxies;
 * approximated pairs of clusters satisfy the acceptance test, and clusters with proxies hold
   more points than proxies;
+* a cluster's grid has order + 1 points along its longest side, no more along any other, and
+  one point along a side of zero extent (a flat sheet);
 * every block starts and ends on a pair boundary (one pairing of the slot list serves all
   blocks), padding slots are the only sources missing from the slot list.
 """
@@ -48,7 +50,6 @@ def test_layout_covers_every_pair_once(kind, kernel, dual):
     order, theta = 3, 0.6
     s, blocks, slot_src, trg_order, clusters, tclusters = TC.layout(kernel, xs, xt, order=order, theta=theta,
                                                                     leaf_max=96, batch_max=64, dual=dual)
-    npts = (order + 1) ** 3
     per_point = 3 if kernel == 3 else 1
     assert s["order"] == order and s["theta"] == theta
     assert s["clusters"] > 0 and s["proxy_interactions"] > 0, "the test geometry must exercise the proxies"
@@ -59,10 +60,21 @@ def test_layout_covers_every_pair_once(kind, kernel, dual):
     assert np.array_equal(np.sort(real[real >= 0]), np.arange(ns))
     assert np.all(slot_src[nsrc:] == -2)
     assert np.array_equal(np.sort(trg_order), np.arange(nt))
-    assert s["target_list"] == nt + npts * s["target_clusters"]
+    sgrid, tgrid = clusters[:, 4:7].prod(1), tclusters[:, 4:7].prod(1)
+    assert s["target_list"] == nt + tgrid.sum()
     assert np.all(blocks[:, 0] % 2 == 0) and np.all(blocks[:, 1] % 2 == 0)
-    assert np.all(clusters[:, 3] - clusters[:, 2] == (npts * per_point + 1) // 2 * 2)
-    assert np.all(tclusters[:, 3] - tclusters[:, 2] == npts) and np.all(tclusters[:, 1] - tclusters[:, 0] > npts)
+    assert np.all(clusters[:, 3] - clusters[:, 2] == (sgrid * per_point + 1) // 2 * 2)
+    assert np.all(tclusters[:, 3] - tclusters[:, 2] == tgrid) and np.all(tclusters[:, 1] - tclusters[:, 0] > tgrid)
+    for c in (clusters, tclusters):
+        assert np.all(c[:, 4:7] >= 1) and np.all(c[:, 4:7] <= order + 1)
+    for c in clusters:  # the longest side has the full order; a flat side one point
+        src = slot_src[c[0]:c[1]]
+        p = xs[src[src >= 0]]
+        ext = p.max(0) - p.min(0)
+        assert c[4 + int(np.argmax(ext))] == order + 1
+        assert np.all(c[4:7][ext == 0] == 1)
+        if kind == "sheet":
+            assert c[6] == 1
     sprox = {int(c[2]): c for c in clusters}
     tprox = {int(c[2]): c for c in tclusters}
     cnt = np.zeros((nt, ns), np.uint8)  # (sorted target, source) coverage
@@ -74,7 +86,7 @@ def test_layout_covers_every_pair_once(kind, kernel, dual):
             ta, tb_ = t0, t0 + tn
         else:
             c = tprox[t0]
-            assert tn == npts
+            assert tn == c[4:7].prod()
             ta, tb_ = int(c[0]), int(c[1])
         tset = np.arange(ta, tb_)
         if s0 < nsrc:
@@ -87,7 +99,7 @@ def test_layout_covers_every_pair_once(kind, kernel, dual):
                 c = sprox[pos]
                 src = slot_src[c[0]:c[1]]
                 groups.append(src[src >= 0])
-                assert groups[-1].size > npts * per_point
+                assert groups[-1].size > c[4:7].prod() * per_point
                 pos = int(c[3])
             assert pos == s0 + sn
         for g in groups:
