@@ -31,12 +31,17 @@
 namespace sctlgpu {
 
 enum { KER_LFXU = 0, KER_LDXU = 1, KER_SFXU = 2, KER_SDXU = 3 };
+// Internal: the Stokes double layer of a symmetric 3 x 3 density S per source (the treecode's
+// proxies carry the symmetric part of the moment sum_s L_k(y_s) n_s (x) f_s), u = 3/(4 pi) r
+// (r . S r) / r^5 -- records hold diag(S) as the "normal" and (2 S01, 2 S02, 2 S12) as the
+// "density".  Only the packed double-float near-batch kernel implements it.
+enum { KER_SDXU_SYM = 4 };
 enum { MODE_F64 = 0, MODE_F32 = 1, MODE_MXLO = 2, MODE_MXDF = 3 };
 
 template <int KER>
 constexpr double scale_of() {  // uKerScaleFactor, kernel_functions.hpp:40,69,133,188
   constexpr double pi = 3.14159265358979323846264338327950288;
-  return KER == 2 ? 1.0 / (8.0 * pi) : KER == 3 ? 3.0 / (4.0 * pi) : 1.0 / (4.0 * pi);
+  return KER == 2 ? 1.0 / (8.0 * pi) : (KER == 3 || KER == 4) ? 3.0 / (4.0 * pi) : 1.0 / (4.0 * pi);
 }
 
 template <int KER>
@@ -45,6 +50,7 @@ template <> struct KDims<KER_LFXU> { static constexpr int ND = 0, K0 = 1, K1 = 1
 template <> struct KDims<KER_LDXU> { static constexpr int ND = 3, K0 = 1, K1 = 1; };
 template <> struct KDims<KER_SFXU> { static constexpr int ND = 0, K0 = 3, K1 = 3; };
 template <> struct KDims<KER_SDXU> { static constexpr int ND = 3, K0 = 3, K1 = 3; };
+template <> struct KDims<KER_SDXU_SYM> { static constexpr int ND = 3, K0 = 3, K1 = 3; };
 
 // Grid shared by all points of one mixed-precision call: x = o + xh + xl with
 // xh a float on the grid g = L*2^-23 (|x-o| <= L, L a power of two), so the

@@ -114,6 +114,7 @@ template <> struct RecPk<KER_SFXU> { v2 xh, yh, zh, xl, yl, zl, fh0, fh1, fh2, f
 template <> struct RecPk<KER_SDXU> {
   v2 xh, yh, zh, xl, yl, zl, fh0, fh1, fh2, fl0, fl1, fl2, nh0, nh1, nh2, nl0, nl1, nl2;
 };
+template <> struct RecPk<KER_SDXU_SYM> : RecPk<KER_SDXU> {};  // n: diag(S), f: 2 S01, 2 S02, 2 S12
 
 // The pair record of sources sa (lane x) and sa + 1 (lane y); without a real
 // second source (real_b false) lane y is a copy of sa with zero densities (it
@@ -139,7 +140,7 @@ __device__ __forceinline__ RecPk<KER> pair_record(const MixedFrame& fr, int64_t 
     } else {
 #pragma unroll
       for (int k = 0; k < 3; ++k) split_val(f[s * 3 + k] * ws, v[lane][6 + k], v[lane][9 + k]);
-      if constexpr (KER == KER_SDXU) {
+      if constexpr (KER == KER_SDXU || KER == KER_SDXU_SYM) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) split_val(nrm[s * 3 + k], v[lane][12 + k], v[lane][15 + k]);
       }
@@ -257,11 +258,34 @@ struct PairPk {
         dv2 y5 = vtwo_prod(q2.h, y0);
         y5.l = vfma(q2.l, y0, y5.l);
         y5.l = vfma(y5.h, vmul(vdup(2.5f), rho), y5.l);
-        const v2 nh[3] = {s.nh0, s.nh1, s.nh2}, nl[3] = {s.nl0, s.nl1, s.nl2};
-        const v2 fh[3] = {s.fh0, s.fh1, s.fh2}, fl[3] = {s.fl0, s.fl1, s.fl2};
-        const dv2 dn = vdot3(nh, nl, D, d);
-        const dv2 fd = vdot3(fh, fl, D, d);
-        const dv2 c = vdf_mul(vdf_mul(fd, dn), y5);
+        dv2 c;
+        if constexpr (KER == KER_SDXU) {
+          const v2 nh[3] = {s.nh0, s.nh1, s.nh2}, nl[3] = {s.nl0, s.nl1, s.nl2};
+          const v2 fh[3] = {s.fh0, s.fh1, s.fh2}, fl[3] = {s.fl0, s.fl1, s.fl2};
+          const dv2 dn = vdot3(nh, nl, D, d);
+          const dv2 fd = vdot3(fh, fl, D, d);
+          c = vdf_mul(vdf_mul(fd, dn), y5);
+        } else {
+          // r . S r = sum_i S_ii r_i^2 + sum_{i<j} 2 S_ij r_i r_j: the six products r_i r_j in
+          // double-float (hi products exact, first-order lo terms), weighted and summed by TwoSum
+          const dv2 C01 = vtwo_prod(D[0], D[1]), C02 = vtwo_prod(D[0], D[2]), C12 = vtwo_prod(D[1], D[2]);
+          const dv2 m[6] = {{P0.h, vfma(vadd(D[0], D[0]), d[0], P0.l)},
+                            {P1.h, vfma(vadd(D[1], D[1]), d[1], P1.l)},
+                            {P2.h, vfma(vadd(D[2], D[2]), d[2], P2.l)},
+                            {C01.h, vfma(D[0], d[1], vfma(d[0], D[1], C01.l))},
+                            {C02.h, vfma(D[0], d[2], vfma(d[0], D[2], C02.l))},
+                            {C12.h, vfma(D[1], d[2], vfma(d[1], D[2], C12.l))}};
+          const dv2 w[6] = {{s.nh0, s.nl0}, {s.nh1, s.nl1}, {s.nh2, s.nl2},
+                            {s.fh0, s.fl0}, {s.fh1, s.fl1}, {s.fh2, s.fl2}};
+          dv2 q = vdf_mul(w[0], m[0]);
+#pragma unroll
+          for (int k = 1; k < 6; ++k) {
+            const dv2 tk = vdf_mul(w[k], m[k]);
+            const dv2 sk = vtwo_sum(q.h, tk.h);
+            q = {sk.h, vadd(vadd(q.l, tk.l), sk.l)};
+          }
+          c = vdf_mul(q, y5);
+        }
 #pragma unroll
         for (int i = 0; i < 3; ++i) vdf_acc(t.acc[i], vdf_mul(dv2{D[i], d[i]}, c));
       }

@@ -97,6 +97,7 @@ inline NearOps near_ops_pk(int kernel) {
     case KER_LFXU: return make_near_ops_pk<KER_LFXU>();
     case KER_LDXU: return make_near_ops_pk<KER_LDXU>();
     case KER_SFXU: return make_near_ops_pk<KER_SFXU>();
+    case KER_SDXU_SYM: return make_near_ops_pk<KER_SDXU_SYM>();
     default: return make_near_ops_pk<KER_SDXU>();
   }
 }

@@ -295,45 +295,11 @@ void free_plan(sctlgpu_near_plan_s* P) {
   delete P;
 }
 
-}  // namespace
-
-extern "C" {
-
-int sctlgpu_near_autotune(int kernel, int mode, int digits, int* splits) {
-  int nd, sd, td;
-  if (kernel < 0 || kernel > SCTLGPU_STOKES3D_DXU) return SCTLGPU_ERR_INVALID_KERNEL;  // the four hot-path kernels
-  if (sctlgpu_kernel_dims(kernel, nullptr, &nd, &sd, &td) != SCTLGPU_OK) return SCTLGPU_ERR_INVALID_KERNEL;
-  if (mode != SCTLGPU_F64 && mode != SCTLGPU_F32 && mode != SCTLGPU_MIXED) return SCTLGPU_ERR_INVALID_MODE;
-  int dev;
-  unsigned* status;
-  int sms;
-  int rc = runtime_device(&dev, &status, &sms);
-  if (rc) return rc;
-  int newton;
-  const int imode = imode_for(mode, runtime_effective_digits(mode, digits), &newton);
-  const NearOps ops = ops_for(kernel, imode, newton);
-  std::array<int, SCTLGPU_NEAR_CLASSES> table;
-  rc = autotune(kernel, imode, newton, ops, sms, mode, table);
-  if (rc) return rc;
-  if (splits)
-    for (int i = 0; i < SCTLGPU_NEAR_CLASSES; ++i) splits[i] = table[i];
-  return SCTLGPU_OK;
-}
-
-int sctlgpu_near_plan_create(sctlgpu_near_plan* out, int kernel, int mode, int digits, int64_t nblk,
-                             const sctlgpu_block* blocks, int64_t ns, int64_t nt, const int64_t* trg_map,
-                             int64_t n_out) {
-  return sctlgpu_near_plan_create_indexed(out, kernel, mode, digits, nblk, blocks, ns, nt, nullptr, 0, trg_map, n_out);
-}
-
-int sctlgpu_near_plan_create_indexed(sctlgpu_near_plan* out, int kernel, int mode, int digits, int64_t nblk,
-                                     const sctlgpu_block* blocks, int64_t ns, int64_t nt, const int64_t* trg_index,
-                                     int64_t n_index, const int64_t* trg_map, int64_t n_out) {
-  if (!out) return SCTLGPU_ERR_NULL_POINTER;
-  *out = nullptr;
-  int nd, sd, td;
-  if (kernel < 0 || kernel > SCTLGPU_STOKES3D_DXU) return SCTLGPU_ERR_INVALID_KERNEL;  // the four hot-path kernels
-  if (sctlgpu_kernel_dims(kernel, nullptr, &nd, &sd, &td) != SCTLGPU_OK) return SCTLGPU_ERR_INVALID_KERNEL;
+// `kernel`: the public id (split-table tuning); `ker`: the kernel evaluated (== kernel, or an
+// internal variant); nd, td: normal and target dimensions.
+int plan_create(sctlgpu_near_plan* out, int kernel, int ker, int nd, int td, int mode, int digits, int64_t nblk,
+                const sctlgpu_block* blocks, int64_t ns, int64_t nt, const int64_t* trg_index, int64_t n_index,
+                const int64_t* trg_map, int64_t n_out) {
   if (mode != SCTLGPU_F64 && mode != SCTLGPU_F32 && mode != SCTLGPU_MIXED) return SCTLGPU_ERR_INVALID_MODE;
   if (nblk < 0 || ns < 0 || nt < 0 || nblk > INT32_MAX) return SCTLGPU_ERR_INVALID_SIZE;
   if (nblk > 0 && !blocks) return SCTLGPU_ERR_NULL_POINTER;
@@ -369,10 +335,9 @@ int sctlgpu_near_plan_create_indexed(sctlgpu_near_plan* out, int kernel, int mod
   P->mode = mode;
   P->digits = digits;
   P->imode = imode_for(mode, runtime_effective_digits(mode, digits), &P->newton);
-  P->ops = ops_for(kernel, P->imode, P->newton);
+  P->ops = ops_for(ker, P->imode, P->newton);
   P->K1 = td;
   P->ND = nd;
-  P->SD = sd;
   P->nblk = nblk;
   P->ns = ns;
   P->nt = nt;
@@ -383,7 +348,8 @@ int sctlgpu_near_plan_create_indexed(sctlgpu_near_plan* out, int kernel, int mod
   P->pairs = pairs;
 
   std::array<int, SCTLGPU_NEAR_CLASSES> table;
-  rc = autotune(kernel, P->imode, P->newton, P->ops, sms, mode, table);
+  rc = autotune(kernel, P->imode, P->newton, ker == kernel ? P->ops : ops_for(kernel, P->imode, P->newton), sms, mode,
+                table);
   if (rc) {
     delete P;
     return rc;
@@ -448,6 +414,69 @@ int sctlgpu_near_plan_create_indexed(sctlgpu_near_plan* out, int kernel, int mod
   *out = P;
   return SCTLGPU_OK;
 }
+
+}  // namespace
+
+extern "C" {
+
+int sctlgpu_near_autotune(int kernel, int mode, int digits, int* splits) {
+  int nd, sd, td;
+  if (kernel < 0 || kernel > SCTLGPU_STOKES3D_DXU) return SCTLGPU_ERR_INVALID_KERNEL;  // the four hot-path kernels
+  if (sctlgpu_kernel_dims(kernel, nullptr, &nd, &sd, &td) != SCTLGPU_OK) return SCTLGPU_ERR_INVALID_KERNEL;
+  if (mode != SCTLGPU_F64 && mode != SCTLGPU_F32 && mode != SCTLGPU_MIXED) return SCTLGPU_ERR_INVALID_MODE;
+  int dev;
+  unsigned* status;
+  int sms;
+  int rc = runtime_device(&dev, &status, &sms);
+  if (rc) return rc;
+  int newton;
+  const int imode = imode_for(mode, runtime_effective_digits(mode, digits), &newton);
+  const NearOps ops = ops_for(kernel, imode, newton);
+  std::array<int, SCTLGPU_NEAR_CLASSES> table;
+  rc = autotune(kernel, imode, newton, ops, sms, mode, table);
+  if (rc) return rc;
+  if (splits)
+    for (int i = 0; i < SCTLGPU_NEAR_CLASSES; ++i) splits[i] = table[i];
+  return SCTLGPU_OK;
+}
+
+int sctlgpu_near_plan_create(sctlgpu_near_plan* out, int kernel, int mode, int digits, int64_t nblk,
+                             const sctlgpu_block* blocks, int64_t ns, int64_t nt, const int64_t* trg_map,
+                             int64_t n_out) {
+  return sctlgpu_near_plan_create_indexed(out, kernel, mode, digits, nblk, blocks, ns, nt, nullptr, 0, trg_map, n_out);
+}
+
+int sctlgpu_near_plan_create_indexed(sctlgpu_near_plan* out, int kernel, int mode, int digits, int64_t nblk,
+                                     const sctlgpu_block* blocks, int64_t ns, int64_t nt, const int64_t* trg_index,
+                                     int64_t n_index, const int64_t* trg_map, int64_t n_out) {
+  if (!out) return SCTLGPU_ERR_NULL_POINTER;
+  *out = nullptr;
+  int nd, sd, td;
+  if (kernel < 0 || kernel > SCTLGPU_STOKES3D_DXU) return SCTLGPU_ERR_INVALID_KERNEL;  // the four hot-path kernels
+  if (sctlgpu_kernel_dims(kernel, nullptr, &nd, &sd, &td) != SCTLGPU_OK) return SCTLGPU_ERR_INVALID_KERNEL;
+  return plan_create(out, kernel, kernel, nd, td, mode, digits, nblk, blocks, ns, nt, trg_index, n_index, trg_map,
+                     n_out);
+}
+
+}  // extern "C"
+
+namespace sctlgpu {
+
+int near_plan_create_sym(::sctlgpu_near_plan_s** out, int mode, int digits, int64_t nblk, const void* blocks,
+                         int64_t ns, int64_t nt, const int64_t* trg_map, int64_t n_out) {
+  if (!out) return SCTLGPU_ERR_NULL_POINTER;
+  *out = nullptr;
+  int newton;
+  if (mode != SCTLGPU_MIXED || imode_for(mode, runtime_effective_digits(mode, digits), &newton) != NEAR_MXDF)
+    return SCTLGPU_ERR_INVALID_MODE;
+  // split table tuned for the Stokes double layer (the same targets per thread and a similar cost)
+  return plan_create(out, SCTLGPU_STOKES3D_DXU, KER_SDXU_SYM, 3, 3, mode, digits, nblk,
+                     static_cast<const sctlgpu_block*>(blocks), ns, nt, nullptr, 0, trg_map, n_out);
+}
+
+}  // namespace sctlgpu
+
+extern "C" {
 
 int sctlgpu_near_plan_execute(sctlgpu_near_plan P, const void* r_trg, const void* r_src, const void* n_src,
                               const void* v_src, const void* w_src, void* v_out, unsigned flags, void* stream) {

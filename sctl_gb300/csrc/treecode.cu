@@ -24,7 +24,9 @@
 //    source charges q_s: the density (single layers), the density times the
 //    normal (Laplace double layer: the moment is the proxy's normal), or
 //    normal (x) density (Stokes double layer: three proxies per point with
-//    unit normals e_c and densities M_k[c][:]).
+//    unit normals e_c and densities M_k[c][:]; with double-float plans one proxy
+//    per point whose symmetric density sym(M_k) gives the same field, since
+//    (r.n)(r.f) = r . (n (x) f) r, evaluated by KER_SDXU_SYM in a second plan).
 //  * device, per evaluation: densities gathered into slot order, moments per
 //    (cluster, 256-slot chunk) -- in double-float on the FP32 pipe when the
 //    plan's arithmetic is FP32 or double-float, else in FP64 -- reduced per
@@ -55,6 +57,10 @@ constexpr int TC_CHUNK = 256;   // source slots per moment work item
 constexpr int TC_THREADS = 256;
 constexpr int TC_MAX_BATCH = 2048;
 constexpr double TC_DIRECT_FRACTION = 0.75;  // treecode interactions above this share of Ns * Nt: direct sum
+// Cost of one symmetric-density proxy of the Stokes double layer (KER_SDXU_SYM: r . S r, six
+// double-float products) in Stokes double-layer interactions (two compensated dot products);
+// measured on GB300: 179 against 227 G interactions/s.
+constexpr double TC_SYM_COST = 1.25;
 constexpr double TC_PART_BYTES = 1e9;  // partial moments held at once (2^20 sources, degree 11: 0.7-2 GB in all)  // targets per batch (the downward pass keeps a batch's sums in shared memory)
 
 struct TcNode {
@@ -145,7 +151,10 @@ bool split_node(const double* X, std::vector<int64_t>& perm, std::vector<int64_t
 // Octree on tight boxes: nodes with more than `leaf_max` points are split (split_node).  The
 // first levels are split in order until there are subtrees for every host thread; those are
 // built concurrently (disjoint ranges of `perm`) and appended in order, so the node numbering
-// keeps children consecutive and after their parent.
+// keeps children consecutive and after their parent.  (Binary trees split at the median along
+// the longest side -- leaves of exactly leaf_max points -- were measured: 5-15 % faster at
+// digits 10, but their elongated boxes let the acceptance test admit targets closer to the
+// long side, and 3000 coincident targets met 3e-10 against 1e-10.)
 void build_octree(const double* X, int64_t n, int64_t leaf_max, std::vector<int64_t>& perm,
                   std::vector<TcNode>& nodes) {
   perm.resize((size_t)n);
@@ -261,6 +270,10 @@ void tc_grid(TcNode& C, int order, double theta) {
 
 struct TcLayout {
   int order = 0, np = 0, npts = 0, per_point = 1;  // np, npts: the largest grid (order + 1 per dimension)
+  // Stokes double layer with double-float plans: one proxy per grid point carrying the
+  // symmetric part of its moment (evaluated by KER_SDXU_SYM, cost pw each) instead of three
+  bool sym = false;
+  double pw = 1.0;
   double theta = 0;
   std::vector<TcNode> src, trg;
   std::vector<int64_t> sperm, tperm;
@@ -316,7 +329,8 @@ void tc_defaults(int digits, int* order, double* theta) {
 }
 
 int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, const double* r_trg, int order,
-                    double theta, double theta_trg, int64_t leaf_max, int64_t batch_max, bool dual, TcLayout& L) {
+                    double theta, double theta_trg, int64_t leaf_max, int64_t batch_max, bool dual, bool sym,
+                    TcLayout& L) {
   if (order < 1 || order >= TC_MAX_NP || !(theta > 0) || theta >= 1.0) return SCTLGPU_ERR_INVALID_ARGUMENT;
   if (batch_max > TC_MAX_BATCH || theta_trg > theta) return SCTLGPU_ERR_INVALID_ARGUMENT;
   L.dual = dual;
@@ -324,9 +338,11 @@ int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, con
   L.order = order;
   L.np = order + 1;
   L.npts = L.np * L.np * L.np;
-  L.per_point = kernel == SCTLGPU_STOKES3D_DXU ? 3 : 1;
+  L.sym = sym && kernel == SCTLGPU_STOKES3D_DXU;
+  L.per_point = kernel == SCTLGPU_STOKES3D_DXU && !L.sym ? 3 : 1;
+  L.pw = L.sym ? TC_SYM_COST : 1.0;
   L.theta = theta;
-  if (leaf_max <= 0) leaf_max = std::max<int64_t>(64, (int64_t)L.npts * L.per_point);
+  if (leaf_max <= 0) leaf_max = std::max<int64_t>(64, (int64_t)std::ceil(L.npts * L.per_point * L.pw));
   if (batch_max <= 0) batch_max = 512;
   {  // the two trees are independent
     std::thread tt([&] { build_octree(r_trg, nt, batch_max, L.tperm, L.trg); });
@@ -390,14 +406,15 @@ int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, con
     const double dist = std::sqrt(dx * dx + dy * dy + dz * dz);
     const int64_t nT = T.e - T.b, nS = S.e - S.b, sS = S.se - S.sb;
     const int64_t Ps = (int64_t)S.npts * L.per_point, Pt = T.npts;  // the clusters' proxies
+    const double Pc = (double)Ps * L.pw;                              // the source proxies' cost
     if (T.r + S.r < theta * dist) {
       // target-side interpolation (a target cluster's proxies) only under the stricter theta_trg
-      const bool src_ok = nS > Ps, trg_ok = L.dual && nT > Pt && T.r + S.r < L.theta_trg * dist;
+      const bool src_ok = (double)nS > Pc, trg_ok = L.dual && nT > Pt && T.r + S.r < L.theta_trg * dist;
       double best = (double)nT * sS;
       char kind = 0;
-      if (src_ok && (double)nT * Ps < best) best = (double)nT * Ps, kind = 1;
+      if (src_ok && (double)nT * Pc < best) best = (double)nT * Pc, kind = 1;
       if (trg_ok && (double)Pt * sS < best) best = (double)Pt * sS, kind = 2;
-      if (src_ok && trg_ok && (double)Pt * Ps < best) best = (double)Pt * Ps, kind = 3;
+      if (src_ok && trg_ok && (double)Pt * Pc < best) best = (double)Pt * Pc, kind = 3;
       recs.push_back({ti, si, kind});
       if (kind & 1) sused[si] = 1;
       if (kind & 2) tused[ti] = 1;
@@ -500,6 +517,7 @@ struct TcMomParams {
   double* pv;       // proxy densities
   int np;           // the largest grid's points per dimension (shared-memory stride)
   const TcCheb* cheb;
+  int sym;          // Stokes double layer: one symmetric-density proxy per point (else three)
 };
 
 template <int KER>
@@ -712,6 +730,12 @@ __global__ void tc_reduce_kernel(TcMomParams p, int n_clusters) {
       for (int q = 0; q < 3; ++q) put(&p.pn[(C.proxy + k) * 3 + q], m[q]);
     } else if constexpr (KER == SCTLGPU_STOKES3D_FXU) {
       for (int q = 0; q < 3; ++q) put(&p.pv[(C.proxy + k) * 3 + q], m[q]);
+    } else if (p.sym) {  // proxy k: diag(M_k) as the normal, its symmetrised off-diagonal pairs
+      const int64_t o = (C.proxy + k) * 3;
+      for (int c = 0; c < 3; ++c) put(&p.pn[o + c], m[c * 4]);
+      put(&p.pv[o + 0], m[1] + m[3]);
+      put(&p.pv[o + 1], m[2] + m[6]);
+      put(&p.pv[o + 2], m[5] + m[7]);
     } else {  // proxy (k, c): normal e_c, density M_k[c][:]
       for (int q = 0; q < Q; ++q) put(&p.pv[(C.proxy + 3 * k + q / 3) * 3 + q % 3], m[q]);
     }
@@ -781,41 +805,58 @@ __global__ void __launch_bounds__(TC_THREADS) tc_l2p_kernel(TcL2PParams p) {
   const int tn = p.btn[b];
   for (int e = threadIdx.x; e < tn * TD; e += blockDim.x) acc_t[e] = p.u[t0 * TD + e];
   for (int a = p.anc_ptr[b]; a < p.anc_ptr[b + 1]; ++a) {
-    const TcTrgBox A = p.boxes[p.anc[a]];
-    const int g1 = A.g[1], g2 = A.g[2], npts = A.g[0] * g1 * g2;
+    const TcTrgBox* A = p.boxes + p.anc[a];  // read in place (indexed by lane below)
+    const int g0 = A->g[0], g1 = A->g[1], g2 = A->g[2], g01 = g0 * g1, npts = g01 * g2;
+    const int64_t aproxy = A->proxy;
     __syncthreads();
-    for (int e = threadIdx.x; e < npts * TD; e += blockDim.x) {
-      const double v = p.u[A.proxy * TD + e];
+    for (int e = threadIdx.x; e < npts * TD; e += blockDim.x) {  // stored [l][i, j][c]
+      const double v = p.u[aproxy * TD + e];
+      const int kk = e / TD, c = e - kk * TD, ij = kk / g2, l = kk - ij * g2;
+      V* dst = P + ((size_t)l * g01 + ij) * TD + c;
       if constexpr (DF)
-        P[e] = tc_split(v);
+        *dst = tc_split(v);
       else
-        P[e] = v;
+        *dst = v;
     }
     __syncthreads();
     for (int t = warp; t < tn; t += nwarps) {  // one warp per target
       const int64_t k = t0 + t;
       if (lane < 3) {
-        double tt = (p.r[k * 3 + lane] - A.lo[lane]) * A.inv[lane] - 1.0;
+        double tt = (p.r[k * 3 + lane] - A->lo[lane]) * A->inv[lane] - 1.0;
         tt = fmin(1.0, fmax(-1.0, tt));
-        const int gd = A.g[lane];
+        const int gd = A->g[lane];
         if constexpr (DF)
           tc_lagrange_df(tt, gd, p.cheb, Lw + lane * TC_MAX_NP);
         else
           tc_lagrange(tt, gd, p.cheb->x[gd - 1], p.cheb->w[gd - 1], Lw + lane * TC_MAX_NP);
       }
       __syncwarp();
+      // sum_i L_i(x) sum_j L_j(y) sum_l L_l(z) P[i][j][l]: the lanes split the (i, j) rows
       V acc[TD];
       for (int c = 0; c < TD; ++c) acc[c] = V{};
-      for (int kk = lane; kk < npts; kk += 32) {
-        const int i = kk / (g1 * g2), j = (kk / g2) % g1, l = kk % g2;
+      for (int ij = lane; ij < g01; ij += 32) {
+        const int i = ij / g1, j = ij - i * g1;
+        V part[TD];
+        for (int c = 0; c < TD; ++c) part[c] = V{};
+        for (int l = 0; l < g2; ++l) {
+          const V z = Lw[2 * TC_MAX_NP + l];
+          const V* pl = P + ((size_t)l * g01 + ij) * TD;
+#pragma unroll
+          for (int c = 0; c < TD; ++c) {
+            if constexpr (DF)
+              df_acc(part[c], df_mul(z, pl[c]));
+            else
+              part[c] = fma(z, pl[c], part[c]);
+          }
+        }
         if constexpr (DF) {
-          const f2 wgt = df_mul(df_mul(Lw[i], Lw[TC_MAX_NP + j]), Lw[2 * TC_MAX_NP + l]);
+          const f2 xy = df_mul(Lw[i], Lw[TC_MAX_NP + j]);
 #pragma unroll
-          for (int c = 0; c < TD; ++c) df_acc(acc[c], df_mul(wgt, P[kk * TD + c]));
+          for (int c = 0; c < TD; ++c) df_acc(acc[c], df_mul(xy, two_sum(part[c].h, part[c].l)));
         } else {
-          const double wgt = Lw[i] * Lw[TC_MAX_NP + j] * Lw[2 * TC_MAX_NP + l];
+          const double xy = Lw[i] * Lw[TC_MAX_NP + j];
 #pragma unroll
-          for (int c = 0; c < TD; ++c) acc[c] = fma(wgt, P[kk * TD + c], acc[c]);
+          for (int c = 0; c < TD; ++c) acc[c] = fma(xy, part[c], acc[c]);
         }
       }
 #pragma unroll
@@ -874,12 +915,14 @@ struct sctlgpu_treecode_s {
   TcTrgBox* d_boxes = nullptr;
   TcCheb* d_cheb = nullptr;
   sctlgpu_near_plan plan = nullptr;
+  sctlgpu_near_plan plan_sym = nullptr;  // the symmetric-density proxies' blocks (Stokes double layer)
 };
 
 namespace {
 
 void tc_free(sctlgpu_treecode_s* T) {
   if (T->plan) sctlgpu_near_plan_destroy(T->plan);
+  if (T->plan_sym) sctlgpu_near_plan_destroy(T->plan_sym);
   for (void* q : {(void*)T->d_trg, (void*)T->d_r, (void*)T->d_n, (void*)T->d_v, (void*)T->d_part, (void*)T->d_u,
                   (void*)T->h_in, (void*)T->h_out, (void*)T->d_xs, (void*)T->d_xn, (void*)T->d_xt,
                   (void*)T->d_slot_src, (void*)T->d_tperm, (void*)T->d_bt0, (void*)T->d_btn, (void*)T->d_anc_ptr,
@@ -899,7 +942,7 @@ int tc_check_common(int kernel, int64_t ns, const double* r_src, int64_t nt, con
   return SCTLGPU_OK;
 }
 
-int tc_layout_from(int kernel, int digits, int64_t ns, const double* r_src, int64_t nt, const double* r_trg,
+int tc_layout_from(int kernel, int mode, int digits, int64_t ns, const double* r_src, int64_t nt, const double* r_trg,
                    const sctlgpu_treecode_params* prm, TcLayout& L, int* batch_max) {
   int order = prm ? prm->order : 0;
   double theta = prm ? prm->theta : 0.0;
@@ -907,21 +950,31 @@ int tc_layout_from(int kernel, int digits, int64_t ns, const double* r_src, int6
   const double theta_trg = prm ? prm->theta_trg : 0.0;
   const int64_t leaf = prm ? prm->leaf_max : 0;
   const bool dual = !prm || prm->dual != 0;
+  // symmetric-density proxies where the plans run double-float (KER_SDXU_SYM has no other form)
+  const bool sym = mode == SCTLGPU_MIXED &&
+                   runtime_mixed_arith(runtime_effective_digits(mode, digits)) == MIXED_ARITH_DF;
   if (prm && prm->batch_max > 0) {
     if (batch_max) *batch_max = prm->batch_max;
-    return tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, theta_trg, leaf, prm->batch_max, dual, L);
+    return tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, theta_trg, leaf, prm->batch_max, dual, sym,
+                           L);
   }
-  // Batches of 512 and of 256 targets: the one with fewer interactions, the larger on a near tie
-  // (fewer blocks).  Targets filling a volume favour 256 (sphere/ball: 0.147 vs 0.166 of Ns * Nt
-  // at digits 10, 7-17 % faster), targets hugging a surface tie (torus).
-  int rc = tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, theta_trg, leaf, 512, dual, L);
+  // Batches of 512 and of 256 targets (built concurrently): the one with fewer interactions, the
+  // larger on a near tie (fewer blocks).  Targets filling a volume favour 256 (sphere/ball: 0.147
+  // vs 0.166 of Ns * Nt at digits 10, 7-17 % faster), targets hugging a surface tie (torus).
+  TcLayout S;
+  int rc_s = SCTLGPU_OK;
+  std::thread small;
+  if (nt > 512)
+    small = std::thread([&] {
+      rc_s = tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, theta_trg, leaf, 256, dual, sym, S);
+    });
+  int rc = tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, theta_trg, leaf, 512, dual, sym, L);
+  if (small.joinable()) small.join();
   if (rc) return rc;
   if (batch_max) *batch_max = 512;
   if (nt > 512) {
-    TcLayout S;
-    rc = tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, theta_trg, leaf, 256, dual, S);
-    if (rc) return rc;
-    if ((double)(S.pp + S.approx) < 0.97 * (double)(L.pp + L.approx)) {
+    if (rc_s) return rc_s;
+    if ((double)S.pp + S.pw * (double)S.approx < 0.97 * ((double)L.pp + L.pw * (double)L.approx)) {
       L = std::move(S);
       if (batch_max) *batch_max = 256;
     }
@@ -954,7 +1007,7 @@ int sctlgpu_treecode_layout(int kernel, int64_t ns, const double* r_src, int64_t
   if (rc) return rc;
   if (!sizes) return SCTLGPU_ERR_NULL_POINTER;
   TcLayout L;
-  if ((rc = tc_layout_from(kernel, digits, ns, r_src, nt, r_trg, prm, L, nullptr))) return rc;
+  if ((rc = tc_layout_from(kernel, SCTLGPU_MIXED, digits, ns, r_src, nt, r_trg, prm, L, nullptr))) return rc;
   tc_sizes(L, sizes);
   if (theta_out) *theta_out = L.theta;
   if (blocks) std::copy(L.blocks.begin(), L.blocks.end(), blocks);
@@ -1005,7 +1058,7 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   T->nt = nt;
   T->df = mode == SCTLGPU_MIXED && runtime_mixed_arith(runtime_effective_digits(mode, digits)) != MIXED_ARITH_F64;
   TcLayout& L = T->L;
-  if ((rc = tc_layout_from(kernel, digits, ns, r_src, nt, r_trg, prm, L, &T->batch_max))) {
+  if ((rc = tc_layout_from(kernel, mode, digits, ns, r_src, nt, r_trg, prm, L, &T->batch_max))) {
     delete T;
     return rc;
   }
@@ -1062,7 +1115,7 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
       grid_point(C, pt, hr.data() + slot * 3);
       const bool real = k < C.npts * L.per_point;
       if (kernel == SCTLGPU_LAPLACE3D_DXU && real) hv[slot] = 1.0;  // the moment is the proxy's normal
-      if (kernel == SCTLGPU_STOKES3D_DXU && real) hn[slot * 3 + k % 3] = 1.0;  // normal e_c
+      if (kernel == SCTLGPU_STOKES3D_DXU && !L.sym && real) hn[slot * 3 + k % 3] = 1.0;  // normal e_c
     }
     hc.push_back(tc);
   }
@@ -1130,13 +1183,17 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
     return runtime_record(e);
   }
   // the plan accumulates into d_u over the whole target list (identity map: the scattered,
-  // zero-initialised form of the plan)
+  // zero-initialised form of the plan); with symmetric-density proxies their blocks form a
+  // second plan that adds to the first one's sums
   std::vector<int64_t> ident((size_t)NT);
   std::iota(ident.begin(), ident.end(), (int64_t)0);
-  rc = sctlgpu_near_plan_create(&T->plan, kernel, mode, digits, (int64_t)L.blocks.size(), L.blocks.data(), S, NT,
+  std::vector<sctlgpu_block> pb, sb;
+  for (const sctlgpu_block& b : L.blocks) (L.sym && b.src_begin >= L.n_src_slots ? sb : pb).push_back(b);
+  rc = sctlgpu_near_plan_create(&T->plan, kernel, mode, digits, (int64_t)pb.size(), pb.data(), S, NT,
                                 NT ? ident.data() : nullptr, NT);
+  if (!rc && !sb.empty())
+    rc = near_plan_create_sym(&T->plan_sym, mode, digits, (int64_t)sb.size(), sb.data(), S, NT, ident.data(), NT);
   if (rc) {
-    T->plan = nullptr;
     tc_free(T);
     return rc;
   }
@@ -1170,7 +1227,9 @@ int sctlgpu_treecode_execute(sctlgpu_treecode T, const double* v_src, double* v_
   if (bout && (e = cudaMemcpyAsync(v_out, T->h_out, bout, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
     return runtime_record(e);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return runtime_record(e);
-  return T->plan ? sctlgpu_near_plan_status(T->plan, stream) : SCTLGPU_OK;
+  int rc2 = T->plan ? sctlgpu_near_plan_status(T->plan, stream) : SCTLGPU_OK;
+  if (!rc2 && T->plan_sym) rc2 = sctlgpu_near_plan_status(T->plan_sym, stream);
+  return rc2;
 }
 
 static int tc_execute_device(sctlgpu_treecode T, const double* v_src, double* v_out, unsigned flags, void* stream) {
@@ -1199,6 +1258,7 @@ static int tc_execute_device(sctlgpu_treecode T, const double* v_src, double* v_
   p.pv = T->d_v;
   p.np = L.np;
   p.cheb = T->d_cheb;
+  p.sym = L.sym ? 1 : 0;
   TcL2PParams q{};
   q.boxes = T->d_boxes;
   q.bt0 = T->d_bt0;
@@ -1223,6 +1283,10 @@ static int tc_execute_device(sctlgpu_treecode T, const double* v_src, double* v_
   int rc = sctlgpu_near_plan_execute(T->plan, T->d_trg, T->d_r, T->d_n, T->d_v, nullptr, T->d_u, SCTLGPU_DEVICE_PTRS,
                                      stream);
   if (rc) return rc;
+  if (T->plan_sym &&
+      (rc = sctlgpu_near_plan_execute(T->plan_sym, T->d_trg, T->d_r, T->d_n, T->d_v, nullptr, T->d_u,
+                                      SCTLGPU_DEVICE_PTRS | SCTLGPU_ACCUMULATE, stream)))
+    return rc;
   e = tc_launch_l2p(q, T->TD, T->df, (int)T->n_pieces, T->batch_max, st);
   return e == cudaSuccess ? SCTLGPU_OK : runtime_record(e);
 }
@@ -1240,7 +1304,9 @@ int sctlgpu_treecode_status(sctlgpu_treecode T, void* stream) {
     const cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
     return e == cudaSuccess ? sctlgpu_device_status(stream) : runtime_record(e);
   }
-  return sctlgpu_near_plan_status(T->plan, stream);
+  int rc = sctlgpu_near_plan_status(T->plan, stream);
+  if (!rc && T->plan_sym) rc = sctlgpu_near_plan_status(T->plan_sym, stream);
+  return rc;
 }
 
 int sctlgpu_treecode_destroy(sctlgpu_treecode T) {
