@@ -286,10 +286,9 @@ int sctlgpu_near_list_destroy(sctlgpu_near_list list);
  * fmm-wrapper.txx:505-540): source coordinates and normals (double-layer
  * kernels), target coordinates; builds both trees, the interaction blocks and
  * the device-side plan.  params may be NULL: order and theta then follow
- * `digits`, leaf_max = the cost of a full grid's proxies ((order+1)^3; for the
- * Stokes double layer three proxies per point, or with double-float plans one
- * proxy per point carrying the symmetric part of its moment, costed 1.25
- * interactions), batch_max = 512 or 256, whichever leaves
+ * `digits`, leaf_max = the cost of a full grid's proxies ((order+1)^3; the
+ * Stokes double layer's proxies carry the symmetric part of their moment and
+ * cost 1.25 interactions each), batch_max = 512 or 256, whichever leaves
  * fewer interactions (512 unless 256 saves 3 %).
  * execute: v_src (ns * SrcDim, source order as given; SetDensitySL / DL) ->
  * v_out (nt * TrgDim, target order as given); flags may hold
@@ -304,7 +303,7 @@ int sctlgpu_near_list_destroy(sctlgpu_near_list list);
  * (targets, then target proxies), target clusters with proxies, 1 when the
  * traversal saves less than a quarter of Ns * Nt and evaluations run the
  * direct sum instead}, and the acceptance parameter.  layout is the host-only part of create (no device
- * needed) for SCTLGPU_MIXED: the blocks (sources index the source slots, targets the target
+ * needed): the blocks (sources index the source slots, targets the target
  * list), the source of every slot (-1 padding, -2 proxy), the target order,
  * per source cluster with proxies {slot begin, end, proxy slot begin, end,
  * grid points along x, y, z} and per target cluster with proxies {target begin,

@@ -34,7 +34,7 @@ enum { KER_LFXU = 0, KER_LDXU = 1, KER_SFXU = 2, KER_SDXU = 3 };
 // Internal: the Stokes double layer of a symmetric 3 x 3 density S per source (the treecode's
 // proxies carry the symmetric part of the moment sum_s L_k(y_s) n_s (x) f_s), u = 3/(4 pi) r
 // (r . S r) / r^5 -- records hold diag(S) as the "normal" and (2 S01, 2 S02, 2 S12) as the
-// "density".  Only the packed double-float near-batch kernel implements it.
+// "density".  Near-batch plans only (FP64, mixed FP32 and packed double-float arithmetic).
 enum { KER_SDXU_SYM = 4 };
 enum { MODE_F64 = 0, MODE_F32 = 1, MODE_MXLO = 2, MODE_MXDF = 3 };
 
@@ -126,6 +126,9 @@ template <> struct Rec<KER_SFXU, MODE_MXDF> { float xh, yh, zh, fh0, xl, yl, zl,
 template <> struct Rec<KER_SDXU, MODE_MXDF> {
   float xh, yh, zh, fh0, xl, yl, zl, fl0, fh1, fh2, fl1, fl2, nh0, nh1, nh2, p0, nl0, nl1, nl2, p1;
 };
+template <> struct Rec<KER_SDXU_SYM, MODE_F64> : Rec<KER_SDXU, MODE_F64> {};  // n: diag(S), f: 2 S_ij
+template <> struct Rec<KER_SDXU_SYM, MODE_F32> : Rec<KER_SDXU, MODE_F32> {};
+template <> struct Rec<KER_SDXU_SYM, MODE_MXDF> : Rec<KER_SDXU, MODE_MXDF> {};
 template <int KER> struct Rec<KER, MODE_MXLO> : Rec<KER, MODE_MXDF> {};
 
 // ----------------------------------------------------------------- packing
@@ -207,7 +210,7 @@ __global__ void pack_sources_kernel(int64_t ns, const Real* __restrict__ xs, con
         split_val((double)f[s * 3 + 0] * ws, r.fh0, r.fl0);
         split_val((double)f[s * 3 + 1] * ws, r.fh1, r.fl1);
         split_val((double)f[s * 3 + 2] * ws, r.fh2, r.fl2);
-        if constexpr (KER == KER_SDXU) {
+        if constexpr (KER == KER_SDXU || KER == KER_SDXU_SYM) {
           split_val((double)nrm[s * 3 + 0], r.nh0, r.nl0);
           split_val((double)nrm[s * 3 + 1], r.nh1, r.nl1);
           split_val((double)nrm[s * 3 + 2], r.nh2, r.nl2);
@@ -265,9 +268,15 @@ struct PlainPair {
     } else {
       const Real y2 = y * y;
       const Real y5 = y2 * y2 * y;
-      const Real dn = fma(d2, s.n2, fma(d1, s.n1, d0 * s.n0));
-      const Real fd = fma(d2, s.f2, fma(d1, s.f1, d0 * s.f0));
-      const Real c = fd * dn * y5;
+      Real q;
+      if constexpr (KER == KER_SDXU) {
+        const Real dn = fma(d2, s.n2, fma(d1, s.n1, d0 * s.n0));
+        const Real fd = fma(d2, s.f2, fma(d1, s.f1, d0 * s.f0));
+        q = fd * dn;
+      } else {  // r . S r: diag(S) in n, (2 S01, 2 S02, 2 S12) in f
+        q = fma(s.n0 * d0, d0, fma(s.n1 * d1, d1, fma(s.n2 * d2, d2, fma(s.f0 * d0, d1, fma(s.f1 * d0, d2, s.f2 * d1 * d2)))));
+      }
+      const Real c = q * y5;
       t.acc[0] = fma(d0, c, t.acc[0]);
       t.acc[1] = fma(d1, c, t.acc[1]);
       t.acc[2] = fma(d2, c, t.acc[2]);
@@ -330,9 +339,16 @@ struct Pair<KER, MODE_MXLO, NEWTON> {
     } else {
       const float y2 = y * y;
       const float y5 = y2 * y2 * y;
-      const float dn = fmaf(d2, s.nh2, fmaf(d1, s.nh1, d0 * s.nh0));
-      const float fd = fmaf(d2, s.fh2, fmaf(d1, s.fh1, d0 * s.fh0));
-      const float c = fd * dn * y5;
+      float q;
+      if constexpr (KER == KER_SDXU) {
+        const float dn = fmaf(d2, s.nh2, fmaf(d1, s.nh1, d0 * s.nh0));
+        const float fd = fmaf(d2, s.fh2, fmaf(d1, s.fh1, d0 * s.fh0));
+        q = fd * dn;
+      } else {  // r . S r: diag(S) in n, (2 S01, 2 S02, 2 S12) in f
+        q = fmaf(s.nh0 * d0, d0, fmaf(s.nh1 * d1, d1, fmaf(s.nh2 * d2, d2,
+                 fmaf(s.fh0 * d0, d1, fmaf(s.fh1 * d0, d2, s.fh2 * d1 * d2)))));
+      }
+      const float c = q * y5;
       kahan_add(t.acc[0], d0 * c);
       kahan_add(t.acc[1], d1 * c);
       kahan_add(t.acc[2], d2 * c);

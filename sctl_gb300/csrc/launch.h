@@ -114,9 +114,9 @@ enum { MIXED_ARITH_F32 = 0, MIXED_ARITH_DF = 1, MIXED_ARITH_F64 = 2 };
 int runtime_mixed_arith(int digits);
 
 // A near plan of the Stokes double layer with a symmetric 3 x 3 density per source (the
-// treecode's proxies, KER_SDXU_SYM): n_src holds diag(S), v_src (2 S01, 2 S02, 2 S12).  Only
-// SCTLGPU_MIXED at double-float digits (SCTLGPU_ERR_INVALID_MODE otherwise); executed,
-// queried and destroyed like any plan.
+// treecode's proxies, KER_SDXU_SYM): n_src holds diag(S), v_src (2 S01, 2 S02, 2 S12).
+// SCTLGPU_MIXED or SCTLGPU_F64 (SCTLGPU_ERR_INVALID_MODE otherwise); executed, queried and
+// destroyed like any plan.
 int near_plan_create_sym(::sctlgpu_near_plan_s** out, int mode, int digits, int64_t nblk, const void* blocks,
                          int64_t ns, int64_t nt, const int64_t* trg_map, int64_t n_out);
 

@@ -108,6 +108,9 @@ NearOps near_ops_for(int kernel) {
     case KER_LFXU: return make_near_ops<KER_LFXU, MODE, NEWTON>();
     case KER_LDXU: return make_near_ops<KER_LDXU, MODE, NEWTON>();
     case KER_SFXU: return make_near_ops<KER_SFXU, MODE, NEWTON>();
+    case KER_SDXU_SYM:  // FP64 and mixed plans only (plans with FP32 results refuse it)
+      if constexpr (MODE != MODE_F32) return make_near_ops<KER_SDXU_SYM, MODE, NEWTON>();
+      return make_near_ops<KER_SDXU, MODE, NEWTON>();
     default: return make_near_ops<KER_SDXU, MODE, NEWTON>();
   }
 }

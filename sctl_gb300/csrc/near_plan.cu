@@ -466,9 +466,7 @@ int near_plan_create_sym(::sctlgpu_near_plan_s** out, int mode, int digits, int6
                          int64_t ns, int64_t nt, const int64_t* trg_map, int64_t n_out) {
   if (!out) return SCTLGPU_ERR_NULL_POINTER;
   *out = nullptr;
-  int newton;
-  if (mode != SCTLGPU_MIXED || imode_for(mode, runtime_effective_digits(mode, digits), &newton) != NEAR_MXDF)
-    return SCTLGPU_ERR_INVALID_MODE;
+  if (mode != SCTLGPU_MIXED && mode != SCTLGPU_F64) return SCTLGPU_ERR_INVALID_MODE;
   // split table tuned for the Stokes double layer (the same targets per thread and a similar cost)
   return plan_create(out, SCTLGPU_STOKES3D_DXU, KER_SDXU_SYM, 3, 3, mode, digits, nblk,
                      static_cast<const sctlgpu_block*>(blocks), ns, nt, nullptr, 0, trg_map, n_out);

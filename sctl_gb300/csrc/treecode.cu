@@ -24,9 +24,10 @@
 //    source charges q_s: the density (single layers), the density times the
 //    normal (Laplace double layer: the moment is the proxy's normal), or
 //    normal (x) density (Stokes double layer: three proxies per point with
-//    unit normals e_c and densities M_k[c][:]; with double-float plans one proxy
-//    per point whose symmetric density sym(M_k) gives the same field, since
-//    (r.n)(r.f) = r . (n (x) f) r, evaluated by KER_SDXU_SYM in a second plan).
+//    unit normals e_c and densities M_k[c][:] would do; instead one proxy per
+//    point carries the symmetric density sym(M_k), which gives the same field
+//    since (r.n)(r.f) = r . (n (x) f) r, evaluated by KER_SDXU_SYM in a second
+//    plan).
 //  * device, per evaluation: densities gathered into slot order, moments per
 //    (cluster, 256-slot chunk) -- in double-float on the FP32 pipe when the
 //    plan's arithmetic is FP32 or double-float, else in FP64 -- reduced per
@@ -270,8 +271,8 @@ void tc_grid(TcNode& C, int order, double theta) {
 
 struct TcLayout {
   int order = 0, np = 0, npts = 0, per_point = 1;  // np, npts: the largest grid (order + 1 per dimension)
-  // Stokes double layer with double-float plans: one proxy per grid point carrying the
-  // symmetric part of its moment (evaluated by KER_SDXU_SYM, cost pw each) instead of three
+  // Stokes double layer: one proxy per grid point carrying the symmetric part of its moment
+  // (evaluated by KER_SDXU_SYM, cost pw each) instead of three with unit normals
   bool sym = false;
   double pw = 1.0;
   double theta = 0;
@@ -942,7 +943,7 @@ int tc_check_common(int kernel, int64_t ns, const double* r_src, int64_t nt, con
   return SCTLGPU_OK;
 }
 
-int tc_layout_from(int kernel, int mode, int digits, int64_t ns, const double* r_src, int64_t nt, const double* r_trg,
+int tc_layout_from(int kernel, int digits, int64_t ns, const double* r_src, int64_t nt, const double* r_trg,
                    const sctlgpu_treecode_params* prm, TcLayout& L, int* batch_max) {
   int order = prm ? prm->order : 0;
   double theta = prm ? prm->theta : 0.0;
@@ -950,9 +951,7 @@ int tc_layout_from(int kernel, int mode, int digits, int64_t ns, const double* r
   const double theta_trg = prm ? prm->theta_trg : 0.0;
   const int64_t leaf = prm ? prm->leaf_max : 0;
   const bool dual = !prm || prm->dual != 0;
-  // symmetric-density proxies where the plans run double-float (KER_SDXU_SYM has no other form)
-  const bool sym = mode == SCTLGPU_MIXED &&
-                   runtime_mixed_arith(runtime_effective_digits(mode, digits)) == MIXED_ARITH_DF;
+  const bool sym = true;  // the Stokes double layer's proxies: one symmetric density per point
   if (prm && prm->batch_max > 0) {
     if (batch_max) *batch_max = prm->batch_max;
     return tc_build_layout(kernel, ns, r_src, nt, r_trg, order, theta, theta_trg, leaf, prm->batch_max, dual, sym,
@@ -1007,7 +1006,7 @@ int sctlgpu_treecode_layout(int kernel, int64_t ns, const double* r_src, int64_t
   if (rc) return rc;
   if (!sizes) return SCTLGPU_ERR_NULL_POINTER;
   TcLayout L;
-  if ((rc = tc_layout_from(kernel, SCTLGPU_MIXED, digits, ns, r_src, nt, r_trg, prm, L, nullptr))) return rc;
+  if ((rc = tc_layout_from(kernel, digits, ns, r_src, nt, r_trg, prm, L, nullptr))) return rc;
   tc_sizes(L, sizes);
   if (theta_out) *theta_out = L.theta;
   if (blocks) std::copy(L.blocks.begin(), L.blocks.end(), blocks);
@@ -1058,7 +1057,7 @@ int sctlgpu_treecode_create(sctlgpu_treecode* out, int kernel, int mode, int dig
   T->nt = nt;
   T->df = mode == SCTLGPU_MIXED && runtime_mixed_arith(runtime_effective_digits(mode, digits)) != MIXED_ARITH_F64;
   TcLayout& L = T->L;
-  if ((rc = tc_layout_from(kernel, mode, digits, ns, r_src, nt, r_trg, prm, L, &T->batch_max))) {
+  if ((rc = tc_layout_from(kernel, digits, ns, r_src, nt, r_trg, prm, L, &T->batch_max))) {
     delete T;
     return rc;
   }
