@@ -17,7 +17,7 @@
 using namespace sctlgpu;
 
 struct sctlgpu_near_plan_s {
-  int kernel = 0, mode = 0, digits = -1, imode = 0, newton = 0, K1 = 1, ND = 0, SD = 1;
+  int kernel = 0, mode = 0, digits = -1, imode = 0, newton = 0, K1 = 1, ND = 0;
   NearOps ops;
   int64_t nblk = 0, ns = 0, nt = 0, n_out = 0, n_items = 0, pairs = 0;
   bool has_map = false;

@@ -771,7 +771,8 @@ cudaError_t tc_launch_moments(TcMomParams p, int n_items, int pass_items, int n_
 // its target clusters A with proxies (its batch and the batch's ancestors),
 // sum_k L_k(x) u[A's proxy k] -- the interpolation of the potentials the plan accumulated at
 // A's Chebyshev points -- and is written (or added) to out[perm[k]].  One CTA per batch, one
-// warp per target: the lanes split the cluster's grid points, in double-float (DF) or FP64.
+// warp per target: the lanes split the rows (i, j) of the cluster's grid, in double-float (DF) or
+// FP64.
 struct TcTrgBox {
   double lo[3], inv[3];
   int64_t proxy;  // first proxy entry of the target list
