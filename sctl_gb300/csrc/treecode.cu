@@ -474,15 +474,31 @@ int tc_build_layout(int kernel, int64_t ns, const double* r_src, int64_t nt, con
   std::sort(bl.begin(), bl.end(), [](const Blk& a, const Blk& b) {
     return a.t0 != b.t0 ? a.t0 < b.t0 : (a.tn != b.tn ? a.tn < b.tn : a.s0 < b.s0);
   });
-  L.blocks.clear();
-  L.pp = L.approx = 0;
+  std::vector<Blk> merged;
   for (size_t k = 0; k < bl.size();) {
     Blk cur = bl[k];
     size_t j = k + 1;
-    const bool direct = cur.t0 < nt && cur.s0 < L.n_src_slots;
     while (j < bl.size() && bl[j].t0 == cur.t0 && bl[j].tn == cur.tn && bl[j].s0 == cur.s1 &&
            (bl[j].s0 < L.n_src_slots) == (cur.s0 < L.n_src_slots))
       cur.s1 = bl[j++].s1;
+    merged.push_back(cur);
+    k = j;
+  }
+  // then blocks over the same sources whose target ranges adjoin (sibling batches or target
+  // clusters that accepted the same source nodes): fewer, fuller blocks (the lanes of an item
+  // take up to 128 or 256 targets; batches average 130-270)
+  std::sort(merged.begin(), merged.end(), [](const Blk& a, const Blk& b) {
+    return a.s0 != b.s0 ? a.s0 < b.s0 : (a.s1 != b.s1 ? a.s1 < b.s1 : a.t0 < b.t0);
+  });
+  L.blocks.clear();
+  L.pp = L.approx = 0;
+  for (size_t k = 0; k < merged.size();) {
+    Blk cur = merged[k];
+    size_t j = k + 1;
+    while (j < merged.size() && merged[j].s0 == cur.s0 && merged[j].s1 == cur.s1 &&
+           merged[j].t0 == cur.t0 + cur.tn && (merged[j].t0 < nt) == (cur.t0 < nt))
+      cur.tn += merged[j++].tn;
+    const bool direct = cur.t0 < nt && cur.s0 < L.n_src_slots;
     L.blocks.push_back({cur.s0, cur.s1 - cur.s0, cur.t0, cur.tn});
     (direct ? L.pp : L.approx) += (cur.s1 - cur.s0) * cur.tn;
     k = j;

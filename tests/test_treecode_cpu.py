@@ -81,14 +81,16 @@ def test_layout_covers_every_pair_once(kind, kernel, dual):
     direct = approx = 0
     for b in blocks:
         s0, sn, t0, tn = (int(v) for v in b)
-        if t0 < nt:
+        if t0 < nt:  # sorted targets (adjacent batches merged)
             assert t0 + tn <= nt
-            ta, tb_ = t0, t0 + tn
-        else:
-            c = tprox[t0]
-            assert tn == c[4:7].prod()
-            ta, tb_ = int(c[0]), int(c[1])
-        tset = np.arange(ta, tb_)
+            tgroups = [np.arange(t0, t0 + tn)]
+        else:  # target clusters' proxies (adjacent clusters merged)
+            tgroups, pos = [], t0
+            while pos < t0 + tn:
+                c = tprox[pos]
+                tgroups.append(np.arange(c[0], c[1]))
+                pos = int(c[3])
+            assert pos == t0 + tn
         if s0 < nsrc:
             assert s0 + sn <= nsrc
             src = slot_src[s0:s0 + sn]
@@ -102,15 +104,19 @@ def test_layout_covers_every_pair_once(kind, kernel, dual):
                 assert groups[-1].size > c[4:7].prod() * per_point
                 pos = int(c[3])
             assert pos == s0 + sn
-        for g in groups:
-            cnt[np.ix_(tset, g)] += 1
+        for tset in tgroups:
             cb, rb = _box(xt[trg_order[tset]])
-            if s0 >= nsrc:  # a source cluster's proxies: the two boxes are separated
-                cc, rc = _box(xs[g])
-                assert rb + rc < theta * np.linalg.norm(cb - cc) * (1 + 1e-12)
-            elif t0 >= nt:  # target proxies against sources (adjacent source nodes merged): every
-                # source is beyond r_t / theta of the target cluster's centre
-                assert rb < theta * np.linalg.norm(xs[g] - cb, axis=1).min() * (1 + 1e-12)
+            for g in groups:
+                cnt[np.ix_(tset, g)] += 1
+                if s0 >= nsrc:
+                    cc, rc = _box(xs[g])
+                    if t0 >= nt:  # cluster-cluster: the two boxes are separated
+                        assert rb + rc < theta * np.linalg.norm(cb - cc) * (1 + 1e-12)
+                    else:  # merged batches against a source cluster: every target beyond r_s / theta
+                        assert rc < theta * np.linalg.norm(xt[trg_order[tset]] - cc, axis=1).min() * (1 + 1e-12)
+                elif t0 >= nt:  # target proxies against sources (adjacent source nodes merged): every
+                    # source is beyond r_t / theta of the target cluster's centre
+                    assert rb < theta * np.linalg.norm(xs[g] - cb, axis=1).min() * (1 + 1e-12)
         if t0 < nt and s0 < nsrc:
             direct += sn * tn
         else:
