@@ -171,6 +171,28 @@ def test_stokes_double_layer_symmetric_proxies(cuda):
     assert O.rel_l2(b, a) < 1e-15
 
 
+def test_treecode_coincident_sources(cuda):
+    """Half the sources on one point outside the target ball: their leaf has a one-point grid
+    (zero extent in every dimension), whose single proxy carries the leaf's whole moment exactly."""
+    torch = cuda
+    rng = np.random.default_rng(12)
+    for k in (1, 3):
+        d = W.sphere_ball(1 << 17, 1 << 13, k, seed=60 + k)
+        xs, xn = d["r_src"].copy(), d["n_src"].copy()
+        xs[: 1 << 16] = [2.5, 0.5, 0.25]
+        xn[: 1 << 16] = rng.standard_normal((1 << 16, 3))
+        xn /= np.linalg.norm(xn, axis=1, keepdims=True)
+        lay = TC.layout(k, xs, d["r_trg"], digits=10)
+        assert np.any(lay[4][:, 4:7].prod(1) == 1), "a one-point source cluster"
+        tc = TC.Treecode(k, xs, d["r_trg"], n_src=xn, digits=10)
+        assert tc.info()["direct_fallback"] == 0
+        u = tc.eval(dev(torch, d["v_src"])).cpu().numpy()
+        td = 3 if k == 3 else 1
+        sub = np.arange(0, 1 << 13, 16)
+        ref = O.eval(k, d["r_trg"][sub], xs, xn, d["v_src"])
+        assert O.rel_l2(u.reshape(-1, td)[sub].reshape(-1), ref) < 1e-10, k
+
+
 def test_treecode_falls_back_to_the_direct_sum(cuda):
     """A geometry where the traversal would keep over three quarters of Ns * Nt: evaluations run
     the direct sum, identical to sctlgpu_eval on the same arrays."""

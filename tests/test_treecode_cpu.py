@@ -30,6 +30,12 @@ def _points(kind, ns, nt, seed):
         xs = c[rng.integers(0, 5, ns)] + 1e-2 * rng.standard_normal((ns, 3))
         xt = c[rng.integers(0, 5, nt)] + 3e-2 * rng.standard_normal((nt, 3))
         return xs, xt
+    if kind == "coincident":  # half the sources on one point: a cluster with a one-point grid
+        c = rng.standard_normal((5, 3))
+        xs = c[rng.integers(0, 5, ns)] + 1e-2 * rng.standard_normal((ns, 3))
+        xs[: ns // 2] = c[0] + 0.5
+        xt = c[rng.integers(0, 5, nt)] + 3e-2 * rng.standard_normal((nt, 3))
+        return xs, xt
     # flat sheet (z = 0) with targets above it
     xs = np.c_[rng.uniform(-1, 1, (ns, 2)), np.zeros(ns)]
     xt = np.c_[rng.uniform(-1, 1, (nt, 2)), rng.uniform(0.01, 1, nt)]
@@ -41,7 +47,7 @@ def _box(p):
     return 0.5 * (lo + hi), 0.5 * np.linalg.norm(hi - lo)
 
 
-@pytest.mark.parametrize("kind", ["sphere_ball", "clusters", "sheet"])
+@pytest.mark.parametrize("kind", ["sphere_ball", "clusters", "sheet", "coincident"])
 @pytest.mark.parametrize("kernel", [0, 3])
 @pytest.mark.parametrize("dual", [True, False])
 def test_layout_covers_every_pair_once(kind, kernel, dual):
@@ -71,10 +77,13 @@ def test_layout_covers_every_pair_once(kind, kernel, dual):
         src = slot_src[c[0]:c[1]]
         p = xs[src[src >= 0]]
         ext = p.max(0) - p.min(0)
-        assert c[4 + int(np.argmax(ext))] == order + 1
+        if ext.max() > 0:
+            assert c[4 + int(np.argmax(ext))] == order + 1
         assert np.all(c[4:7][ext == 0] == 1)
         if kind == "sheet":
             assert c[6] == 1
+    if kind == "coincident":  # the coincident sources' leaf is approximated by a single proxy
+        assert np.any(clusters[:, 4:7].prod(1) == 1)
     sprox = {int(c[2]): c for c in clusters}
     tprox = {int(c[2]): c for c in tclusters}
     cnt = np.zeros((nt, ns), np.uint8)  # (sorted target, source) coverage
