@@ -285,7 +285,7 @@ int sctlgpu_near_list_destroy(sctlgpu_near_list list);
  * create: the geometry (host arrays; the reference's SetSrcCoord / SetTrgCoord,
  * fmm-wrapper.txx:505-540): source coordinates and normals (double-layer
  * kernels), target coordinates; builds both trees, the interaction blocks and
- * the device-side plan.  params may be NULL: order and theta then follow
+ * the device-side plans.  params may be NULL: order and theta then follow
  * `digits`, leaf_max = the cost of a full grid's proxies ((order+1)^3; the
  * Stokes double layer's proxies carry the symmetric part of their moment and
  * cost 1.25 interactions each), batch_max = 512 or 256, whichever leaves
@@ -313,7 +313,7 @@ int sctlgpu_near_list_destroy(sctlgpu_near_list list);
 typedef struct sctlgpu_treecode_params {
   double theta;  /* a pair of clusters is separated when (r_trg + r_src) < theta * distance; <= 0: from digits */
   int order;     /* interpolation degree per dimension, 1..15; <= 0: from digits */
-  int leaf_max;  /* sources per leaf; <= 0: the proxy slots of a full grid */
+  int leaf_max;  /* sources per leaf; <= 0: the cost of a full grid's proxies */
   int batch_max; /* targets per batch, <= 2048; <= 0: 512 or 256 (fewer interactions) */
   int dual;      /* nonzero: target clusters interpolate too (cluster-cluster interactions, a downward pass);
                     0: particle-cluster only */
