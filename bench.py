@@ -564,10 +564,18 @@ def treecode_section(torch, n=1 << 20):
             setup_s = time.perf_counter() - t0
             t_tc = _ev_ms(torch, lambda: tc.eval(dv["f"], out=out), reps=2)
             err = O.rel_l2(out.cpu().numpy().reshape(nt, td)[sub].reshape(-1), ref)
+            # end to end from host arrays (densities in, potentials out, synchronous)
+            fh, uh = np.ascontiguousarray(f, np.float64).reshape(-1), np.zeros(nt * td)
+            t_host = 1e30
+            for _ in range(2):
+                t0 = time.perf_counter()
+                tc.eval_host(fh, out=uh)
+                t_host = min(t_host, (time.perf_counter() - t0) * 1e3)
             info = tc.info()
             tc.close()
             r[f"digits{digits}"] = {
                 "direct_ms": t_direct, "direct_rel_l2": err_direct, "treecode_ms": t_tc, "treecode_rel_l2": err,
+                "treecode_host_arrays_ms": t_host,
                 "speedup": t_direct / t_tc, "setup_s": setup_s, "order": info["order"], "theta": info["theta"],
                 "interactions_vs_direct": (info["direct_interactions"] + info["proxy_interactions"])
                 / info["direct_sum_interactions"], "clusters": info["clusters"], "blocks": info["blocks"]}

@@ -7,7 +7,7 @@ fmm-wrapper.txx:854-1038; Eval at :542-549), for the four hot-path kernels.
 
 The geometry calls play SetSrcCoord / SetTrgCoord (fmm-wrapper.txx:505-540):
 they build both trees and the interaction blocks once; `eval` is
-SetDensitySL/DL + Eval on the device.  Accuracy follows `digits` (interpolation
+SetDensitySL/DL + Eval on the device, `eval_host` the same from host arrays.  Accuracy follows `digits` (interpolation
 degree and acceptance parameter), or explicit `order` / `theta`.
 """
 from __future__ import annotations
@@ -72,6 +72,23 @@ class Treecode:
         flags = capi.DEVICE_PTRS | (capi.ACCUMULATE if accumulate else 0)
         rc = capi.load().sctlgpu_treecode_execute(self._h, v.data_ptr() if v.numel() else None,
                                                   out.data_ptr() if out.numel() else None, flags, stream)
+        capi.check(rc, "sctlgpu_treecode_execute")
+        return out
+
+    def eval_host(self, v_src, out=None, accumulate=False):
+        """The same from host arrays (ParticleFMM's Eval on SCTL vectors): densities copied in and
+        potentials copied out by the library, synchronously; numpy float64 in and out."""
+        v = np.ascontiguousarray(v_src, dtype=np.float64).reshape(-1)
+        if v.size != self.ns * self.sd:
+            raise ValueError("v_src must hold ns * SrcDim entries")
+        if out is None:
+            out = np.zeros(self.nt * self.td)
+            accumulate = False
+        if out.dtype != np.float64 or not out.flags.c_contiguous or out.size != self.nt * self.td:
+            raise ValueError("out must be a contiguous float64 array of nt * TrgDim entries")
+        flags = capi.ACCUMULATE if accumulate else 0
+        rc = capi.load().sctlgpu_treecode_execute(self._h, v.ctypes.data if v.size else None,
+                                                  out.ctypes.data if out.size else None, flags, None)
         capi.check(rc, "sctlgpu_treecode_execute")
         return out
 

@@ -77,6 +77,11 @@ def test_treecode_accumulate_and_new_densities(cuda):
     out = u1.clone()
     tc.eval(v2, out=out, accumulate=True)
     assert torch.allclose(out, u1 + u2, rtol=0, atol=1e-13 * float(out.abs().max()))
+    # host arrays (ParticleFMM's Eval on SCTL vectors): the same potentials, and accumulation
+    uh = tc.eval_host(d["v_src"])
+    assert np.abs(uh - u1.cpu().numpy()).max() <= 1e-14 * np.abs(uh).max()
+    tc.eval_host(np.asarray(v2.cpu()), out=uh, accumulate=True)
+    assert np.abs(uh - (u1 + u2).cpu().numpy()).max() <= 1e-13 * np.abs(uh).max()
     # linearity of the whole pipeline (moments, proxies, direct blocks)
     u3 = tc.eval(2.0 * v1 - v2)  # to the arithmetic's rounding (FP32 at digits 6)
     assert float((u3 - (2 * u1 - u2)).norm() / u3.norm()) < 1e-6
