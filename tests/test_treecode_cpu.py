@@ -177,3 +177,19 @@ def test_layout_empty_and_single_leaf():
     assert s["blocks"] == 0 and s["slots"] == 0
     s, blocks, *_ = TC.layout(0, xs, np.zeros((0, 3)))
     assert s["blocks"] == 0
+
+
+@pytest.mark.parametrize("kernel", [0, 1, 2, 3])
+def test_numpy_restatement_matches_the_direct_sum(kernel):
+    """The treecode restated in numpy from its host layout (moments, every block, the downward
+    pass; tests/treecode_numpy.py) against the direct-sum oracle: the algorithm the layout
+    describes is accurate to its interpolation degree."""
+    import treecode_numpy as TN
+    from oracle import oracle as O
+    d = W.sphere_ball(1 << 13, 1 << 13, kernel, seed=70 + kernel)
+    xn = d["n_src"] if kernel in (1, 3) else None
+    u, s = TN.evaluate(kernel, d["r_src"], xn, d["v_src"], d["r_trg"], order=4, theta=0.5, leaf_max=128,
+                       batch_max=64, digits=10)
+    assert s["proxy_interactions"] > 0 and s["target_clusters"] > 0
+    ref = O.eval(kernel, d["r_trg"], d["r_src"], xn, d["v_src"])
+    assert O.rel_l2(u, ref) < 1e-3  # degree 4
