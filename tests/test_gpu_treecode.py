@@ -248,20 +248,22 @@ def test_treecode_torus_far_field(cuda):
         assert err < 10.0 ** -digits
 
 
+@pytest.mark.parametrize("mode,digits,tol", [("f64", -1, 1e-12), ("mixed", 10, 1e-10)])
 @pytest.mark.parametrize("k", [1, 3])
-def test_treecode_equals_its_numpy_restatement(cuda, k):
-    """The FP64 treecode against its numpy restatement from the host layout (moments, every
-    block, the downward pass; tests/treecode_numpy.py) at degree 4, where the approximation
-    error (~1e-4) is far above both evaluations' rounding: agreement to 1e-12 pins the device
-    implementation to the algorithm the layout describes."""
+def test_treecode_equals_its_numpy_restatement(cuda, k, mode, digits, tol):
+    """The treecode against its numpy restatement from the host layout (moments, every block,
+    the downward pass; tests/treecode_numpy.py) at degree 4, where the approximation error
+    (~1e-6) is far above both evaluations' rounding: agreement to 1e-12 (FP64) or 1e-10
+    (double-float moments, interactions and downward pass) pins the device implementation to
+    the algorithm the layout describes."""
     import treecode_numpy as TN
     torch = cuda
     d = W.sphere_ball(1 << 14, 1 << 13, k, seed=80 + k)
     kw = dict(order=4, theta=0.45, leaf_max=128, batch_max=64)
     want, s = TN.evaluate(k, d["r_src"], d["n_src"], d["v_src"], d["r_trg"], digits=-1, **kw)
     assert s["target_clusters"] > 0 and s["clusters"] > 0 and s["direct_fallback"] == 0
-    tc = TC.Treecode(k, d["r_src"], d["r_trg"], n_src=d["n_src"], digits=-1, mode="f64", **kw)
+    tc = TC.Treecode(k, d["r_src"], d["r_trg"], n_src=d["n_src"], digits=digits, mode=mode, **kw)
     got = tc.eval(dev(torch, d["v_src"])).cpu().numpy()
-    assert O.rel_l2(got, want) < 1e-12
+    assert O.rel_l2(got, want) < tol
     ref = O.eval(k, d["r_trg"], d["r_src"], d["n_src"], d["v_src"])
-    assert 1e-8 < O.rel_l2(got, ref) < 1e-2  # the approximation itself is far from exact
+    assert 1e-8 < O.rel_l2(got, ref) < 1e-4  # the approximation itself is far from exact
